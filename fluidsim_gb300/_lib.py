@@ -1,0 +1,109 @@
+"""ctypes binding of ``libgbspec.so`` (C ABI declared in ``include/gbspec.h``).
+
+The library is the only compute path: if it cannot be loaded, every call
+raises ``ImportError``; there is no CPU fallback.
+"""
+
+import ctypes
+import threading
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libgbspec.so"
+
+GBS_OK = 0
+GBS_EINVAL = -22
+GBS_ENOMEM = -12
+GBS_ECUDA = -5
+GBS_ENAN = -33
+GBS_F32 = 0
+GBS_F64 = 1
+
+EXPORTED = (
+    "gbs_last_error", "gbs_version", "gbs_fft_plan_create",
+    "gbs_fft_plan_destroy", "gbs_fft_r2c", "gbs_fft_c2r", "gbs_ns_create",
+    "gbs_ns_destroy", "gbs_ns_tendencies", "gbs_ns_step_rk4",
+    "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
+    "gbs_ns_spectrum_size", "gbs_ns_spectrum",
+)
+
+
+class NSParams(ctypes.Structure):
+    """Mirror of ``gbs_ns_params``."""
+
+    _fields_ = [
+        ("ndim", ctypes.c_int),
+        ("nx", ctypes.c_int64), ("ny", ctypes.c_int64), ("nz", ctypes.c_int64),
+        ("Lx", ctypes.c_double), ("Ly", ctypes.c_double), ("Lz", ctypes.c_double),
+        ("nu_2", ctypes.c_double), ("nu_4", ctypes.c_double),
+        ("nu_8", ctypes.c_double), ("nu_m4", ctypes.c_double),
+        ("beta", ctypes.c_double), ("f", ctypes.c_double),
+        ("has_f", ctypes.c_int),
+        ("kcut_x", ctypes.c_int64), ("kcut_y", ctypes.c_int64),
+        ("kcut_z", ctypes.c_int64),
+        ("dtype", ctypes.c_int),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _declare(lib):
+    P = ctypes.c_void_p
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    I64P = ctypes.POINTER(ctypes.c_int64)
+    DP = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "gbs_last_error": (ctypes.c_char_p, []),
+        "gbs_version": (ctypes.c_char_p, []),
+        "gbs_fft_plan_create": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.c_int, ctypes.c_int, PP]),
+        "gbs_fft_plan_destroy": (ctypes.c_int, [P]),
+        "gbs_fft_r2c": (ctypes.c_int, [P, P, P, P]),
+        "gbs_fft_c2r": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
+        "gbs_ns_create": (ctypes.c_int, [ctypes.POINTER(NSParams), PP]),
+        "gbs_ns_destroy": (ctypes.c_int, [P]),
+        "gbs_ns_tendencies": (ctypes.c_int, [P, P, P, P]),
+        "gbs_ns_step_rk4": (ctypes.c_int, [P, P, DP, DP, ctypes.c_int, P]),
+        "gbs_ns_max_velocity": (ctypes.c_int, [P, P, DP, P]),
+        "gbs_cfl_update": (ctypes.c_double, [ctypes.c_double] * 4),
+        "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),
+        "gbs_ns_spectrum_size": (ctypes.c_int, [P, I64P]),
+        "gbs_ns_spectrum": (ctypes.c_int, [P, P, DP, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def load(build_if_missing=True):
+    """Return the loaded library (building it in tree once if absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not LIB_PATH.exists() and build_if_missing:
+            from .build import build
+            build()
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -m fluidsim_gb300.build`"
+            )
+        lib = ctypes.CDLL(str(LIB_PATH))
+        _declare(lib)
+        _lib = lib
+        return lib
+
+
+def check(rc, what=""):
+    """Map a GBS_E* return code to the exception the reference raises."""
+    if rc == GBS_OK:
+        return
+    msg = _lib.gbs_last_error().decode(errors="replace") if _lib else ""
+    text = f"{what}: {msg}" if what else msg
+    if rc in (GBS_EINVAL, GBS_ENAN):
+        raise ValueError(text)
+    if rc == GBS_ENOMEM:
+        raise MemoryError(text)
+    raise RuntimeError(f"{text} (code {rc})")

@@ -1,0 +1,1028 @@
+// Fused pseudo-spectral RK4 stages for ns2d / ns3d.
+//
+// One evaluation of the nonlinear tendencies plus the RK4 stage update is
+// five kernels (ns3d; ns2d has the same shape with one axis less):
+//   A  inverse z pass: read v_hat, form omega_hat = i k x v_hat on the fly,
+//      transform the 6 fields along z                       (3 in, 6 out)
+//   -  inverse y pass on the 6 fields                       (6 in, 6 out)
+//   B  x pass: C2R of the 6 rows, v x omega in shared memory, R2C of the 3
+//      products; no physical field is ever written to HBM   (6 in, 3 out)
+//   -  forward y pass on the 3 products                     (3 in, 3 out)
+//   C  forward z pass, 1/N, P_perp projection, dealiasing and the RK4
+//      stage update (or the plain tendency / final state)   (3 + state)
+// Reference: fluidsim/solvers/ns3d/solver.py:180-263,
+// fluidsim/solvers/ns2d/solver.py:33-39,111-194,
+// fluidsim/base/time_stepping/pseudo_spect.py:798-984.
+#include <cmath>
+#include <new>
+
+#include "gbs_internal.cuh"
+
+namespace gbs {
+
+extern __shared__ __align__(16) unsigned char g_smem_ns[];
+
+template <typename T> int make_twiddles(cplx<T>* tw, int n, cudaStream_t st);
+template <typename T, int DIR>
+int launch_col(const cplx<T>* in, cplx<T>* out, int n, int ncols, int nouter,
+               int nfields, int64_t es, int64_t os, int64_t fs,
+               const cplx<T>* tw, T scale, cudaStream_t st);
+
+// Geometry and physics constants passed by value to every kernel.
+struct NSK {
+  int nx, ny, nz, nkx, M;
+  int kcx, kcy, kcz;
+  double dkx, dky, dkz;
+  double nu2, nu4, nu8, num4;
+  double beta, f;
+  int has_f;
+  double inv_n;
+  double k2_hypo0;  // K2 at (iz, iy, ix) = (0, 0, 1): f_d_hypo[0,..,0] source
+  int TX, L, LP;
+};
+
+// RK4 stage selector for kernel C.
+enum Mode { kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4 };
+
+struct RKArgs {
+  const void* S;  // state (read) for kRK0..kRK2
+  void* Sout;     // state (write) for kRK3
+  void* tmp;      // _state_spect_tmp
+  void* tmp1;     // _state_spect_tmp1
+  void* tend;     // output for kTend
+  double dt;
+  int* nan_flag;
+};
+
+__device__ __forceinline__ bool removed(const NSK& q, int ix, int ky, int kz) {
+  return ix >= q.kcx || iabs(ky) >= q.kcy || iabs(kz) >= q.kcz;
+}
+
+// sigma(k) = f_d + f_d_hypo, fluidsim/base/solvers/pseudo_spect.py:166-191
+template <typename T>
+__device__ __forceinline__ T freq_lin(const NSK& q, T k2, bool k0) {
+  T fd = q.nu2 > 0 ? T(q.nu2) * k2 : T(0);
+  if (q.nu4 > 0) fd += T(q.nu4) * (k2 * k2);
+  if (q.nu8 > 0) {
+    T k4 = k2 * k2;
+    fd += T(q.nu8) * (k4 * k4);
+  }
+  if (q.num4 != 0) {
+    T k2n0 = k0 ? T(q.k2_hypo0) : k2;
+    fd += T(q.num4) / (k2n0 * k2n0);
+  }
+  return fd;
+}
+
+__device__ __forceinline__ double dexp(double x) { return exp(x); }
+__device__ __forceinline__ float dexp(float x) { return expf(x); }
+
+// RK4 stage update at one mode, pseudo_spect.py:898-984 (same evaluation
+// order as the numpy expressions there).
+template <typename C, typename T>
+__device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
+                                         C N, T sigma) {
+  const T dt = T(a.dt);
+  C* tmp = static_cast<C*>(a.tmp);
+  C* tmp1 = static_cast<C*>(a.tmp1);
+  if (mode == kRK0) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c6 = dt / T(6), c2 = dt / T(2);
+    tmp[i] = cscale(mk<C>(S.x + c6 * N.x, S.y + c6 * N.y), E);
+    tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
+  } else if (mode == kRK1) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c2 = dt / T(2);
+    C t = tmp[i];
+    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1[i] = mk<C>(S.x * E2 + c2 * N.x, S.y * E2 + c2 * N.y);
+  } else if (mode == kRK2) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c1 = dt * E2;
+    C t = tmp[i];
+    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void block_max3(T a, T b, T c,
+                                           unsigned long long* dst) {
+  __shared__ double red[3][32];
+  double v[3] = {(double)a, (double)b, (double)c};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o; o >>= 1) v[k] = fmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if (lane == 0) red[k][w] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double x = lane < nw ? red[k][lane] : 0.0;
+      for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+      if (lane == 0) atomicMax(dst + k, (unsigned long long)__double_as_longlong(x));
+    }
+  }
+}
+
+// C2R pre-processing of row element j (see k_row_c2r in gbs_fft.cu).
+template <typename C>
+__device__ __forceinline__ C c2r_pre(const C* row, int j, int M, const C* twx) {
+  C a = row[j];
+  C b = cconj(row[M - j]);
+  if (j == 0) { a.y = 0; b.y = 0; }
+  C s = cadd(a, b), d = csub(a, b);
+  C wd = cmulc(d, twx[j]);
+  return mk<C>(s.x - wd.y, s.y + wd.x);
+}
+
+template <typename C, typename T>
+__device__ __forceinline__ C r2c_post(const C* buf, int k, int M, int LP,
+                                      int line, const C* twx) {
+  C a = buf[(k == M ? 0 : k) * LP + line];
+  C b = cconj(buf[(k == 0 ? 0 : M - k) * LP + line]);
+  C s = cadd(a, b), d = csub(a, b);
+  C wd = cmul(twx[k], d);
+  const T h = T(0.5);
+  return mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+}
+
+// =====================================================================  ns3d
+// A: inverse z pass with the curl.  grid (tiles of TX along x, ny).
+// lines: field f (0..2 = v, 3..5 = omega) x column c -> line f*TX + c.
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k3_inv_z_curl(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
+              const cplx<T>* __restrict__ twz) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.nz * q.LP;
+  const int TX = q.TX, LP = q.LP;
+  const int c0 = blockIdx.x * TX, iy = blockIdx.y;
+  const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  const int64_t plane = (int64_t)q.ny * q.nkx;
+  const T ky = T(q.dky * kadim(iy, q.ny));
+  for (int idx = threadIdx.x; idx < q.nz * TX; idx += blockDim.x) {
+    const int c = idx % TX, iz = idx / TX, ix = c0 + c;
+    C v[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) v[f] = mk<C>(0, 0);
+    if (ix < q.nkx) {
+      const int64_t i = iz * plane + (int64_t)iy * q.nkx + ix;
+      const C vx = S[i], vy = S[i + nK], vz = S[i + 2 * nK];
+      const T kx = T(q.dkx * ix), kz = T(q.dkz * kadim(iz, q.nz));
+      v[0] = vx;
+      v[1] = vy;
+      v[2] = vz;
+      // omega = i (k x v)   (fluidfft rotfft_from_vecfft)
+      C a = mk<C>(ky * vz.x - kz * vy.x, ky * vz.y - kz * vy.y);
+      C b = mk<C>(kz * vx.x - kx * vz.x, kz * vx.y - kx * vz.y);
+      C d = mk<C>(kx * vy.x - ky * vx.x, kx * vy.y - ky * vx.y);
+      v[3] = mk<C>(-a.y, a.x);
+      v[4] = mk<C>(-b.y, b.x);
+      v[5] = mk<C>(-d.y, d.x);
+      if (q.has_f && ix == 0 && iy == 0 && iz == 0) v[5].x += T(q.f);
+    }
+#pragma unroll
+    for (int f = 0; f < 6; ++f) buf[iz * LP + f * TX + c] = v[f];
+  }
+  __syncthreads();
+  fft_tile<+1, kTPT>(buf, buf2, q.nz, 6 * TX, LP, twz, 1);
+  for (int idx = threadIdx.x; idx < q.nz * TX; idx += blockDim.x) {
+    const int c = idx % TX, iz = idx / TX, ix = c0 + c;
+    if (ix >= q.nkx) continue;
+    const int64_t i = iz * plane + (int64_t)iy * q.nkx + ix;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) W[i + f * nK] = buf[iz * LP + f * TX + c];
+  }
+}
+
+// B: x pass.  Rows (iz, iy); L rows per CTA; lines f*L + l (f < 6).
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k3_x_product(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, NSK q,
+             const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.M * q.LP;
+  const int L = q.L, LP = q.LP, M = q.M, nkx = q.nkx;
+  const int64_t nrows = (int64_t)q.nz * q.ny;
+  const int64_t nK = nrows * nkx;
+  const int64_t r0 = (int64_t)blockIdx.x * L;
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int j = idx % M, l = idx / M;
+    const bool ok = r0 + l < nrows;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      C z = mk<C>(0, 0);
+      if (ok) z = c2r_pre(W + f * nK + (r0 + l) * nkx, j, M, twx);
+      buf[j * LP + f * L + l] = z;
+    }
+  }
+  __syncthreads();
+  fft_tile<+1, kTPT>(buf, buf2, M, 6 * L, LP, twx, 2);
+  T mx = 0, my = 0, mz = 0;
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int j = idx % M, l = idx / M;
+    C* p = buf + j * LP + l;
+    const C vx = p[0], vy = p[L], vz = p[2 * L];
+    const C ox = p[3 * L], oy = p[4 * L], oz = p[5 * L];
+    // fluidfft vector_product(v, omega) = v x omega, both packed reals
+    p[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
+    p[L] = mk<C>(vz.x * ox.x - vx.x * oz.x, vz.y * ox.y - vx.y * oz.y);
+    p[2 * L] = mk<C>(vx.x * oy.x - vy.x * ox.x, vx.y * oy.y - vy.y * ox.y);
+    if (vmax && r0 + l < nrows) {
+      mx = fmax(mx, fmax(fabs(vx.x), fabs(vx.y)));
+      my = fmax(my, fmax(fabs(vy.x), fabs(vy.y)));
+      mz = fmax(mz, fmax(fabs(vz.x), fabs(vz.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, mz, vmax);
+  fft_tile<-1, kTPT>(buf, buf2, M, 3 * L, LP, twx, 2);
+  for (int idx = threadIdx.x; idx < L * nkx; idx += blockDim.x) {
+    const int k = idx % nkx, l = idx / nkx;
+    if (r0 + l >= nrows) continue;
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+      F[f * nK + (r0 + l) * nkx + k] = r2c_post<C, T>(buf, k, M, LP, f * L + l, twx);
+  }
+}
+
+// C: forward z pass + 1/N + projection + dealiasing + RK4 stage.
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k3_fwd_z_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ twz,
+            int mode, RKArgs a) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.nz * q.LP;
+  const int TX = q.TX, LP = q.LP;
+  const int c0 = blockIdx.x * TX, iy = blockIdx.y;
+  const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  const int64_t plane = (int64_t)q.ny * q.nkx;
+  for (int idx = threadIdx.x; idx < q.nz * TX; idx += blockDim.x) {
+    const int c = idx % TX, iz = idx / TX, ix = c0 + c;
+    const int64_t i = iz * plane + (int64_t)iy * q.nkx + ix;
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+      buf[iz * LP + f * TX + c] = ix < q.nkx ? F[i + f * nK] : mk<C>(0, 0);
+  }
+  __syncthreads();
+  fft_tile<-1, kTPT>(buf, buf2, q.nz, 3 * TX, LP, twz, 1);
+  const int kyi = kadim(iy, q.ny);
+  const T ky = T(q.dky * kyi);
+  const T inv_n = T(q.inv_n);
+  for (int idx = threadIdx.x; idx < q.nz * TX; idx += blockDim.x) {
+    const int c = idx % TX, iz = idx / TX, ix = c0 + c;
+    if (ix >= q.nkx) continue;
+    const int64_t i = iz * plane + (int64_t)iy * q.nkx + ix;
+    const int kzi = kadim(iz, q.nz);
+    const T kx = T(q.dkx * ix), kz = T(q.dkz * kzi);
+    const T k2 = kx * kx + ky * ky + kz * kz;
+    const bool k0 = (ix == 0 && kyi == 0 && kzi == 0);
+    const bool rm = removed(q, ix, kyi, kzi);
+    C N[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) N[f] = cscale(buf[iz * LP + f * TX + c], inv_n);
+    // project_perpk3d: N -= k (k.N)/|k|^2 ; k = 0 untouched
+    if (!k0) {
+      const T inv = T(1) / k2;
+      C t = mk<C>((kx * N[0].x + ky * N[1].x + kz * N[2].x) * inv,
+                  (kx * N[0].y + ky * N[1].y + kz * N[2].y) * inv);
+      N[0] = csub(N[0], cscale(t, kx));
+      N[1] = csub(N[1], cscale(t, ky));
+      N[2] = csub(N[2], cscale(t, kz));
+    }
+    if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
+    if (mode == kTend) {
+      C* o = static_cast<C*>(a.tend);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
+    } else if (mode == kRK3) {
+      const C* tmp = static_cast<const C*>(a.tmp);
+      const T c6 = T(a.dt) / T(6);
+      C Sn[3];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        C t = tmp[i + f * nK];
+        Sn[f] = mk<C>(t.x + c6 * N[f].x, t.y + c6 * N[f].y);
+      }
+      if (!k0) {
+        const T inv = T(1) / k2;
+        C t = mk<C>((kx * Sn[0].x + ky * Sn[1].x + kz * Sn[2].x) * inv,
+                    (kx * Sn[0].y + ky * Sn[1].y + kz * Sn[2].y) * inv);
+        Sn[0] = csub(Sn[0], cscale(t, kx));
+        Sn[1] = csub(Sn[1], cscale(t, ky));
+        Sn[2] = csub(Sn[2], cscale(t, kz));
+      }
+      if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
+      C* So = static_cast<C*>(a.Sout);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) So[i + f * nK] = Sn[f];
+      if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
+    } else {
+      const T sig = freq_lin<T>(q, k2, k0);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) rk_update<C, T>(mode, a, i + f * nK, N[f], sig);
+    }
+  }
+}
+
+// =====================================================================  ns2d
+// A: inverse y pass; fields ux, uy, d_x rot, d_y rot from rot_fft.
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
+         const cplx<T>* __restrict__ twy) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.ny * q.LP;
+  const int TX = q.TX, LP = q.LP;
+  const int c0 = blockIdx.x * TX;
+  const int64_t nK = (int64_t)q.ny * q.nkx;
+  for (int idx = threadIdx.x; idx < q.ny * TX; idx += blockDim.x) {
+    const int c = idx % TX, iy = idx / TX, ix = c0 + c;
+    C v[4];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) v[f] = mk<C>(0, 0);
+    if (ix < q.nkx) {
+      const C w = S[(int64_t)iy * q.nkx + ix];
+      const T kx = T(q.dkx * ix), ky = T(q.dky * kadim(iy, q.ny));
+      const T k2 = kx * kx + ky * ky;
+      const T inv = (ix == 0 && kadim(iy, q.ny) == 0) ? T(0) : T(1) / k2;
+      const T cx = ky * inv, cy = -(kx * inv);
+      v[0] = mk<C>(-cx * w.y, cx * w.x);  // i ky rot / k^2
+      v[1] = mk<C>(-cy * w.y, cy * w.x);  // -i kx rot / k^2
+      v[2] = mk<C>(-kx * w.y, kx * w.x);  // i kx rot
+      v[3] = mk<C>(-ky * w.y, ky * w.x);  // i ky rot
+    }
+#pragma unroll
+    for (int f = 0; f < 4; ++f) buf[iy * LP + f * TX + c] = v[f];
+  }
+  __syncthreads();
+  fft_tile<+1, kTPT>(buf, buf2, q.ny, 4 * TX, LP, twy, 1);
+  for (int idx = threadIdx.x; idx < q.ny * TX; idx += blockDim.x) {
+    const int c = idx % TX, iy = idx / TX, ix = c0 + c;
+    if (ix >= q.nkx) continue;
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      W[f * nK + (int64_t)iy * q.nkx + ix] = buf[iy * LP + f * TX + c];
+  }
+}
+
+// B: x pass, compute_Frot = -ux d_x rot - uy (d_y rot + beta).
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k2_x_product(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, NSK q,
+             const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.M * q.LP;
+  const int L = q.L, LP = q.LP, M = q.M, nkx = q.nkx;
+  const int64_t nrows = q.ny;
+  const int64_t nK = nrows * nkx;
+  const int64_t r0 = (int64_t)blockIdx.x * L;
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int j = idx % M, l = idx / M;
+    const bool ok = r0 + l < nrows;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      C z = mk<C>(0, 0);
+      if (ok) z = c2r_pre(W + f * nK + (r0 + l) * nkx, j, M, twx);
+      buf[j * LP + f * L + l] = z;
+    }
+  }
+  __syncthreads();
+  fft_tile<+1, kTPT>(buf, buf2, M, 4 * L, LP, twx, 2);
+  T mx = 0, my = 0;
+  const T beta = T(q.beta);
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int j = idx % M, l = idx / M;
+    C* p = buf + j * LP + l;
+    const C ux = p[0], uy = p[L], px = p[2 * L], py = p[3 * L];
+    C r;
+    if (q.beta == 0) {
+      r = mk<C>(-ux.x * px.x - uy.x * py.x, -ux.y * px.y - uy.y * py.y);
+    } else {
+      r = mk<C>(-ux.x * px.x - uy.x * (py.x + beta),
+                -ux.y * px.y - uy.y * (py.y + beta));
+    }
+    p[0] = r;
+    if (vmax && r0 + l < nrows) {
+      mx = fmax(mx, fmax(fabs(ux.x), fabs(ux.y)));
+      my = fmax(my, fmax(fabs(uy.x), fabs(uy.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, T(0), vmax);
+  fft_tile<-1, kTPT>(buf, buf2, M, L, LP, twx, 2);
+  for (int idx = threadIdx.x; idx < L * nkx; idx += blockDim.x) {
+    const int k = idx % nkx, l = idx / nkx;
+    if (r0 + l >= nrows) continue;
+    F[(r0 + l) * nkx + k] = r2c_post<C, T>(buf, k, M, LP, l, twx);
+  }
+}
+
+// C: forward y pass + 1/N + dealiasing + RK4 stage.
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads)
+k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ twy,
+            int mode, RKArgs a) {
+  using C = cplx<T>;
+  C* buf = reinterpret_cast<C*>(g_smem_ns);
+  C* buf2 = buf + (size_t)q.ny * q.LP;
+  const int TX = q.TX, LP = q.LP;
+  const int c0 = blockIdx.x * TX;
+  for (int idx = threadIdx.x; idx < q.ny * TX; idx += blockDim.x) {
+    const int c = idx % TX, iy = idx / TX, ix = c0 + c;
+    buf[iy * LP + c] = ix < q.nkx ? F[(int64_t)iy * q.nkx + ix] : mk<C>(0, 0);
+  }
+  __syncthreads();
+  fft_tile<-1, kTPT>(buf, buf2, q.ny, TX, LP, twy, 1);
+  const T inv_n = T(q.inv_n);
+  for (int idx = threadIdx.x; idx < q.ny * TX; idx += blockDim.x) {
+    const int c = idx % TX, iy = idx / TX, ix = c0 + c;
+    if (ix >= q.nkx) continue;
+    const int64_t i = (int64_t)iy * q.nkx + ix;
+    const int kyi = kadim(iy, q.ny);
+    const bool rm = removed(q, ix, kyi, 0);
+    C N = cscale(buf[iy * LP + c], inv_n);
+    if (rm) N = mk<C>(0, 0);
+    if (mode == kTend) {
+      static_cast<C*>(a.tend)[i] = N;
+    } else if (mode == kRK3) {
+      const C t = static_cast<const C*>(a.tmp)[i];
+      const T c6 = T(a.dt) / T(6);
+      C Sn = mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
+      if (rm) Sn = mk<C>(0, 0);
+      static_cast<C*>(a.Sout)[i] = Sn;
+      if (isnan(Sn.x) || isnan(Sn.y)) atomicOr(a.nan_flag, 1);
+    } else {
+      const T kx = T(q.dkx * ix), ky = T(q.dky * kyi);
+      const T k2 = kx * kx + ky * ky;
+      const T sig = freq_lin<T>(q, k2, ix == 0 && kyi == 0);
+      rk_update<C, T>(mode, a, i, N, sig);
+    }
+  }
+}
+
+// ================================================================ solver
+struct Solver {
+  gbs_ns_params p;
+  NSK q;
+  int nvar;
+  int64_t nK;
+  size_t csize;
+  void* tw[3];
+  void* W;
+  void* F;
+  void* tmp;
+  void* tmp1;
+  unsigned long long* dmax;  // 3 maxima (double bits)
+  int* dflag;
+  double* dred;              // reduction partials
+  double* hbuf;              // pinned host mirror (8 doubles)
+  // launch shapes
+  int txA, txC, Lb;
+  int thA, thB, thC;
+  size_t smA, smB, smC;
+};
+
+template <typename T>
+static int setup_shapes(Solver* s) {
+  const size_t cs = sizeof(cplx<T>);
+  NSK& q = s->q;
+  const int txmax = sizeof(T) == 4 ? 16 : 8;
+  if (s->p.ndim == 3) {
+    s->txA = pick_tx(q.nz, 6, cs, txmax, q.nkx);
+    s->txC = pick_tx(q.nz, 3, cs, txmax, q.nkx);
+    s->smA = tile_smem(q.nz, 6 * s->txA, cs);
+    s->smC = tile_smem(q.nz, 3 * s->txC, cs);
+    s->thA = tile_threads(q.nz, 6 * s->txA);
+    s->thC = tile_threads(q.nz, 3 * s->txC);
+    int L = sizeof(T) == 4 ? 8 : 4;
+    const int64_t nrows = (int64_t)q.nz * q.ny;
+    while (L > 1 && (tile_smem(q.M, 6 * L + 1, cs) > kSmemBudget ||
+                     !tile_fits(q.M, 6 * L) || L / 2 >= nrows))
+      L /= 2;
+    s->Lb = L;
+    s->smB = tile_smem(q.M, 6 * L + 1, cs);
+    s->thB = tile_threads(q.M, 6 * L);
+    int rc = allow_smem(k3_inv_z_curl<T>, s->smA);
+    if (!rc) rc = allow_smem(k3_x_product<T>, s->smB);
+    if (!rc) rc = allow_smem(k3_fwd_z_rk<T>, s->smC);
+    if (rc) return rc;
+    if (s->smA > kSmemMax - 1024 || s->smB > kSmemMax - 1024 || s->smC > kSmemMax - 1024 ||
+        !tile_fits(q.nz, 6 * s->txA) || !tile_fits(q.nz, 3 * s->txC) ||
+        !tile_fits(q.M, 6 * L)) {
+      set_error("grid too large for the fused kernels");
+      return GBS_EINVAL;
+    }
+  } else {
+    s->txA = pick_tx(q.ny, 4, cs, txmax, q.nkx);
+    s->txC = pick_tx(q.ny, 1, cs, txmax, q.nkx);
+    s->smA = tile_smem(q.ny, 4 * s->txA, cs);
+    s->smC = tile_smem(q.ny, s->txC, cs);
+    s->thA = tile_threads(q.ny, 4 * s->txA);
+    s->thC = tile_threads(q.ny, s->txC);
+    int L = sizeof(T) == 4 ? 8 : 4;
+    while (L > 1 && (tile_smem(q.M, 4 * L + 1, cs) > kSmemBudget ||
+                     !tile_fits(q.M, 4 * L) || L / 2 >= q.ny))
+      L /= 2;
+    s->Lb = L;
+    s->smB = tile_smem(q.M, 4 * L + 1, cs);
+    s->thB = tile_threads(q.M, 4 * L);
+    int rc = allow_smem(k2_inv_y<T>, s->smA);
+    if (!rc) rc = allow_smem(k2_x_product<T>, s->smB);
+    if (!rc) rc = allow_smem(k2_fwd_y_rk<T>, s->smC);
+    if (rc) return rc;
+    if (s->smA > kSmemMax - 1024 || s->smB > kSmemMax - 1024 || s->smC > kSmemMax - 1024 ||
+        !tile_fits(q.ny, 4 * s->txA) || !tile_fits(q.ny, s->txC) ||
+        !tile_fits(q.M, 4 * L)) {
+      set_error("grid too large for the fused kernels");
+      return GBS_EINVAL;
+    }
+  }
+  return GBS_OK;
+}
+
+// One tendency evaluation from `in`; kernel C runs `mode`.
+template <typename T>
+static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
+                bool want_max, cudaStream_t st) {
+  using C = cplx<T>;
+  NSK q = s->q;
+  const C* twx = static_cast<const C*>(s->tw[0]);
+  const C* twy = static_cast<const C*>(s->tw[1]);
+  const C* twz = static_cast<const C*>(s->tw[2]);
+  C* W = static_cast<C*>(s->W);
+  C* F = static_cast<C*>(s->F);
+  unsigned long long* vmax = want_max ? s->dmax : nullptr;
+  int rc;
+  if (s->p.ndim == 3) {
+    q.TX = s->txA;
+    q.LP = 6 * q.TX;
+    k3_inv_z_curl<T><<<dim3(ceil_div(q.nkx, q.TX), q.ny), s->thA, s->smA, st>>>(
+        static_cast<const C*>(in), W, q, twz);
+    GBS_CHECK_LAUNCH();
+    rc = launch_col<T, 1>(W, W, q.ny, q.nkx, q.nz, 6, q.nkx,
+                          (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    if (rc) return rc;
+    q.L = s->Lb;
+    q.LP = 6 * q.L + 1;
+    k3_x_product<T><<<ceil_div((int64_t)q.nz * q.ny, q.L), s->thB, s->smB, st>>>(
+        W, F, q, twx, vmax);
+    GBS_CHECK_LAUNCH();
+    rc = launch_col<T, -1>(F, F, q.ny, q.nkx, q.nz, 3, q.nkx,
+                           (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    if (rc) return rc;
+    return GBS_OK;
+  }
+  q.TX = s->txA;
+  q.LP = 4 * q.TX;
+  k2_inv_y<T><<<ceil_div(q.nkx, q.TX), s->thA, s->smA, st>>>(
+      static_cast<const C*>(in), W, q, twy);
+  GBS_CHECK_LAUNCH();
+  q.L = s->Lb;
+  q.LP = 4 * q.L + 1;
+  k2_x_product<T><<<ceil_div(q.ny, q.L), s->thB, s->smB, st>>>(W, F, q, twx, vmax);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st) {
+  using C = cplx<T>;
+  NSK q = s->q;
+  const C* F = static_cast<const C*>(s->F);
+  if (s->p.ndim == 3) {
+    q.TX = s->txC;
+    q.LP = 3 * q.TX;
+    k3_fwd_z_rk<T><<<dim3(ceil_div(q.nkx, q.TX), q.ny), s->thC, s->smC, st>>>(
+        F, q, static_cast<const C*>(s->tw[2]), mode, a);
+  } else {
+    q.TX = s->txC;
+    q.LP = q.TX;
+    k2_fwd_y_rk<T><<<ceil_div(q.nkx, q.TX), s->thC, s->smC, st>>>(
+        F, q, static_cast<const C*>(s->tw[1]), mode, a);
+  }
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+static int tendencies(Solver* s, const void* S, void* tend, cudaStream_t st) {
+  RKArgs a{};
+  a.tend = tend;
+  int rc = eval<T>(s, S, kTend, a, false, st);
+  if (rc) return rc;
+  return finish<T>(s, kTend, a, st);
+}
+
+double cfl_rule(double dt, double tmp, double cfl, double dtmax) {
+  // fluidsim/base/time_stepping/base.py:334-354
+  double deltat_CFL = tmp > 0 ? cfl / tmp : dtmax;
+  double maybe_new_dt = deltat_CFL < dtmax ? deltat_CFL : dtmax;
+  double normalize_diff = fabs(dt - maybe_new_dt) / maybe_new_dt;
+  if (normalize_diff > 0.02) dt = maybe_new_dt;
+  return dt;
+}
+
+static double cfl_tmp(const Solver* s, const double* m) {
+  // max_ux / deltax + max_uy / deltay (+ max_uz / deltaz), base.py:330-334
+  double t = m[0] / (s->p.Lx / s->p.nx) + m[1] / (s->p.Ly / s->p.ny);
+  if (s->p.ndim == 3) t += m[2] / (s->p.Lz / s->p.nz);
+  return t;
+}
+
+template <typename T>
+static int step(Solver* s, void* S, double* dt, const double* cfl,
+                int check_nan, cudaStream_t st) {
+  RKArgs a{};
+  a.S = S;
+  a.Sout = S;
+  a.tmp = s->tmp;
+  a.tmp1 = s->tmp1;
+  a.nan_flag = s->dflag;
+  int rc;
+  if (cfl) GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
+  if (check_nan) GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
+  rc = eval<T>(s, S, kRK0, a, cfl != nullptr, st);
+  if (rc) return rc;
+  if (cfl) {
+    GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
+  }
+  a.dt = *dt;
+  rc = finish<T>(s, kRK0, a, st);
+  if (rc) return rc;
+  for (int m = kRK1; m <= kRK3; ++m) {
+    rc = eval<T>(s, s->tmp1, m, a, false, st);
+    if (rc) return rc;
+    rc = finish<T>(s, m, a, st);
+    if (rc) return rc;
+  }
+  if (check_nan) {
+    GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf + 4, s->dflag, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    int flag;
+    memcpy(&flag, s->hbuf + 4, sizeof(int));
+    if (flag) {
+      set_error("nan in state_spect[0] after the time step");
+      return GBS_ENAN;
+    }
+  }
+  return GBS_OK;
+}
+
+template <typename T>
+static int max_velocity(Solver* s, const void* S, double* out, cudaStream_t st) {
+  RKArgs a{};
+  GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
+  int rc = eval<T>(s, S, kTend, a, true, st);
+  if (rc) return rc;
+  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < s->p.ndim; ++i) out[i] = s->hbuf[i];
+  return GBS_OK;
+}
+
+// --------------------------------------------------- FP64 reductions
+// Spatial means: per-mode quantities with Hermitian weights, block partial
+// sums reduced in a fixed order (deterministic for a given launch shape).
+constexpr int kRedBlocks = 304;
+constexpr int kRedThreads = 256;
+constexpr int kNQ = 6;
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+k_means(const cplx<T>* __restrict__ S, NSK q, int ndim, double* partial) {
+  using C = cplx<T>;
+  const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  double acc[kNQ] = {0, 0, 0, 0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % q.nkx);
+    const int64_t r = i / q.nkx;
+    const int iy = (int)(r % q.ny), iz = (int)(r / q.ny);
+    const double w = (ix == 0 || (q.nx % 2 == 0 && ix == q.nx / 2)) ? 1.0 : 2.0;
+    const double kx = q.dkx * ix, ky = q.dky * kadim(iy, q.ny);
+    const double kz = ndim == 3 ? q.dkz * kadim(iz, q.nz) : 0.0;
+    const double k2 = ndim == 3 ? kx * kx + ky * ky + kz * kz : kx * kx + ky * ky;
+    const bool k0 = ix == 0 && kadim(iy, q.ny) == 0 && (ndim == 2 || kadim(iz, q.nz) == 0);
+    double fd = q.nu2 > 0 ? q.nu2 * k2 : 0.0;
+    if (q.nu4 > 0) fd += q.nu4 * (k2 * k2);
+    if (q.nu8 > 0) fd += q.nu8 * ((k2 * k2) * (k2 * k2));
+    double fh = 0.0;
+    if (q.num4 != 0) {
+      double kk = k0 ? q.k2_hypo0 : k2;
+      fh = q.num4 / (kk * kk);
+    }
+    if (ndim == 3) {
+      const C a = S[i], b = S[i + nK], c = S[i + 2 * nK];
+      const double ex = 0.5 * ((double)a.x * a.x + (double)a.y * a.y);
+      const double ey = 0.5 * ((double)b.x * b.x + (double)b.y * b.y);
+      const double ez = 0.5 * ((double)c.x * c.x + (double)c.y * c.y);
+      const double e = ex + ey + ez;
+      acc[0] += w * e;
+      acc[1] += w * ex;
+      acc[2] += w * ey;
+      acc[3] += w * ez;
+      acc[4] += w * fd * 2 * e;
+      acc[5] += w * fh * 2 * e;
+    } else {
+      const C rt = S[i];
+      const double z = 0.5 * ((double)rt.x * rt.x + (double)rt.y * rt.y);
+      const double e = k0 ? 0.0 : z / k2;  // |u|^2/2 = |rot|^2 / (2 k^2)
+      acc[0] += w * e;
+      acc[1] += w * z;
+      acc[2] += w * fd * 2 * e;
+      acc[3] += w * fh * 2 * e;
+      acc[4] += w * fd * 2 * z;
+      acc[5] += w * fh * 2 * z;
+    }
+  }
+  __shared__ double red[kNQ][kRedThreads];
+#pragma unroll
+  for (int k = 0; k < kNQ; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int k = 0; k < kNQ; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < kNQ) partial[threadIdx.x * kRedBlocks + blockIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_sum_partials(const double* partial, int nb, double* out) {
+  const int k = threadIdx.x;
+  if (k >= kNQ) return;
+  double s = 0;
+  for (int b = 0; b < nb; ++b) s += partial[k * kRedBlocks + b];
+  out[k] = s;
+}
+
+template <typename T>
+static int spatial_means(Solver* s, const void* S, double* out, cudaStream_t st) {
+  k_means<T><<<kRedBlocks, kRedThreads, 0, st>>>(static_cast<const cplx<T>*>(S),
+                                                  s->q, s->p.ndim, s->dred);
+  GBS_CHECK_LAUNCH();
+  k_sum_partials<<<1, 32, 0, st>>>(s->dred, kRedBlocks, s->dred + kNQ * kRedBlocks);
+  GBS_CHECK_LAUNCH();
+  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dred + kNQ * kRedBlocks,
+                               kNQ * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int k = 0; k < kNQ; ++k) out[k] = s->hbuf[k];
+  return GBS_OK;
+}
+
+static int64_t spectrum_bins(const Solver* s) {
+  const NSK& q = s->q;
+  double dk = q.dkx < q.dky ? q.dkx : q.dky;
+  if (s->p.ndim == 3 && q.dkz < dk) dk = q.dkz;
+  double kx = q.dkx * (q.nkx - 1), ky = q.dky * (q.ny / 2), kz = q.dkz * (q.nz / 2);
+  double kmax = sqrt(kx * kx + ky * ky + (s->p.ndim == 3 ? kz * kz : 0.0));
+  return (int64_t)floor(kmax / dk + 0.5) + 1;
+}
+
+template <typename T>
+__global__ void k_spectrum(const cplx<T>* __restrict__ S, NSK q, int ndim,
+                           double dk, int64_t nbins, double* spec) {
+  using C = cplx<T>;
+  const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % q.nkx);
+    const int64_t r = i / q.nkx;
+    const int iy = (int)(r % q.ny), iz = (int)(r / q.ny);
+    const double w = (ix == 0 || (q.nx % 2 == 0 && ix == q.nx / 2)) ? 1.0 : 2.0;
+    const double kx = q.dkx * ix, ky = q.dky * kadim(iy, q.ny);
+    const double kz = ndim == 3 ? q.dkz * kadim(iz, q.nz) : 0.0;
+    const double k2 = kx * kx + ky * ky + kz * kz;
+    double e;
+    if (ndim == 3) {
+      const C a = S[i], b = S[i + nK], c = S[i + 2 * nK];
+      e = 0.5 * ((double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x +
+                 (double)b.y * b.y + (double)c.x * c.x + (double)c.y * c.y);
+    } else {
+      const C rt = S[i];
+      e = k2 > 0 ? 0.5 * ((double)rt.x * rt.x + (double)rt.y * rt.y) / k2 : 0.0;
+    }
+    int64_t b = (int64_t)floor(sqrt(k2) / dk + 0.5);
+    if (b >= nbins) b = nbins - 1;
+    atomicAdd(spec + b, w * e / dk);
+  }
+}
+
+}  // namespace gbs
+
+using gbs::Solver;
+
+struct gbs_ns {
+  Solver s;
+};
+
+static void free_solver(Solver* s) {
+  for (void* t : s->tw)
+    if (t) cudaFree(t);
+  void* ptrs[] = {s->W, s->F, s->tmp, s->tmp1, s->dmax, s->dflag, s->dred};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->hbuf) cudaFreeHost(s->hbuf);
+}
+
+namespace gbs {
+int twiddle_alloc(void** out, int n, int dtype, cudaStream_t st);
+}
+
+extern "C" {
+
+double gbs_cfl_update(double dt, double tmp, double cfl_coef,
+                      double deltat_max) {
+  return gbs::cfl_rule(dt, tmp, cfl_coef, deltat_max);
+}
+
+int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
+  gbs::clear_error();
+  if (!prm || !out) {
+    gbs::set_error("gbs_ns_create: null argument");
+    return GBS_EINVAL;
+  }
+  *out = nullptr;
+  const gbs_ns_params& p = *prm;
+  if ((p.ndim != 2 && p.ndim != 3) || (p.dtype != GBS_F32 && p.dtype != GBS_F64) ||
+      p.nx < 2 || p.nx % 2 || p.ny < 1 || p.nz < 1 || (p.ndim == 2 && p.nz != 1) ||
+      p.nx > 65536 || p.ny > 65535 || p.nz > 65536 || !(p.Lx > 0) || !(p.Ly > 0) ||
+      (p.ndim == 3 && !(p.Lz > 0))) {
+    gbs::set_error("gbs_ns_create: invalid parameters (nx must be even)");
+    return GBS_EINVAL;
+  }
+  gbs_ns* h = new (std::nothrow) gbs_ns();
+  if (!h) return GBS_ENOMEM;
+  Solver* s = &h->s;
+  memset(s, 0, sizeof(*s));
+  s->p = p;
+  s->nvar = p.ndim == 3 ? 3 : 1;
+  gbs::NSK& q = s->q;
+  q.nx = (int)p.nx;
+  q.ny = (int)p.ny;
+  q.nz = (int)p.nz;
+  q.nkx = q.nx / 2 + 1;
+  q.M = q.nx / 2;
+  q.kcx = (int)(p.kcut_x < p.nx ? p.kcut_x : p.nx + 1);
+  q.kcy = (int)(p.kcut_y < p.ny ? p.kcut_y : p.ny + 1);
+  q.kcz = p.ndim == 3 ? (int)(p.kcut_z < p.nz ? p.kcut_z : p.nz + 1) : 1 << 30;
+  const double pi2 = 6.283185307179586;
+  q.dkx = pi2 / p.Lx;
+  q.dky = pi2 / p.Ly;
+  q.dkz = p.ndim == 3 ? pi2 / p.Lz : 0.0;
+  q.nu2 = p.nu_2;
+  q.nu4 = p.nu_4;
+  q.nu8 = p.nu_8;
+  q.num4 = p.nu_m4;
+  q.beta = p.beta;
+  q.f = p.f;
+  q.has_f = p.ndim == 3 && p.has_f;
+  q.inv_n = 1.0 / ((double)p.nx * p.ny * p.nz);
+  q.k2_hypo0 = q.dkx * q.dkx;
+  s->nK = (int64_t)q.nz * q.ny * q.nkx;
+  s->csize = p.dtype == GBS_F64 ? sizeof(double2) : sizeof(float2);
+  int rc = 0;
+  int ns[3] = {q.nx, q.ny, q.nz};
+  for (int a = 0; a < 3 && !rc; ++a) rc = gbs::twiddle_alloc(&s->tw[a], ns[a], p.dtype, 0);
+  const size_t fb = s->csize * s->nK;
+  const int nW = p.ndim == 3 ? 6 : 4;
+  if (!rc) {
+    if (cudaMalloc(&s->W, fb * nW) != cudaSuccess ||
+        cudaMalloc(&s->F, fb * s->nvar) != cudaSuccess ||
+        cudaMalloc(&s->tmp, fb * s->nvar) != cudaSuccess ||
+        cudaMalloc(&s->tmp1, fb * s->nvar) != cudaSuccess ||
+        cudaMalloc(&s->dmax, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&s->dflag, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&s->dred, sizeof(double) * (gbs::kNQ * gbs::kRedBlocks + 16)) != cudaSuccess ||
+        cudaMallocHost(&s->hbuf, 8 * sizeof(double)) != cudaSuccess) {
+      gbs::set_error("gbs_ns_create: device allocation failed (%zu MB requested)",
+                     (size_t)(fb * (nW + 3 * s->nvar) >> 20));
+      rc = GBS_ENOMEM;
+    }
+  }
+  if (!rc) rc = p.dtype == GBS_F64 ? gbs::setup_shapes<double>(s) : gbs::setup_shapes<float>(s);
+  if (!rc) {
+    // tmp / tmp1 start at zero so that modes never written stay zero
+    if (cudaMemset(s->tmp, 0, fb * s->nvar) != cudaSuccess ||
+        cudaMemset(s->tmp1, 0, fb * s->nvar) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {
+      gbs::set_error("gbs_ns_create: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = GBS_ECUDA;
+    }
+  }
+  if (rc) {
+    free_solver(s);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GBS_OK;
+}
+
+int gbs_ns_destroy(gbs_ns* h) {
+  if (!h) return GBS_OK;
+  free_solver(&h->s);
+  delete h;
+  return GBS_OK;
+}
+
+int gbs_ns_tendencies(gbs_ns* h, const void* S, void* tend, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !tend) {
+    gbs::set_error("gbs_ns_tendencies: null argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h->s.p.dtype == GBS_F64) return gbs::tendencies<double>(&h->s, S, tend, st);
+  return gbs::tendencies<float>(&h->s, S, tend, st);
+}
+
+int gbs_ns_step_rk4(gbs_ns* h, void* S, double* dt, const double* cfl,
+                    int check_nan, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !dt || !(*dt > 0)) {
+    gbs::set_error("gbs_ns_step_rk4: invalid argument");
+    return GBS_EINVAL;
+  }
+  if (cfl && (!(cfl[0] > 0) || !(cfl[1] > 0))) {
+    gbs::set_error("gbs_ns_step_rk4: invalid CFL parameters");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h->s.p.dtype == GBS_F64) return gbs::step<double>(&h->s, S, dt, cfl, check_nan, st);
+  return gbs::step<float>(&h->s, S, dt, cfl, check_nan, st);
+}
+
+int gbs_ns_max_velocity(gbs_ns* h, const void* S, double* out, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !out) {
+    gbs::set_error("gbs_ns_max_velocity: null argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h->s.p.dtype == GBS_F64) return gbs::max_velocity<double>(&h->s, S, out, st);
+  return gbs::max_velocity<float>(&h->s, S, out, st);
+}
+
+int gbs_ns_spatial_means(gbs_ns* h, const void* S, double* out, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !out) {
+    gbs::set_error("gbs_ns_spatial_means: null argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (h->s.p.dtype == GBS_F64) return gbs::spatial_means<double>(&h->s, S, out, st);
+  return gbs::spatial_means<float>(&h->s, S, out, st);
+}
+
+int gbs_ns_spectrum_size(gbs_ns* h, int64_t* nk) {
+  gbs::clear_error();
+  if (!h || !nk) {
+    gbs::set_error("gbs_ns_spectrum_size: null argument");
+    return GBS_EINVAL;
+  }
+  *nk = gbs::spectrum_bins(&h->s);
+  return GBS_OK;
+}
+
+int gbs_ns_spectrum(gbs_ns* h, const void* S, double* spec, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !spec) {
+    gbs::set_error("gbs_ns_spectrum: null argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Solver* s = &h->s;
+  const int64_t nb = gbs::spectrum_bins(s);
+  double dk = s->q.dkx < s->q.dky ? s->q.dkx : s->q.dky;
+  if (s->p.ndim == 3 && s->q.dkz < dk) dk = s->q.dkz;
+  GBS_CUDA_TRY(cudaMemsetAsync(spec, 0, nb * sizeof(double), st));
+  if (s->p.dtype == GBS_F64)
+    gbs::k_spectrum<double><<<gbs::kRedBlocks, gbs::kRedThreads, 0, st>>>(
+        static_cast<const double2*>(S), s->q, s->p.ndim, dk, nb, spec);
+  else
+    gbs::k_spectrum<float><<<gbs::kRedBlocks, gbs::kRedThreads, 0, st>>>(
+        static_cast<const float2*>(S), s->q, s->p.ndim, dk, nb, spec);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+}  // extern "C"

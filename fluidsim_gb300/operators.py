@@ -1,0 +1,276 @@
+"""Operators on device arrays with the fluidsim operator-class surface.
+
+``OperatorsPseudoSpectral2D`` / ``OperatorsPseudoSpectral3D`` mirror the
+attributes and methods of ``fluidsim/operators/operators2d.py:85-259`` and
+``fluidsim/operators/operators3d.py:116-342`` that the ns2d/ns3d hot path
+and its outputs use (wavenumber arrays, ``where_dealiased``, ``dealiasing``,
+curl / gradient / projection helpers, ``sum_wavenumbers``), over CUDA
+tensors.  The transforms go through the GB300 FFT plugin; the fused time
+step does not call these helpers (it recomputes k on the fly inside its
+kernels), they serve user scripts and outputs.
+
+Wavenumber conventions: ``k_adim = ik`` if ``ik <= n//2`` else ``ik - n``
+(``operators3d.py:1196-1199``), x non-negative; cubic truncation removes
+``|k_adim| >= kcut`` on any axis, kcut from ``init_fields.cubic_dealias_cutoff``.
+"""
+
+from math import pi
+
+import numpy as np
+import torch
+
+from .fft import FFT2DGB300, FFT3DGB300, import_fft_class
+from .init_fields import cubic_dealias_cutoff
+from .params import Parameters
+
+
+def _kadim(n):
+    ik = np.arange(n)
+    return np.where(ik <= n // 2, ik, ik - n)
+
+
+class _OperBase:
+    is_sequential = True
+    SAME_SIZE_IN_ALL_PROC = True
+
+    def _finish_init(self):
+        self._has_to_dealiase = self.coef_dealiasing < 1.0
+        mask = np.zeros(self.shapeK, dtype=bool)
+        for axis, (n, L, cut) in enumerate(zip(self.shapeX, self._lengths, self.kcut)):
+            ks = np.abs(_kadim(n)) if axis < self.ndim - 1 else np.arange(n // 2 + 1)
+            shape = [1] * self.ndim
+            shape[axis] = -1
+            mask = mask | (ks >= cut).reshape(shape)
+        self._where_dealiased_np = mask.astype(np.uint8)
+        self.where_dealiased = torch.from_numpy(self._where_dealiased_np).to(self.device)
+        self._keep = (self.where_dealiased == 0).to(self.rdtype)
+
+    # ----- transforms (fluidfft operator API) -----
+    def fft(self, fieldX):
+        return self.opfft.fft(fieldX)
+
+    def ifft(self, fieldK):
+        return self.opfft.ifft(fieldK)
+
+    def fft_as_arg(self, fieldX, fieldK):
+        return self.opfft.fft_as_arg(fieldX, fieldK)
+
+    def ifft_as_arg(self, fieldK, fieldX):
+        return self.opfft.ifft_as_arg(fieldK, fieldX)
+
+    def ifft_as_arg_destroy(self, fieldK, fieldX):
+        return self.opfft.ifft_as_arg_destroy(fieldK, fieldX)
+
+    def create_arrayX(self, value=None, shape="loc"):
+        return self.opfft.create_arrayX(value)
+
+    def create_arrayK(self, value=None, shape="loc"):
+        return self.opfft.create_arrayK(value)
+
+    def get_shapeX_loc(self):
+        return self.shapeX
+
+    def get_shapeK_loc(self):
+        return self.shapeK
+
+    def get_k_adim_loc(self):
+        return self.opfft.get_k_adim_loc()
+
+    def sum_wavenumbers(self, arrK):
+        return self.opfft.sum_wavenumbers(arrK)
+
+    def mean_space(self, arr):
+        return float(arr.to(torch.float64).mean()) if isinstance(arr, torch.Tensor) else float(np.mean(arr))
+
+    # ----- dealiasing (operators3d.py:336-342, operators2d.py:200-220) -----
+    def dealiasing_variable(self, ff_fft):
+        if self._has_to_dealiase:
+            ff_fft.mul_(self._keep)
+
+    def dealiasing_setofvar(self, sov):
+        if self._has_to_dealiase:
+            sov.mul_(self._keep)
+
+    def dealiasing(self, *args):
+        for thing in args:
+            if isinstance(thing, torch.Tensor):
+                if self._has_to_dealiase:
+                    thing.mul_(self._keep)
+            else:
+                arr = np.asarray(thing)
+                if self._has_to_dealiase:
+                    arr[..., self._where_dealiased_np.astype(bool)] = 0.0
+
+
+class OperatorsPseudoSpectral2D(_OperBase):
+    ndim = 2
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        """Same defaults as ``operators2d.py:100-112``."""
+        params._set_child("oper", attribs={
+            "type_fft": "default", "coef_dealiasing": 2.0 / 3, "nx": 48, "ny": 48,
+            "Lx": 8, "Ly": 8, "truncation_shape": "cubic", "NO_SHEAR_MODES": False,
+            "NO_KY0": False})
+
+    def __init__(self, params, precision="float64", device=None):
+        self.params = params
+        po = params.oper
+        if po.truncation_shape != "cubic" or po.NO_SHEAR_MODES or po.NO_KY0:
+            raise NotImplementedError("only the cubic truncation is implemented on GB300")
+        self.nx, self.ny = int(po.nx), int(po.ny)
+        self.Lx = self.lx = float(po.Lx)
+        self.Ly = self.ly = float(po.Ly)
+        self.coef_dealiasing = po.coef_dealiasing
+        cls = import_fft_class(po.type_fft, 2)
+        self.opfft = self.oper_fft = cls(self.ny, self.nx, precision=precision, device=device)
+        self.device = self.opfft.device
+        self.rdtype, self.cdtype = self.opfft.rdtype, self.opfft.cdtype
+        self.shapeX = self.shapeX_seq = self.shapeX_loc = (self.ny, self.nx)
+        self.shapeK = self.shapeK_seq = self.shapeK_loc = (self.ny, self.nx // 2 + 1)
+        self.deltax, self.deltay = self.Lx / self.nx, self.Ly / self.ny
+        self.deltakx, self.deltaky = 2 * pi / self.Lx, 2 * pi / self.Ly
+        self._lengths = (self.Ly, self.Lx)
+        self.kcut = (cubic_dealias_cutoff(self.ny, self.Ly, self.coef_dealiasing),
+                     cubic_dealias_cutoff(self.nx, self.Lx, self.coef_dealiasing))
+        kx = torch.tensor(self.deltakx * np.arange(self.nx // 2 + 1), dtype=self.rdtype,
+                          device=self.device)
+        ky = torch.tensor(self.deltaky * _kadim(self.ny), dtype=self.rdtype, device=self.device)
+        self.kx, self.ky = kx, ky
+        self.KX = kx[None, :].expand(self.shapeK)
+        self.KY = ky[:, None].expand(self.shapeK)
+        self.K2 = self.KX**2 + self.KY**2
+        self.K4 = self.K2**2
+        self.K8 = self.K4**2
+        self.K2_not0 = self.K2.clone()
+        self.K2_not0[0, 0] = 1e-14
+        self.inv_K_square_nozero = 1.0 / self.K2_not0
+        self.inv_K_square_nozero[0, 0] = 0.0
+        self.K_not0 = torch.sqrt(self.K2_not0)
+        x = torch.arange(self.nx, dtype=torch.float64) * self.deltax
+        y = torch.arange(self.ny, dtype=torch.float64) * self.deltay
+        self.x = self.x_seq = self.x_loc = x
+        self.y = self.y_seq = self.y_loc = y
+        self._finish_init()
+
+    def vecfft_from_rotfft(self, rot_fft):
+        ux = 1j * self.KY * self.inv_K_square_nozero * rot_fft
+        uy = -1j * self.KX * self.inv_K_square_nozero * rot_fft
+        return ux, uy
+
+    def rotfft_from_vecfft(self, vecx_fft, vecy_fft):
+        return 1j * (self.KX * vecy_fft - self.KY * vecx_fft)
+
+    def divfft_from_vecfft(self, vecx_fft, vecy_fft):
+        return 1j * (self.KX * vecx_fft + self.KY * vecy_fft)
+
+    def gradfft_from_fft(self, f_fft):
+        return 1j * self.KX * f_fft, 1j * self.KY * f_fft
+
+    def laplacian_fft(self, a_fft, order=2):
+        return a_fft * self.K2 ** (order // 2)
+
+    def invlaplacian_fft(self, a_fft, order=2):
+        r = a_fft / self.K2_not0 ** (order // 2)
+        r[0, 0] = 0.0
+        return r
+
+    def get_XY_loc(self):
+        Y, X = torch.meshgrid(self.y, self.x, indexing="ij")
+        return X, Y
+
+    def produce_str_describing_oper(self):
+        return f"{self.nx}x{self.ny}"
+
+
+class OperatorsPseudoSpectral3D(_OperBase):
+    ndim = 3
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        """Same defaults as ``operators3d.py:152-168``."""
+        params._set_child("oper", attribs={
+            "type_fft": "default", "type_fft2d": "sequential", "coef_dealiasing": 2.0 / 3,
+            "nx": 48, "ny": 48, "nz": 48, "Lx": 2 * pi, "Ly": 2 * pi, "Lz": 2 * pi,
+            "truncation_shape": "cubic", "NO_SHEAR_MODES": False})
+
+    def __init__(self, params, precision="float64", device=None):
+        self.params = params
+        po = params.oper
+        if po.truncation_shape != "cubic" or po.NO_SHEAR_MODES:
+            raise NotImplementedError("only the cubic truncation is implemented on GB300")
+        self.axes = ("z", "y", "x")
+        self.nx, self.ny, self.nz = int(po.nx), int(po.ny), int(po.nz)
+        self.Lx, self.Ly, self.Lz = float(po.Lx), float(po.Ly), float(po.Lz)
+        self.coef_dealiasing = po.coef_dealiasing
+        cls = import_fft_class(po.type_fft, 3)
+        self.opfft = self.oper_fft = cls(self.nz, self.ny, self.nx, precision=precision,
+                                         device=device)
+        self.device = self.opfft.device
+        self.rdtype, self.cdtype = self.opfft.rdtype, self.opfft.cdtype
+        self.shapeX = self.shapeX_seq = self.shapeX_loc = (self.nz, self.ny, self.nx)
+        self.shapeK = self.shapeK_seq = self.shapeK_loc = (self.nz, self.ny, self.nx // 2 + 1)
+        self.seq_indices_first_K = (0, 0, 0)
+        self.dimX_K = (0, 1, 2)
+        self.deltax, self.deltay, self.deltaz = (self.Lx / self.nx, self.Ly / self.ny,
+                                                 self.Lz / self.nz)
+        self.deltakx, self.deltaky, self.deltakz = (2 * pi / self.Lx, 2 * pi / self.Ly,
+                                                    2 * pi / self.Lz)
+        self._lengths = (self.Lz, self.Ly, self.Lx)
+        self.kcut = (cubic_dealias_cutoff(self.nz, self.Lz, self.coef_dealiasing),
+                     cubic_dealias_cutoff(self.ny, self.Ly, self.coef_dealiasing),
+                     cubic_dealias_cutoff(self.nx, self.Lx, self.coef_dealiasing))
+        dev, rd = self.device, self.rdtype
+        self.kx = torch.tensor(self.deltakx * np.arange(self.nx // 2 + 1), dtype=rd, device=dev)
+        self.ky = torch.tensor(self.deltaky * _kadim(self.ny), dtype=rd, device=dev)
+        self.kz = torch.tensor(self.deltakz * _kadim(self.nz), dtype=rd, device=dev)
+        self.Kx = self.kx[None, None, :].expand(self.shapeK)
+        self.Ky = self.ky[None, :, None].expand(self.shapeK)
+        self.Kz = self.kz[:, None, None].expand(self.shapeK)
+        self._finish_init()
+
+    # full-size arrays are built on demand (a 512^3 float64 K2 is 0.5 GB)
+    @property
+    def K2(self):
+        return self.Kx**2 + self.Ky**2 + self.Kz**2
+
+    @property
+    def K4(self):
+        return self.K2**2
+
+    @property
+    def K8(self):
+        return self.K4**2
+
+    @property
+    def K2_not0(self):
+        K2 = self.K2
+        K2[0, 0, 0] = 1e-14
+        return K2
+
+    @property
+    def inv_K_square_nozero(self):
+        return 1.0 / self.K2_not0
+
+    def rotfft_from_vecfft(self, vx_fft, vy_fft, vz_fft):
+        return (1j * (self.Ky * vz_fft - self.Kz * vy_fft),
+                1j * (self.Kz * vx_fft - self.Kx * vz_fft),
+                1j * (self.Kx * vy_fft - self.Ky * vx_fft))
+
+    def rotfft_from_vecfft_outin(self, vx_fft, vy_fft, vz_fft, rx, ry, rz):
+        ox, oy, oz = self.rotfft_from_vecfft(vx_fft, vy_fft, vz_fft)
+        rx.copy_(ox)
+        ry.copy_(oy)
+        rz.copy_(oz)
+
+    def divfft_from_vecfft(self, vx_fft, vy_fft, vz_fft):
+        return 1j * (self.Kx * vx_fft + self.Ky * vy_fft + self.Kz * vz_fft)
+
+    def project_perpk3d(self, vx_fft, vy_fft, vz_fft):
+        tmp = (self.Kx * vx_fft + self.Ky * vy_fft + self.Kz * vz_fft) * self.inv_K_square_nozero
+        vx_fft.sub_(self.Kx * tmp)
+        vy_fft.sub_(self.Ky * tmp)
+        vz_fft.sub_(self.Kz * tmp)
+
+    def produce_str_describing_oper(self):
+        return f"{self.nx}x{self.ny}x{self.nz}"

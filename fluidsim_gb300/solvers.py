@@ -1,0 +1,373 @@
+"""ns2d / ns3d solvers whose time step runs in libgbspec on one GB300.
+
+The class layout follows fluidsim's (``Simul`` with ``create_default_params``
+and ``tendencies_nonlin``, ``State`` with ``state_spect`` / ``state_phys``,
+``TimeSteppingPseudoSpectral`` with ``start`` / ``one_time_step``, ``Output``
+with the spatial means), so solver scripts written for
+``fluidsim.solvers.ns2d`` / ``ns3d`` run unchanged on the parts listed here:
+
+* ``fluidsim/solvers/ns2d/solver.py:111-194`` / ``ns3d/solver.py:180-263``
+  -> ``Simul.tendencies_nonlin`` (fused kernels, ``gbs_ns_tendencies``);
+* ``fluidsim/base/time_stepping/pseudo_spect.py:798-984`` (RK4 with exact
+  integrating factor) + ``one_time_step_computation`` (236-243, ns3d
+  ``time_stepping.py:8-20``) -> ``gbs_ns_step_rk4``;
+* ``fluidsim/base/time_stepping/base.py:182-354`` (loop, CFL with the 2 %
+  hysteresis, ``max_elapsed``, SIGUSR2 stop) -> ``TimeSteppingPseudoSpectral``;
+* spatial means / spectra (FP64 device reductions).
+
+State arrays are CUDA tensors in the sequential fluidfft layout; the
+precision is chosen with ``params.precision`` ("float64" or "float32").
+"""
+
+import ctypes
+import signal
+from datetime import datetime, timedelta
+from math import pi
+from time import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .fft import current_stream_handle
+from .operators import OperatorsPseudoSpectral2D, OperatorsPseudoSpectral3D
+from .params import Parameters
+
+
+class StatePseudoSpectral:
+    """``fluidsim/base/state.py:209-392`` on device tensors."""
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.oper = sim.oper
+        self.keys_state_spect = list(sim.keys_state_spect)
+        self.keys_state_phys = list(sim.keys_state_phys)
+        self.state_spect = torch.zeros((len(self.keys_state_spect),) + self.oper.shapeK,
+                                       dtype=self.oper.cdtype, device=self.oper.device)
+        self._phys = None
+        self._phys_stamp = None
+        self.is_initialized = False
+
+    # state_phys is regenerated lazily from state_spect (3 C2R transforms)
+    def _stamp(self):
+        return (self.sim.time_stepping.it, self.state_spect._version)
+
+    @property
+    def state_phys(self):
+        if self._phys is None or self._phys_stamp != self._stamp():
+            self._phys = self.sim._statephys_from_statespect(self.state_spect)
+            self._phys_stamp = self._stamp()
+        return self._phys
+
+    def statephys_from_statespect(self):
+        self._phys = None
+        return self.state_phys
+
+    def get_var(self, key):
+        if key in self.keys_state_spect:
+            return self.state_spect[self.keys_state_spect.index(key)]
+        if key in self.keys_state_phys:
+            return self.state_phys[self.keys_state_phys.index(key)]
+        raise ValueError(f'Do not know how to compute "{key}".')
+
+    def has_vars(self, *keys):
+        return set(keys).issubset(set(self.keys_state_spect + self.keys_state_phys))
+
+    def init_statespect_from(self, **kwargs):
+        """``fluidsim/base/state.py:345-382``: other keys are set to zero."""
+        self.state_spect.zero_()
+        for key, value in kwargs.items():
+            if key not in self.keys_state_spect:
+                raise ValueError(f"Do not know how to initialize with key '{key}'.")
+            v = value if isinstance(value, torch.Tensor) else torch.from_numpy(np.asarray(value))
+            self.state_spect[self.keys_state_spect.index(key)].copy_(v)
+        self._phys = None
+        self.is_initialized = True
+
+
+class TimeSteppingPseudoSpectral:
+    """RK4 pseudo-spectral time stepping with the reference loop semantics."""
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        # base.py:33-46 + pseudo_spect.py:159-167 (USE_CFL = True)
+        params._set_child("time_stepping", attribs={
+            "USE_T_END": True, "t_end": 10.0, "it_end": 10, "USE_CFL": True,
+            "type_time_scheme": "RK4", "deltat0": 0.2, "deltat_max": 0.2,
+            "cfl_coef": None, "max_elapsed": None})
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.params = sim.params
+        pts = self.params.time_stepping
+        self.it = 0
+        self.t = 0.0
+        self._has_to_stop = False
+        self._stop_signal_received = False
+        if pts.type_time_scheme != "RK4":
+            raise NotImplementedError(
+                f"type_time_scheme {pts.type_time_scheme!r}: only RK4 runs on GB300")
+        if pts.USE_CFL:
+            self.CFL = pts.cfl_coef if pts.cfl_coef is not None else 1.0
+        self.deltat = pts.deltat0
+        self.deltat_max = pts.deltat_max
+        self._nan_check = True
+
+        def handler(signum, stack):
+            self._stop_signal_received = signum
+
+        try:
+            signal.signal(signal.SIGUSR2, handler)
+        except (ValueError, AttributeError):
+            pass
+        self.max_elapsed = None
+        if pts.max_elapsed is not None:
+            try:
+                self.max_elapsed = float(pts.max_elapsed)
+            except ValueError:
+                tt = datetime.strptime(pts.max_elapsed, "%H:%M:%S")
+                self.max_elapsed = timedelta(
+                    hours=tt.hour, minutes=tt.minute, seconds=tt.second).total_seconds()
+            self._time_should_stop = time() + self.max_elapsed
+
+    def start(self):
+        self.main_loop()
+
+    def main_loop(self, print_begin=False, save_init_field=False):
+        pts = self.params.time_stepping
+        if pts.USE_T_END:
+            while self.t < pts.t_end and not self._has_to_stop:
+                self.one_time_step()
+        else:
+            while self.it < pts.it_end and not self._has_to_stop:
+                self.one_time_step()
+
+    def one_time_step(self):
+        """``fluidsim/base/time_stepping/base.py:208-244``."""
+        if self.max_elapsed is not None and time() > self._time_should_stop:
+            self._has_to_stop = True
+        if self._stop_signal_received:
+            self._has_to_stop = True
+        self.sim.output.one_time_step()
+        self.one_time_step_computation()
+        self.t += self.deltat
+        self.it += 1
+
+    def one_time_step_computation(self):
+        """RK4 + projection (ns3d) + dealiasing + NaN check, one library call."""
+        pts = self.params.time_stepping
+        dt = ctypes.c_double(self.deltat)
+        cfl = (ctypes.c_double * 2)(self.CFL, self.deltat_max) if pts.USE_CFL else None
+        rc = self.sim._lib.gbs_ns_step_rk4(
+            self.sim._solver, ctypes.c_void_p(self.sim.state.state_spect.data_ptr()),
+            ctypes.byref(dt), cfl, int(self._nan_check), current_stream_handle())
+        self.deltat = dt.value
+        self.sim.state._phys = None
+        if rc == _lib.GBS_ENAN:
+            raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")
+        _lib.check(rc, "gbs_ns_step_rk4")
+
+
+class Output:
+    """Spatial means and spectra (FP64 device reductions)."""
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        params._set_child("output", attribs={"HAS_TO_SAVE": False, "sub_directory": ""})
+        params.output._set_child("periods_save", attribs={"spatial_means": 0.0})
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.spatial_means_series = []
+        self._t_last = -np.inf
+
+    def one_time_step(self):
+        period = self.sim.params.output.periods_save.spatial_means
+        ts = self.sim.time_stepping
+        if period and ts.t >= self._t_last + period:
+            self._t_last = ts.t
+            self.spatial_means_series.append({"t": ts.t, **self.compute_spatial_means()})
+
+    def compute_spatial_means(self):
+        out = (ctypes.c_double * 6)()
+        sim = self.sim
+        _lib.check(sim._lib.gbs_ns_spatial_means(
+            sim._solver, ctypes.c_void_p(sim.state.state_spect.data_ptr()), out,
+            current_stream_handle()), "gbs_ns_spatial_means")
+        return dict(zip(sim._means_keys, list(out)))
+
+    def compute_energy(self):
+        return self.compute_spatial_means()["E"]
+
+    def compute_spectrum(self):
+        """(k, E(k)) shell spectrum, bins round(|k|/dk_min)."""
+        sim = self.sim
+        nk = ctypes.c_int64()
+        _lib.check(sim._lib.gbs_ns_spectrum_size(sim._solver, ctypes.byref(nk)))
+        spec = torch.empty(nk.value, dtype=torch.float64, device=sim.oper.device)
+        _lib.check(sim._lib.gbs_ns_spectrum(
+            sim._solver, ctypes.c_void_p(sim.state.state_spect.data_ptr()),
+            ctypes.c_void_p(spec.data_ptr()), current_stream_handle()))
+        dk = min(sim.oper.deltakx, sim.oper.deltaky,
+                 getattr(sim.oper, "deltakz", np.inf))
+        return dk * np.arange(nk.value), spec.cpu().numpy()
+
+    def print_stdout(self, *args, **kwargs):
+        print(*args, **kwargs)
+
+
+class _SimulBase:
+    Operators = None
+    ndim = None
+
+    @classmethod
+    def create_default_params(cls):
+        params = Parameters("params", {
+            "short_name_type_run": "", "NEW_DIR_RESULTS": True, "ONLY_COARSE_OPER": False,
+            "nu_2": 0.0, "nu_4": 0.0, "nu_8": 0.0, "nu_m4": 0.0,
+            "precision": "float64"})
+        cls.Operators._complete_params_with_default(params)
+        params.oper._set_attribs({"type_fft": "default"})
+        TimeSteppingPseudoSpectral._complete_params_with_default(params)
+        Output._complete_params_with_default(params)
+        params._set_child("init_fields", attribs={"type": "in_script"})
+        params._set_child("forcing", attribs={"enable": False, "type": ""})
+        cls._complete_params_with_default(params)
+        return params
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        pass
+
+    def __init__(self, params):
+        self.params = params
+        if params.forcing.enable:
+            raise NotImplementedError("forcing is not implemented on GB300 yet")
+        if params.init_fields.type != "in_script":
+            raise NotImplementedError("only init_fields.type = 'in_script' is supported")
+        self._lib = _lib.load()
+        self.oper = self.Operators(params, precision=params.precision)
+        self.state = StatePseudoSpectral(self)
+        self.output = Output(self)
+        self._solver = ctypes.c_void_p()
+        p = self._ns_params()
+        with torch.cuda.device(self.oper.device):
+            _lib.check(self._lib.gbs_ns_create(ctypes.byref(p), ctypes.byref(self._solver)),
+                       "gbs_ns_create")
+        self.time_stepping = TimeSteppingPseudoSpectral(self)
+        self.is_forcing_enabled = False
+
+    def __del__(self):
+        lib = getattr(self, "_lib", None)
+        solver = getattr(self, "_solver", None)
+        if lib is not None and solver:
+            lib.gbs_ns_destroy(solver)
+            self._solver = None
+
+    def _ns_params(self):
+        prm = self.params
+        o = self.oper
+        p = _lib.NSParams()
+        p.ndim = self.ndim
+        p.nx, p.ny = o.nx, o.ny
+        p.nz = o.nz if self.ndim == 3 else 1
+        p.Lx, p.Ly = o.Lx, o.Ly
+        p.Lz = o.Lz if self.ndim == 3 else 1.0
+        p.nu_2, p.nu_4, p.nu_8, p.nu_m4 = prm.nu_2, prm.nu_4, prm.nu_8, prm.nu_m4
+        p.kcut_x = o.kcut[-1]
+        p.kcut_y = o.kcut[-2]
+        p.kcut_z = o.kcut[0] if self.ndim == 3 else 1
+        p.dtype = _lib.GBS_F64 if prm.precision == "float64" else _lib.GBS_F32
+        return p
+
+    def tendencies_nonlin(self, state_spect=None, old=None):
+        """Dealiased nonlinear tendencies of ``state_spect`` (default: the state)."""
+        S = self.state.state_spect if state_spect is None else state_spect
+        if not isinstance(S, torch.Tensor):
+            S = torch.from_numpy(np.ascontiguousarray(S)).to(self.oper.device, self.oper.cdtype)
+        if old is None:
+            old = torch.empty_like(self.state.state_spect)
+        _lib.check(self._lib.gbs_ns_tendencies(
+            self._solver, ctypes.c_void_p(S.contiguous().data_ptr()),
+            ctypes.c_void_p(old.data_ptr()), current_stream_handle()), "tendencies_nonlin")
+        return old
+
+    def max_velocity(self):
+        out = (ctypes.c_double * 3)()
+        _lib.check(self._lib.gbs_ns_max_velocity(
+            self._solver, ctypes.c_void_p(self.state.state_spect.data_ptr()), out,
+            current_stream_handle()))
+        return list(out)[: self.ndim]
+
+
+class SimulNS2D(_SimulBase):
+    """``fluidsim.solvers.ns2d.solver.Simul`` on GB300 (state: rot_fft)."""
+
+    Operators = OperatorsPseudoSpectral2D
+    ndim = 2
+    keys_state_spect = ("rot_fft",)
+    keys_state_phys = ("ux", "uy", "rot")  # ns2d/state.py:31
+    _means_keys = ("E", "Z", "epsK", "epsK_hypo", "epsZ", "epsZ_hypo")
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        params._set_attribs({"beta": 0.0})
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        p.beta = self.params.beta
+        return p
+
+    def _statephys_from_statespect(self, S):
+        """``ns2d/state.py:95-106``: (ux, uy, rot)."""
+        rot_fft = S[0]
+        ux_fft, uy_fft = self.oper.vecfft_from_rotfft(rot_fft)
+        K = torch.stack([ux_fft, uy_fft, rot_fft])
+        X = torch.empty((3,) + self.oper.shapeX, dtype=self.oper.rdtype, device=self.oper.device)
+        self.oper.opfft.ifft_as_arg_destroy(K, X)
+        return X
+
+    def init_from_rotfft(self, rot_fft):
+        """``ns2d/state.py:115-119``: dealiased, then state_phys."""
+        r = rot_fft if isinstance(rot_fft, torch.Tensor) else torch.from_numpy(np.asarray(rot_fft))
+        r = r.to(self.oper.device, self.oper.cdtype).clone()
+        self.oper.dealiasing(r)
+        self.state.init_statespect_from(rot_fft=r)
+
+
+class SimulNS3D(_SimulBase):
+    """``fluidsim.solvers.ns3d.solver.Simul`` on GB300 (vx_fft, vy_fft, vz_fft)."""
+
+    Operators = OperatorsPseudoSpectral3D
+    ndim = 3
+    keys_state_spect = ("vx_fft", "vy_fft", "vz_fft")
+    keys_state_phys = ("vx", "vy", "vz")  # ns3d/state.py:20
+    _means_keys = ("E", "Ex", "Ey", "Ez", "epsK", "epsK_hypo")
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        params._set_attribs({"f": None, "no_vz_kz0": False, "projection": None})
+
+    def __init__(self, params):
+        if params.no_vz_kz0 or params.projection is not None:
+            raise NotImplementedError("no_vz_kz0 / toroidal / poloidal projections")
+        super().__init__(params)
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        if self.params.f is not None:
+            p.has_f = 1
+            p.f = float(self.params.f)
+        return p
+
+    def _statephys_from_statespect(self, S):
+        X = torch.empty((3,) + self.oper.shapeX, dtype=self.oper.rdtype, device=self.oper.device)
+        self.oper.opfft.ifft_as_arg(S.contiguous(), X)
+        return X
+
+    def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
+        """``ns3d/state.py:124-130``: set, then phys -> spect round trip."""
+        self.state.init_statespect_from(vx_fft=vx_fft, vy_fft=vy_fft, vz_fft=vz_fft)
+        X = self.state.state_phys
+        self.oper.opfft.fft_as_arg(X.contiguous(), self.state.state_spect)
+        self.state._phys = None

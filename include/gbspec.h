@@ -1,0 +1,141 @@
+/*
+ * gbspec.h — C ABI of libgbspec, the GB300 (sm_103a) pseudo-spectral time
+ * step behind fluidsim's fluidfft plugin / operator / time-stepping API.
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a negative errno-like code
+ *     (GBS_E*); gbs_last_error() gives a message for the calling thread.
+ *     No C++ exception crosses this boundary.
+ *   - Arrays are device pointers, C order, in fluidfft's sequential layout:
+ *       physical  (nz, ny, nx)        / (ny, nx)          real
+ *       spectral  (nz, ny, nx/2 + 1)  / (ny, nx/2 + 1)    complex (re, im)
+ *     with `batch` (or nvar) such fields stored back to back.
+ *   - dtype GBS_F64: double / complex128;  GBS_F32: float / complex64.
+ *   - The forward transform is divided by the number of points, the
+ *     inverse is not normalised (fluidsim/base/state.py:385-392).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous unless stated; plans / solvers own their workspaces and
+ *     allocate nothing after creation.  A handle is not re-entrant; distinct
+ *     handles are independent.
+ */
+#ifndef GBSPEC_H
+#define GBSPEC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBS_OK 0
+#define GBS_EINVAL (-22) /* bad argument (maps to ValueError)            */
+#define GBS_ENOMEM (-12) /* device allocation failed (MemoryError)       */
+#define GBS_ECUDA (-5)   /* CUDA runtime error (RuntimeError)            */
+#define GBS_ENAN (-33)   /* NaN in the state after a step (ValueError)   */
+
+#define GBS_F32 0
+#define GBS_F64 1
+
+typedef struct gbs_fft_plan gbs_fft_plan;
+typedef struct gbs_ns gbs_ns;
+
+/* Message describing the last error on the calling thread ("" if none). */
+const char* gbs_last_error(void);
+
+/* Library version string. */
+const char* gbs_version(void);
+
+/* ------------------------------------------------------------- FFT plans
+ * Replaces the fluidfft fft2d/fft3d class constructor and transforms
+ * (fluidfft 0.4.2, selected at fluidsim/operators/operators3d.py:222-231 and
+ * operators2d.py:137-144; called as oper.fft_as_arg / ifft_as_arg /
+ * ifft_as_arg_destroy, e.g. fluidsim/solvers/ns3d/solver.py:210-241).
+ * shapeX = (nz, ny, nx) for ndim 3, (ny, nx) for ndim 2; nx must be even.
+ */
+int gbs_fft_plan_create(int ndim, const int64_t* shapeX, int dtype, int batch,
+                        gbs_fft_plan** plan);
+int gbs_fft_plan_destroy(gbs_fft_plan* plan);
+
+/* fft_as_arg: k = rfftn(x) / N for each of `batch` fields. */
+int gbs_fft_r2c(gbs_fft_plan* plan, const void* x, void* k, void* stream);
+
+/* ifft_as_arg (may_destroy = 0: k is preserved, the plan workspace is used)
+ * and ifft_as_arg_destroy (may_destroy = 1: k is used as workspace). */
+int gbs_fft_c2r(gbs_fft_plan* plan, void* k, void* x, int may_destroy,
+                void* stream);
+
+/* ----------------------------------------------------- ns2d / ns3d solver
+ * Parameters of the fused pseudo-spectral step.  ndim 2: ns2d (one state
+ * variable rot_fft, fluidsim/solvers/ns2d/solver.py:111-194); ndim 3: ns3d
+ * (vx_fft, vy_fft, vz_fft, fluidsim/solvers/ns3d/solver.py:180-263).
+ * Dissipation sigma(k) = nu_2 k^2 + nu_4 k^4 + nu_8 k^8 (+ nu_m4 / k^4)
+ * as fluidsim/base/solvers/pseudo_spect.py:134-191.
+ * Cubic dealiasing removes modes with |k_adim| >= kcut_* along any axis
+ * (kcut = n: nothing removed along that axis).
+ */
+typedef struct gbs_ns_params {
+  int ndim;
+  int64_t nx, ny, nz; /* nz = 1 for ndim 2 */
+  double Lx, Ly, Lz;
+  double nu_2, nu_4, nu_8, nu_m4;
+  double beta;  /* ns2d: beta-plane term of compute_Frot              */
+  double f;     /* ns3d: Coriolis parameter added to omega_z(k=0)      */
+  int has_f;    /* ns3d: 1 when params.f is not None                   */
+  int64_t kcut_x, kcut_y, kcut_z;
+  int dtype;
+} gbs_ns_params;
+
+int gbs_ns_create(const gbs_ns_params* params, gbs_ns** solver);
+int gbs_ns_destroy(gbs_ns* solver);
+
+/* Simul.tendencies_nonlin(state_spect): tend = dealias(P_perp FFT(v x w))
+ * (ns3d) or dealias(FFT(-u.grad(rot) - beta u_y)) (ns2d). */
+int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
+                      void* stream);
+
+/* One RK4 step with exact integrating factor, followed by projection
+ * (ns3d), dealiasing and the NaN check: TimeSteppingPseudoSpectral
+ * ._time_step_RK4 (fluidsim/base/time_stepping/pseudo_spect.py:798-984) +
+ * one_time_step_computation (pseudo_spect.py:236-243,
+ * fluidsim/solvers/ns3d/time_stepping.py:8-20).  state_spect is updated in
+ * place.  *dt is the time increment; when cfl != NULL the CFL rule of
+ * fluidsim/base/time_stepping/base.py:320-354 is applied first (from the
+ * velocity of the current state, which the step computes anyway) and *dt is
+ * updated: cfl[0] = CFL coefficient, cfl[1] = deltat_max.  That path
+ * synchronises the stream once.  Returns GBS_ENAN (after completing the
+ * step) when state_spect[0] holds a NaN; the NaN check synchronises the
+ * stream unless check_nan = 0. */
+int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
+                    const double* cfl, int check_nan, void* stream);
+
+/* max |u_i| over the physical grid of state_spect (ns2d: ux, uy; ns3d: vx,
+ * vy, vz) into out[ndim] (host).  Synchronises the stream. */
+int gbs_ns_max_velocity(gbs_ns* solver, const void* state_spect, double* out,
+                        void* stream);
+
+/* Host-only CFL update, fluidsim/base/time_stepping/base.py:334-354:
+ * tmp = sum_i max|u_i| / dx_i.  Returns the new dt (dt if the relative
+ * change is <= 2 %). */
+double gbs_cfl_update(double dt, double tmp, double cfl_coef,
+                      double deltat_max);
+
+/* FP64 spatial means from the spectral state (Hermitian-weighted sums,
+ * fluidsim/solvers/ns2d/output/spatial_means.py:23-36,
+ * fluidsim/solvers/ns3d/output/spatial_means.py:23-40).
+ * out (host): ns2d {E, Z, epsK, epsK_hypo, epsZ, epsZ_hypo};
+ *             ns3d {E, Ex, Ey, Ez, epsK, epsK_hypo}.  Synchronises. */
+int gbs_ns_spatial_means(gbs_ns* solver, const void* state_spect, double* out,
+                         void* stream);
+
+/* Shell energy spectrum in FP64 (device output spectrum[nk], nk from
+ * gbs_ns_spectrum_size): bins round(|k| / dk_min), E summed with Hermitian
+ * weights, divided by dk_min. */
+int gbs_ns_spectrum_size(gbs_ns* solver, int64_t* nk);
+int gbs_ns_spectrum(gbs_ns* solver, const void* state_spect, double* spectrum,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSPEC_H */

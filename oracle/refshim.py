@@ -1,0 +1,283 @@
+"""Run the reference's OWN time-stepping and tendency code on numpy shims.
+
+Test infrastructure only (see ``oracle/__init__.py``); used by
+``tests/golden/make_golden.py`` in an environment that has the fluidsim
+0.8.3 sources.  It never runs where those sources are absent.
+
+The following reference files are executed unmodified, loaded with
+``importlib`` from ``<reference>/fluidsim/...`` (``fluidsim/__init__.py`` is
+bypassed because it needs fluiddyn/h5py/matplotlib, which are absent):
+
+* ``fluidsim/base/time_stepping/base.py``          (loop, CFL, hysteresis)
+* ``fluidsim/base/time_stepping/pseudo_spect.py``  (ExactLinearCoefs, RK4)
+* ``fluidsim/base/solvers/pseudo_spect.py``        (compute_freq_diss)
+* ``fluidsim/base/state.py``                       (StatePseudoSpectral)
+* ``fluidsim/base/setofvariables.py``
+* ``fluidsim/solvers/ns2d/solver.py``, ``state.py``
+* ``fluidsim/solvers/ns3d/solver.py``, ``state.py``, ``time_stepping.py``
+
+Shimmed (written here, not taken from anywhere): ``transonic`` (no-op
+``boost``, ``Transonic().is_transpiled == False`` so the pure-Python
+branches of the transonic blocks run), ``fluiddyn.util.mpi`` (one rank),
+``fluiddyn.calcul.setofvariables.SetOfVariables`` (ndarray subclass),
+``fluidfft.fft3d.operators.vector_product``, and the fluidfft operator
+object (``oracle.spectral``).  ``fluidsim.base.solvers.base`` and
+``fluidsim.operators.operators3d`` are replaced by minimal stand-ins because
+they pull in the parameter/IO machinery; the Simul objects are wired by hand
+below instead of by ``SimulBase.__init__``.
+"""
+
+import importlib.util
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+from .spectral import OperNumpy2D, OperNumpy3D
+
+
+class _Anything:
+    """Accepts the transonic type-annotation syntax and ignores it."""
+
+    def __init__(self, *a, **k):
+        pass
+
+    def __getitem__(self, item):
+        return _Anything()
+
+    def __sub__(self, other):
+        return _Anything()
+
+    __add__ = __sub__
+
+    def __call__(self, *a, **k):
+        return _Anything()
+
+
+class _Transonic:
+    is_transpiled = False
+    is_transpiling = False
+    is_compiled = False
+
+    def use_block(self, name):  # pragma: no cover - never reached
+        raise RuntimeError("transpiled blocks are not available")
+
+
+def _boost(obj=None, **kw):
+    if obj is None:
+        return lambda o: o
+    return obj
+
+
+class SetOfVariables(np.ndarray):
+    """Minimal stand-in for ``fluiddyn.calcul.setofvariables.SetOfVariables``."""
+
+    def __new__(cls, keys=None, shape_variable=None, like=None, value=None,
+                info=None, dtype=None):
+        if like is not None:
+            keys = list(like.keys)
+            shape_variable = like.shape[1:]
+            dtype = like.dtype if dtype is None else dtype
+            info = like.info if info is None else info
+        obj = np.empty((len(keys),) + tuple(shape_variable), dtype=dtype).view(cls)
+        obj.keys = list(keys)
+        obj.nvar = len(keys)
+        obj.info = info
+        if value is not None:
+            obj.fill(value)
+        return obj
+
+    def __array_finalize__(self, obj):
+        if obj is None:
+            return
+        self.keys = getattr(obj, "keys", None)
+        self.nvar = getattr(obj, "nvar", None)
+        self.info = getattr(obj, "info", None)
+
+    def get_var(self, key):
+        return np.asarray(self)[self.keys.index(key)]
+
+    def set_var(self, key, value):
+        np.asarray(self)[self.keys.index(key)] = value
+
+    def initialize(self, value=0):
+        self.fill(value)
+
+
+def vector_product(ax, ay, az, bx, by, bz):
+    """Shim for fluidfft's ``vector_product``: ``a x b``."""
+    return ay * bz - az * by, az * bx - ax * bz, ax * by - ay * bx
+
+
+class _Container:
+    """Attribute container with the ``_set_attribs`` / ``_set_child`` calls."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+    def _set_attribs(self, d):
+        self.__dict__.update(d)
+
+    def _set_child(self, name, attribs=None):
+        child = _Container(**(attribs or {}))
+        setattr(self, name, child)
+        return child
+
+
+class _OutputStub:
+    def one_time_step(self):
+        pass
+
+    def print_stdout(self, *a, **k):
+        pass
+
+
+_LOADED = {}
+
+
+def _module(name, path=None, package=False):
+    if name in sys.modules and name in _LOADED:
+        return sys.modules[name]
+    if path is None:
+        mod = types.ModuleType(name)
+        if package:
+            mod.__path__ = []
+    else:
+        spec = importlib.util.spec_from_file_location(name, str(path))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    sys.modules[name] = mod
+    _LOADED[name] = mod
+    parent, _, child = name.rpartition(".")
+    if parent and parent in sys.modules:
+        setattr(sys.modules[parent], child, mod)
+    return mod
+
+
+def load_reference(root):
+    """Install the shims and load the reference modules; returns a dict."""
+    root = Path(root)
+    fs = root / "fluidsim"
+    if not (fs / "base" / "time_stepping" / "pseudo_spect.py").exists():
+        raise FileNotFoundError(f"fluidsim sources not found under {root}")
+
+    tr = _module("transonic")
+    tr.boost = _boost
+    tr.Transonic = _Transonic
+    tr.Type = tr.NDim = _Anything
+    tr.Array = tr.Union = _Anything()
+
+    _module("fluiddyn", package=True)
+    _module("fluiddyn.util", package=True)
+    mpi = _module("fluiddyn.util.mpi")
+    mpi.rank, mpi.nb_proc, mpi.comm = 0, 1, None
+    mpi.printby0 = print
+    _module("fluiddyn.calcul", package=True)
+    _module("fluiddyn.calcul.setofvariables").SetOfVariables = SetOfVariables
+    _module("fluidfft", package=True)
+    _module("fluidfft.fft3d", package=True)
+    _module("fluidfft.fft3d.operators").vector_product = vector_product
+
+    for pkg in ("fluidsim", "fluidsim.base", "fluidsim.base.solvers",
+                "fluidsim.base.time_stepping", "fluidsim.solvers",
+                "fluidsim.solvers.ns2d", "fluidsim.solvers.ns3d",
+                "fluidsim.operators"):
+        _module(pkg, package=True)
+
+    _module("fluidsim.base.setofvariables", fs / "base" / "setofvariables.py")
+
+    sb = _module("fluidsim.base.solvers.base")
+
+    class InfoSolverBase(_Container):
+        pass
+
+    class SimulBase:
+        pass
+
+    sb.InfoSolverBase, sb.SimulBase = InfoSolverBase, SimulBase
+
+    op3 = _module("fluidsim.operators.operators3d")
+
+    def dealiasing_variable(ff_fft, where_dealiased):
+        ff_fft[np.nonzero(where_dealiased)] = 0.0
+
+    op3.dealiasing_variable = dealiasing_variable
+
+    m = {}
+    m["ps_solver"] = _module("fluidsim.base.solvers.pseudo_spect",
+                             fs / "base" / "solvers" / "pseudo_spect.py")
+    m["ts_base"] = _module("fluidsim.base.time_stepping.base",
+                           fs / "base" / "time_stepping" / "base.py")
+    m["ts_ps"] = _module("fluidsim.base.time_stepping.pseudo_spect",
+                         fs / "base" / "time_stepping" / "pseudo_spect.py")
+    m["state"] = _module("fluidsim.base.state", fs / "base" / "state.py")
+    m["ns2d_solver"] = _module("fluidsim.solvers.ns2d.solver",
+                               fs / "solvers" / "ns2d" / "solver.py")
+    m["ns2d_state"] = _module("fluidsim.solvers.ns2d.state",
+                              fs / "solvers" / "ns2d" / "state.py")
+    m["ns3d_solver"] = _module("fluidsim.solvers.ns3d.solver",
+                               fs / "solvers" / "ns3d" / "solver.py")
+    m["ns3d_state"] = _module("fluidsim.solvers.ns3d.state",
+                              fs / "solvers" / "ns3d" / "state.py")
+    m["ns3d_ts"] = _module("fluidsim.solvers.ns3d.time_stepping",
+                           fs / "solvers" / "ns3d" / "time_stepping.py")
+    return m
+
+
+def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
+            extra):
+    p = _Container(nu_2=nu_2, nu_4=nu_4, nu_8=nu_8, nu_m4=nu_m4)
+    p.__dict__.update(extra)
+    p.forcing = _Container(enable=False)
+    p.time_stepping = _Container(
+        USE_T_END=False, t_end=10.0, it_end=10, USE_CFL=USE_CFL,
+        type_time_scheme="RK4", deltat0=deltat0, deltat_max=deltat_max,
+        cfl_coef=cfl_coef, max_elapsed=None,
+    )
+    return p
+
+
+def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
+              nu_m4=0.0, beta=0.0, USE_CFL=False, deltat0=0.2,
+              deltat_max=0.2, cfl_coef=None):
+    """A reference ns2d ``Simul`` (RK4) wired around ``oper``."""
+    Simul = mods["ns2d_solver"].Simul
+    sim = object.__new__(Simul)
+    sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
+                         deltat_max, cfl_coef, {"beta": beta})
+    info = _Container(solver=_Container(classes=_Container(State=_Container())))
+    mods["ns2d_state"].StateNS2D._complete_info_solver(info.solver)
+    sim.info = info
+    sim.oper = oper
+    sim.output = _OutputStub()
+    sim.is_forcing_enabled = False
+    sim.state = mods["ns2d_state"].StateNS2D(sim)
+    sim.state.state_spect[:] = 0.0
+    sim.state.state_phys[:] = 0.0
+    sim.time_stepping = mods["ts_ps"].TimeSteppingPseudoSpectral(sim)
+    return sim
+
+
+def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
+              nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
+              cfl_coef=None):
+    """A reference ns3d ``Simul`` (RK4) wired around ``oper``."""
+    Simul = mods["ns3d_solver"].Simul
+    sim = object.__new__(Simul)
+    sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
+                         deltat_max, cfl_coef,
+                         {"f": f, "no_vz_kz0": False, "projection": None})
+    info = _Container(solver=_Container(classes=_Container(State=_Container())))
+    mods["ns3d_state"].StateNS3D._complete_info_solver(info.solver)
+    sim.info = info
+    sim.oper = oper
+    sim.output = _OutputStub()
+    sim.is_forcing_enabled = False
+    sim.state = mods["ns3d_state"].StateNS3D(sim)
+    sim.state.state_spect[:] = 0.0
+    sim.state.state_phys[:] = 0.0
+    sim._init_projection()
+    sim.time_stepping = mods["ns3d_ts"].TimeSteppingPseudoSpectralNS3D(sim)
+    return sim

@@ -1,0 +1,294 @@
+"""Restatement of the ns2d / ns3d pseudo-spectral time step (ORACLE).
+
+Test infrastructure only (see ``oracle/__init__.py``).  Every function cites
+the reference lines it follows; all arithmetic is float64 / complex128.
+"""
+
+import numpy as np
+
+from .spectral import OperNumpy2D, OperNumpy3D
+
+
+def max_abs(arr):
+    """``fluidsim/base/time_stepping/base.py:24-25``."""
+    return max(abs(arr.min()), abs(arr.max()))
+
+
+def compute_freq_diss(oper, nu_2=0.0, nu_4=0.0, nu_8=0.0, nu_m4=0.0):
+    """``fluidsim/base/solvers/pseudo_spect.py:134-191``."""
+    if nu_2 > 0:
+        f_d = nu_2 * oper.K2
+    else:
+        f_d = np.zeros_like(oper.K2)
+    if nu_4 > 0.0:
+        f_d = f_d + nu_4 * oper.K4
+    if nu_8 > 0.0:
+        f_d = f_d + nu_8 * oper.K8
+    if nu_m4 != 0.0:
+        f_d_hypo = nu_m4 / oper.K2_not0**2
+        if f_d_hypo.ndim == 2:
+            f_d_hypo[0, 0] = f_d_hypo[0, 1]
+        else:
+            f_d_hypo[0, 0, 0] = f_d_hypo[0, 0, 1]
+    else:
+        f_d_hypo = 0.0
+    return f_d, f_d_hypo
+
+
+class _SolverBase:
+    """IF-RK4 driver shared by ns2d/ns3d.
+
+    ``TimeSteppingPseudoSpectral`` (``fluidsim/base/time_stepping/pseudo_spect.py``):
+    ``ExactLinearCoefs`` 103-152, ``_time_step_RK4`` 798-984; CFL logic
+    ``fluidsim/base/time_stepping/base.py:248-354``; loop 182-244.
+    """
+
+    def __init__(self, oper, nu_2=0.0, nu_4=0.0, nu_8=0.0, nu_m4=0.0,
+                 deltat0=0.2, deltat_max=0.2, USE_CFL=False, cfl_coef=None):
+        self.oper = oper
+        self.nu_2, self.nu_4, self.nu_8, self.nu_m4 = nu_2, nu_4, nu_8, nu_m4
+        f_d, f_d_hypo = compute_freq_diss(oper, nu_2, nu_4, nu_8, nu_m4)
+        self.freq_lin = f_d + f_d_hypo
+        self.USE_CFL = USE_CFL
+        self.CFL = cfl_coef if cfl_coef is not None else 1.0
+        self.deltat = deltat0
+        self.deltat_max = deltat_max
+        self.dt_old = None
+        self.t = 0.0
+        self.it = 0
+        self.state_spect = np.zeros((self.nvar,) + oper.shapeK, np.complex128)
+        self.state_phys = np.zeros((len(self.keys_phys),) + oper.shapeX)
+
+    # ExactLinearCoefs.compute / get_updated_coefs_CLF (pseudo_spect.py:125-146)
+    def _coefs(self):
+        dt = self.deltat
+        if self.dt_old != dt:
+            self.exact = np.exp(-dt * self.freq_lin)
+            self.exact2 = np.exp(-dt / 2 * self.freq_lin)
+            self.dt_old = dt
+        return self.exact, self.exact2
+
+    # base.py:334-354
+    def _cfl_from_tmp(self, tmp):
+        if tmp > 0:
+            deltat_CFL = self.CFL / tmp
+        else:
+            deltat_CFL = self.deltat_max
+        maybe_new_dt = min(deltat_CFL, self.deltat_max)
+        normalize_diff = abs(self.deltat - maybe_new_dt) / maybe_new_dt
+        if normalize_diff > 0.02:
+            self.deltat = maybe_new_dt
+
+    def time_step_RK4(self):
+        """``pseudo_spect.py:798-984`` line for line."""
+        dt = self.deltat
+        diss, diss2 = self._coefs()
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        tmp = (S + dt / 6 * N0) * diss
+        tmp1 = (S + dt / 2 * N0) * diss2
+        N1 = self.tendencies_nonlin(tmp1)
+        tmp += dt / 3 * diss2 * N1
+        tmp1 = S * diss2 + dt / 2 * N1
+        N2 = self.tendencies_nonlin(tmp1)
+        tmp += dt / 3 * diss2 * N2
+        tmp1 = S * diss + dt * diss2 * N2
+        N3 = self.tendencies_nonlin(tmp1)
+        S[:] = tmp + dt / 6 * N3
+
+    def one_time_step(self):
+        """``base.py:208-244`` without outputs, forcing or signals."""
+        if self.USE_CFL:
+            self.compute_time_increment_CLF()
+        self.one_time_step_computation()
+        self.t += self.deltat
+        self.it += 1
+
+    def run(self, it_end=None, t_end=None):
+        if t_end is not None:
+            while self.t < t_end:
+                self.one_time_step()
+        else:
+            while self.it < it_end:
+                self.one_time_step()
+
+
+class NS2DOracle(_SolverBase):
+    """ns2d: ``fluidsim/solvers/ns2d/solver.py`` + ``state.py``."""
+
+    nvar = 1
+    keys_phys = ("ux", "uy", "rot")  # ns2d/state.py:31
+
+    def __init__(self, oper: OperNumpy2D, beta=0.0, **kw):
+        self.beta = beta
+        super().__init__(oper, **kw)
+
+    def statephys_from_statespect(self):
+        """``ns2d/state.py:95-106``."""
+        rot_fft = self.state_spect[0]
+        ux_fft, uy_fft = self.oper.vecfft_from_rotfft(rot_fft)
+        self.state_phys[2] = self.oper.ifft(rot_fft)
+        self.state_phys[0] = self.oper.ifft(ux_fft)
+        self.state_phys[1] = self.oper.ifft(uy_fft)
+
+    def init_from_rotfft(self, rot_fft):
+        """``ns2d/state.py:115-119``."""
+        rot_fft = np.array(rot_fft, dtype=np.complex128)
+        self.oper.dealiasing(rot_fft)
+        self.state_spect[0] = rot_fft
+        self.statephys_from_statespect()
+
+    def tendencies_nonlin(self, state_spect=None):
+        """``ns2d/solver.py:111-194`` with ``compute_Frot`` 33-39."""
+        oper = self.oper
+        if state_spect is None:
+            rot_fft = self.state_spect[0]
+            ux = self.state_phys[0]
+            uy = self.state_phys[1]
+        else:
+            rot_fft = state_spect[0]
+            ux_fft, uy_fft = oper.vecfft_from_rotfft(rot_fft)
+            ux = oper.ifft(ux_fft)
+            uy = oper.ifft(uy_fft)
+        px_rot_fft, py_rot_fft = oper.gradfft_from_fft(rot_fft)
+        px_rot = oper.ifft(px_rot_fft)
+        py_rot = oper.ifft(py_rot_fft)
+        if self.beta == 0:
+            Frot = -ux * px_rot - uy * py_rot
+        else:
+            Frot = -ux * px_rot - uy * (py_rot + self.beta)
+        F = np.empty_like(self.state_spect)
+        F[0] = oper.fft(Frot)
+        oper.dealiasing(F[0])
+        return F
+
+    def one_time_step_computation(self):
+        """``pseudo_spect.py:236-243``."""
+        self.time_step_RK4()
+        self.oper.dealiasing(self.state_spect[0])
+        self.statephys_from_statespect()
+        if np.isnan(np.sum(self.state_spect[0])):
+            raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")
+
+    def compute_time_increment_CLF(self):
+        """``base.py:356-366`` (``_compute_time_increment_CLF_uxuy``)."""
+        ux, uy = self.state_phys[0], self.state_phys[1]
+        tmp = max_abs(ux) / self.oper.deltax + max_abs(uy) / self.oper.deltay
+        self._cfl_from_tmp(tmp)
+
+    # outputs: ns2d/output/__init__.py:110-129, spatial_means.py:23-36
+    def energy_fft(self):
+        ux_fft, uy_fft = self.oper.vecfft_from_rotfft(self.state_spect[0])
+        return (np.abs(ux_fft) ** 2 + np.abs(uy_fft) ** 2) / 2.0
+
+    def enstrophy_fft(self):
+        return np.abs(self.state_spect[0]) ** 2 / 2.0
+
+    def compute_energy(self):
+        return self.oper.sum_wavenumbers(self.energy_fft())
+
+    def compute_enstrophy(self):
+        return self.oper.sum_wavenumbers(self.enstrophy_fft())
+
+    def spatial_means(self):
+        f_d, f_d_hypo = compute_freq_diss(self.oper, self.nu_2, self.nu_4,
+                                          self.nu_8, self.nu_m4)
+        e_fft, z_fft = self.energy_fft(), self.enstrophy_fft()
+        s = self.oper.sum_wavenumbers
+        return {
+            "E": s(e_fft), "Z": s(z_fft),
+            "epsK": s(f_d * 2 * e_fft), "epsK_hypo": s(f_d_hypo * 2 * e_fft),
+            "epsZ": s(f_d * 2 * z_fft), "epsZ_hypo": s(f_d_hypo * 2 * z_fft),
+        }
+
+
+class NS3DOracle(_SolverBase):
+    """ns3d: ``fluidsim/solvers/ns3d/solver.py``, ``time_stepping.py``."""
+
+    nvar = 3
+    keys_phys = ("vx", "vy", "vz")  # ns3d/state.py:20
+
+    def __init__(self, oper: OperNumpy3D, f=None, **kw):
+        self.f = f
+        super().__init__(oper, **kw)
+
+    def statephys_from_statespect(self):
+        """``fluidsim/base/state.py:326-333``."""
+        for ik in range(3):
+            self.state_phys[ik] = self.oper.ifft(self.state_spect[ik])
+
+    def statespect_from_statephys(self):
+        """``fluidsim/base/state.py:318-325``."""
+        for ik in range(3):
+            self.state_spect[ik] = self.oper.fft(self.state_phys[ik])
+
+    def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
+        """``ns3d/state.py:124-130``."""
+        self.state_spect[0] = vx_fft
+        self.state_spect[1] = vy_fft
+        self.state_spect[2] = vz_fft
+        self.statephys_from_statespect()
+        self.statespect_from_statephys()
+
+    def project_state_spect(self, S):
+        """``ns3d/solver.py:255-263`` (default projector ``project_perpk3d``)."""
+        self.oper.project_perpk3d(S[0], S[1], S[2])
+
+    def tendencies_nonlin(self, state_spect=None):
+        """``ns3d/solver.py:180-253``."""
+        oper = self.oper
+        S = self.state_spect if state_spect is None else state_spect
+        vx_fft, vy_fft, vz_fft = S[0], S[1], S[2]
+        ox_fft, oy_fft, oz_fft = oper.rotfft_from_vecfft(vx_fft, vy_fft, vz_fft)
+        if self.f is not None:
+            oz_fft = oz_fft.copy()
+            oz_fft[0, 0, 0] += self.f
+        ox, oy, oz = oper.ifft(ox_fft), oper.ifft(oy_fft), oper.ifft(oz_fft)
+        if state_spect is None:
+            vx, vy, vz = self.state_phys
+        else:
+            vx, vy, vz = oper.ifft(vx_fft), oper.ifft(vy_fft), oper.ifft(vz_fft)
+        # fluidfft vector_product(v, omega) = v x omega
+        fx = vy * oz - vz * oy
+        fy = vz * ox - vx * oz
+        fz = vx * oy - vy * ox
+        F = np.empty_like(self.state_spect)
+        F[0] = oper.fft(fx)
+        F[1] = oper.fft(fy)
+        F[2] = oper.fft(fz)
+        self.project_state_spect(F)
+        oper.dealiasing(F)
+        return F
+
+    def one_time_step_computation(self):
+        """``ns3d/time_stepping.py:8-20``."""
+        self.time_step_RK4()
+        self.project_state_spect(self.state_spect)
+        self.oper.dealiasing(self.state_spect)
+        self.statephys_from_statespect()
+        if np.isnan(np.sum(self.state_spect[0])):
+            raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")
+
+    def compute_time_increment_CLF(self):
+        """``base.py:320-339`` (``_compute_time_increment_CLF_uxuyuz``)."""
+        vx, vy, vz = self.state_phys
+        o = self.oper
+        tmp = (max_abs(vx) / o.deltax + max_abs(vy) / o.deltay
+               + max_abs(vz) / o.deltaz)
+        self._cfl_from_tmp(tmp)
+
+    # outputs: ns3d/output/__init__.py:101-117, spatial_means.py:23-40
+    def energy_fft(self):
+        S = self.state_spect
+        return 0.5 * (np.abs(S[0]) ** 2 + np.abs(S[1]) ** 2 + np.abs(S[2]) ** 2)
+
+    def compute_energy(self):
+        return self.oper.sum_wavenumbers(self.energy_fft())
+
+    def spatial_means(self):
+        f_d, f_d_hypo = compute_freq_diss(self.oper, self.nu_2, self.nu_4,
+                                          self.nu_8, self.nu_m4)
+        e_fft = self.energy_fft()
+        s = self.oper.sum_wavenumbers
+        return {"E": s(e_fft), "epsK": s(f_d * 2 * e_fft),
+                "epsK_hypo": s(f_d_hypo * 2 * e_fft)}

@@ -1,0 +1,150 @@
+"""Generate the golden fixtures from the reference's own Python code.
+
+Usage (needs the fluidsim 0.8.3 sources; writes ``tests/golden/*.npz``)::
+
+    python tests/golden/make_golden.py /root/reference
+
+Each case builds a reference ns2d / ns3d ``Simul`` with ``oracle.refshim``
+(the reference's ``TimeSteppingPseudoSpectral`` RK4, CFL logic,
+``tendencies_nonlin``, ``compute_freq_diss`` and state classes, unmodified,
+on top of the numpy fluidfft restatement), runs it from a seeded initial
+state and stores the inputs, the first tendency and the states/time steps
+after 1 and 10 steps.  The oracle restatement is run beside it and must
+agree to 1e-13 before anything is written.
+"""
+
+import sys
+from math import pi
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from oracle import refshim  # noqa: E402
+from oracle.spectral import OperNumpy2D, OperNumpy3D  # noqa: E402
+from oracle.solvers import NS2DOracle, NS3DOracle  # noqa: E402
+from fluidsim_gb300.init_fields import (  # noqa: E402
+    isotropic_3d, noise_rot_2d, taylor_green_3d)
+
+CASES_2D = [
+    dict(name="ns2d_32_cfl", nx=32, ny=32, Lx=6.0, Ly=6.0, nu_8=2e-5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         init=dict(kmin=2.0, kmax=6.0, seed=1), steps=10),
+    dict(name="ns2d_48x40_beta", nx=48, ny=40, Lx=2 * pi, Ly=2 * pi * 40 / 48,
+         nu_2=1e-3, nu_m4=1e-3, beta=1.0, USE_CFL=False, deltat0=0.01,
+         init=dict(kmin=2.0, kmax=9.0, seed=2), steps=10),
+    dict(name="ns2d_256_c1", nx=256, ny=256, Lx=2 * pi, Ly=2 * pi, nu_2=1e-4,
+         USE_CFL=False, deltat0=1e-3, init=dict(kmin=4.0, kmax=8.0, seed=2024),
+         steps=10),
+]
+
+CASES_3D = [
+    dict(name="ns3d_20x15x10", nx=20, ny=15, nz=10, Lx=6.0, Ly=4.5, Lz=3.0,
+         nu_2=1e-2, USE_CFL=True, deltat0=0.2, deltat_max=0.2,
+         cfl_coef=None, init="iso", seed=3, steps=10),
+    dict(name="ns3d_tgv_32", nx=32, ny=32, nz=32, nu_2=1 / 1600, USE_CFL=True,
+         deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, init="tgv", steps=10),
+    dict(name="ns3d_iso_24x16x32_f", nx=24, ny=16, nz=32, nu_2=5e-3, f=1.0,
+         USE_CFL=False, deltat0=5e-3, init="iso", seed=4, steps=10),
+]
+
+
+def _kw(case, keys):
+    return {k: case[k] for k in keys if k in case}
+
+
+def run_2d(mods, case):
+    oper = OperNumpy2D(case["nx"], case["ny"], case["Lx"], case["Ly"])
+    rot0 = noise_rot_2d(case["nx"], case["ny"], case["Lx"], case["Ly"],
+                        **case["init"])
+    kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
+                    "deltat_max", "cfl_coef"])
+    sim = refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0), **kw)
+    sim.state.init_from_rotfft(rot0.copy())
+    S_init = np.array(sim.state.state_spect)
+    phys_init = np.array(sim.state.state_phys)
+    tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
+    orc = NS2DOracle(oper, beta=case.get("beta", 0.0), **kw)
+    orc.init_from_rotfft(rot0.copy())
+    np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
+                               rtol=0, atol=1e-13 * np.abs(tend0).max())
+    out = dict(S_init=S_init, phys_init=phys_init, tend0=tend0, dts=[], E=[])
+    for it in range(case["steps"]):
+        sim.time_stepping.one_time_step()
+        orc.one_time_step()
+        out["dts"].append(sim.time_stepping.deltat)
+        S = np.array(sim.state.state_spect)
+        err = np.abs(orc.state_spect - S).max() / np.abs(S).max()
+        assert err < 1e-13, (case["name"], it, err)
+        assert orc.deltat == sim.time_stepping.deltat
+        out["E"].append(orc.compute_energy())
+        if it == 0:
+            out["S_1"] = S
+    out["S_end"] = np.array(sim.state.state_spect)
+    out["phys_end"] = np.array(sim.state.state_phys)
+    return out
+
+
+def run_3d(mods, case):
+    nx, ny, nz = case["nx"], case["ny"], case["nz"]
+    L = (case.get("Lx", 2 * pi), case.get("Ly", 2 * pi), case.get("Lz", 2 * pi))
+    oper = OperNumpy3D(nx, ny, nz, *L)
+    if case["init"] == "tgv":
+        v0 = taylor_green_3d(nx, ny, nz, *L)
+    else:
+        v0 = isotropic_3d(nx, ny, nz, *L, seed=case["seed"])
+    kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
+                    "deltat_max", "cfl_coef"])
+    sim = refshim.make_ns3d(mods, oper, f=case.get("f"), **kw)
+    sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
+    S_init = np.array(sim.state.state_spect)
+    phys_init = np.array(sim.state.state_phys)
+    tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
+    orc = NS3DOracle(oper, f=case.get("f"), **kw)
+    orc.init_from_vxvyvzfft(*[c.copy() for c in v0])
+    assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
+    np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
+                               rtol=0, atol=1e-13 * np.abs(tend0).max())
+    out = dict(S_init=S_init, phys_init=phys_init, tend0=tend0, dts=[], E=[])
+    for it in range(case["steps"]):
+        sim.time_stepping.one_time_step()
+        orc.one_time_step()
+        out["dts"].append(sim.time_stepping.deltat)
+        S = np.array(sim.state.state_spect)
+        err = np.abs(orc.state_spect - S).max() / np.abs(S).max()
+        assert err < 1e-13, (case["name"], it, err)
+        assert orc.deltat == sim.time_stepping.deltat
+        out["E"].append(orc.compute_energy())
+        if it == 0:
+            out["S_1"] = S
+    out["S_end"] = np.array(sim.state.state_spect)
+    out["phys_end"] = np.array(sim.state.state_phys)
+    return out
+
+
+def _params_array(case):
+    keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
+            "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps"]
+    return {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
+                                   dtype=np.float64)
+            for k in keys if k in case}
+
+
+def main(ref_root):
+    mods = refshim.load_reference(ref_root)
+    for case in CASES_2D:
+        out = run_2d(mods, case)
+        np.savez_compressed(HERE / f"{case['name']}.npz", **_params_array(case),
+                            **{k: np.asarray(v) for k, v in out.items()})
+        print(case["name"], "ok", out["dts"][-1], out["E"][-1])
+    for case in CASES_3D:
+        out = run_3d(mods, case)
+        np.savez_compressed(HERE / f"{case['name']}.npz", **_params_array(case),
+                            **{k: np.asarray(v) for k, v in out.items()})
+        print(case["name"], "ok", out["dts"][-1], out["E"][-1])
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
