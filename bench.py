@@ -1,0 +1,340 @@
+"""Benchmark: ns3d 512^3 IF-RK4 steps/s on GB300 (FP32, with FP64 beside it).
+
+Workload (decaying isotropic turbulence): 512^3 periodic box L = 2 pi,
+seeded solenoidal random-phase velocity with E(k) ~ k^4 exp(-2 (k/4)^2),
+total energy 0.5, nu_2 = 5e-4, RK4 with exact integrating factor, 2/3
+dealiasing, dt fixed once from the CFL rule with coefficient 0.5.  A step is
+one full RK4 step (4 tendency evaluations + projection + dealiasing + NaN
+check).  The working set (~10 GB in FP32) is far larger than the 129 MB L2,
+so no explicit L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU
+(the spec path has no data-path exchange); value = steps of all ranks
+divided by the slowest rank's time.  The reference arm times the CPU
+restatement of the reference algorithm (float64, scipy.fft on all host
+cores) on a bounded sample of the same workload.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from math import pi
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ns3d 512^3 RK4 steps/s"
+KINDS = ("inv_z_curl", "inv_y", "x_product", "fwd_y", "fwd_z_rk")
+# algorithmic HBM traffic per launch, in units of one spectral field
+# (nz*ny*(nx/2+1) complex): reads + writes of the fused passes
+FIELDS_PER_LAUNCH = {"inv_z_curl": 9, "inv_y": 12, "x_product": 9, "fwd_y": 6,
+                     "fwd_z_rk": (12 + 15 + 15 + 9) / 4}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def initial_state(n):
+    from fluidsim_gb300.init_fields import isotropic_3d
+    return isotropic_3d(n, n, n, k0=4.0, energy=0.5, seed=0)
+
+
+def cfl_dt(vmax, n, cfl=0.5, dtmax=0.2):
+    """dt from the CFL rule of fluidsim/base/time_stepping/base.py:320-354."""
+    dx = 2 * pi / n
+    tmp = sum(v / dx for v in vmax)
+    return min(cfl / tmp, dtmax) if tmp > 0 else dtmax
+
+
+def make_sim(n, precision, v0):
+    import torch
+    from fluidsim_gb300.solvers import SimulNS3D
+    p = SimulNS3D.create_default_params()
+    p.precision = precision
+    p.oper.nx = p.oper.ny = p.oper.nz = n
+    p.nu_2 = 5e-4
+    p.time_stepping.USE_CFL = False
+    p.time_stepping.USE_T_END = False
+    sim = SimulNS3D(p)
+    sim.state.init_statespect_from(**{k: torch.from_numpy(v0[i]) for i, k in
+                                      enumerate(sim.state.keys_state_spect)})
+    return sim
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kind, n):
+    """dram read+write bytes per launch from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == kind and parts[1] == f"{n}^3":
+            return float(parts[2])
+    return None
+
+
+def cpu_sample(n, v0, reps=1):
+    """Oracle (float64, scipy.fft on all cores): one tendency evaluation."""
+    from oracle.solvers import NS3DOracle
+    from oracle.spectral import WORKERS, OperNumpy3D
+    orc = NS3DOracle(OperNumpy3D(n, n, n), nu_2=5e-4)
+    orc.state_spect[:] = v0
+    S = orc.state_spect.copy()
+    small = NS3DOracle(OperNumpy3D(32, 32, 32))
+    small.tendencies_nonlin(small.state_spect.copy())  # warm the code paths
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.tendencies_nonlin(S)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": 1.0 / (4 * dt), "unit": "steps/s", "cores": WORKERS, "kind": "port",
+            "sample": (f"{reps} tendencies_nonlin evaluation(s) of the float64 oracle at "
+                       f"{n}^3 (9 FFTs + curl, v x omega, projection, dealiasing), "
+                       f"{dt:.2f} s each, x4 for one RK4 step (elementwise RK updates "
+                       "not counted)")}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    n = args.n
+    v0 = initial_state(n)
+    reps = max(1, min(args.steps, 3))
+    base = cpu_sample(n, v0, reps=reps)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "steps/s",
+            "n_gpus": args.gpus, "steps": reps, "warmup": 1,
+            "ms_per_step": 1000.0 / base["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"ns3d decaying isotropic turbulence {n}^3", "nx": n,
+                       "nu_2": 5e-4, "scheme": "RK4 exact integrating factor",
+                       "dealiasing": "2/3 cubic"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def rel_l2(a, b):
+    return max(float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(len(b)))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    from fluidsim_gb300 import _lib
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    n = args.n
+    v0 = initial_state(n)
+    sim = make_sim(n, "float32", v0)
+    dt = cfl_dt(sim.max_velocity(), n)
+    sim.time_stepping.deltat = dt
+    lib = sim._lib
+    ts = sim.time_stepping
+    for _ in range(args.warmup):
+        ts.one_time_step()
+    torch.cuda.synchronize()
+
+    launches0 = ctypes.c_int64()
+    _lib.check(lib.gbs_ns_timing_report(sim._solver, None, None, 0, ctypes.byref(launches0)))
+    _lib.check(lib.gbs_ns_timing(sim._solver, 1))
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        start.record()
+        for _ in range(args.steps):
+            ts.one_time_step()
+        stop.record()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    elapsed_ms = start.elapsed_time(stop)
+    ms = (ctypes.c_double * 5)()
+    cnt = (ctypes.c_int64 * 5)()
+    launches = ctypes.c_int64()
+    _lib.check(lib.gbs_ns_timing_report(sim._solver, ms, cnt, 5, ctypes.byref(launches)))
+    _lib.check(lib.gbs_ns_timing(sim._solver, 0))
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    steps_per_s = world * args.steps / (elapsed_ms / 1000.0)
+
+    # roofline of the dominant kernel (largest share of the timed region)
+    field_bytes = n * n * (n // 2 + 1) * 8  # complex64
+    kinds = {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(KINDS)}
+    dom = max(kinds, key=lambda k: kinds[k]["ms"])
+    avg_s = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1) / 1000.0
+    alg_bytes = FIELDS_PER_LAUNCH[dom] * field_bytes
+    peak, peak_src = measured_peak()
+    achieved = alg_bytes / avg_s / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": ncu_traffic(dom, n), "alg_bytes_per_launch": alg_bytes,
+                "kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in kinds.items()},
+                "kernel_share": {k: v["ms"] / sum(x["ms"] for x in kinds.values())
+                                 for k, v in kinds.items()}}
+
+    # end to end: host state in pinned memory, copied in and out every step
+    S = sim.state.state_spect
+    host_in = torch.empty(S.shape, dtype=S.dtype, pin_memory=True)
+    host_in.copy_(S)
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    e_steps = max(3, args.steps // 4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(e_steps):
+        S.copy_(host_in, non_blocking=True)
+        ts.one_time_step()
+        host_out.copy_(S, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_rate = world * e_steps / (e0.elapsed_time(e1) / 1000.0)
+    state_bytes = S.numel() * S.element_size()
+
+    line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"ns3d decaying isotropic turbulence {n}^3", "nx": n,
+                       "ny": n, "nz": n, "L": "2pi", "nu_2": 5e-4, "dt": dt,
+                       "scheme": "RK4 exact integrating factor", "dealiasing": "2/3 cubic",
+                       "precision": "fp32 FFT/products, fp64 twiddles and reductions",
+                       "l2_flush": "none needed: working set ~10 GB >> 129 MB L2",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": int(launches.value - launches0.value),
+            "roofline": roofline,
+            "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes,
+                    "note": "state copied host->device and back around every step"},
+            "clocks": clocks.summary()}
+
+    if not args.no_fp64:
+        sim32 = make_sim(n, "float32", v0)
+        sim32.time_stepping.deltat = dt
+        for _ in range(10):
+            sim32.time_stepping.one_time_step()
+        s32 = sim32.state.state_spect.cpu().numpy()
+        del sim32, sim
+        torch.cuda.empty_cache()
+        sim64 = make_sim(n, "float64", v0)
+        sim64.time_stepping.deltat = dt
+        sim64.time_stepping.one_time_step()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for _ in range(9):
+            sim64.time_stepping.one_time_step()
+        f1.record()
+        torch.cuda.synchronize()
+        fp64_rate = 9 / (f0.elapsed_time(f1) / 1000.0)
+        s64 = sim64.state.state_spect.cpu().numpy()
+        line["fp64"] = {"steps_per_s": fp64_rate, "ms_per_step": 1000.0 / fp64_rate}
+        line["fp32_over_fp64_speedup"] = steps_per_s / world / fp64_rate
+        line["fp32_vs_fp64_rel_l2_10_steps"] = rel_l2(s32.astype(np.complex128), s64)
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(n, v0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -24,7 +24,8 @@ EXPORTED = (
     "gbs_fft_plan_destroy", "gbs_fft_r2c", "gbs_fft_c2r", "gbs_ns_create",
     "gbs_ns_destroy", "gbs_ns_tendencies", "gbs_ns_step_rk4",
     "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
-    "gbs_ns_spectrum_size", "gbs_ns_spectrum",
+    "gbs_ns_spectrum_size", "gbs_ns_spectrum", "gbs_ns_timing",
+    "gbs_ns_timing_report",
 )
 
 
@@ -69,7 +70,9 @@ def _declare(lib):
         "gbs_cfl_update": (ctypes.c_double, [ctypes.c_double] * 4),
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),
         "gbs_ns_spectrum_size": (ctypes.c_int, [P, I64P]),
-        "gbs_ns_spectrum": (ctypes.c_int, [P, P, DP, P]),
+        "gbs_ns_spectrum": (ctypes.c_int, [P, P, P, P]),
+        "gbs_ns_timing": (ctypes.c_int, [P, ctypes.c_int]),
+        "gbs_ns_timing_report": (ctypes.c_int, [P, DP, I64P, ctypes.c_int, I64P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

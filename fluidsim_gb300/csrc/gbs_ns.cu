@@ -474,6 +474,9 @@ k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
 }
 
 // ================================================================ solver
+constexpr int kKinds = 5;     // A, inverse y, B, forward y, C
+constexpr int kMaxEv = 2048;  // event pairs recorded before a harvest
+
 struct Solver {
   gbs_ns_params p;
   NSK q;
@@ -489,10 +492,50 @@ struct Solver {
   int* dflag;
   double* dred;              // reduction partials
   double* hbuf;              // pinned host mirror (8 doubles)
+  // per-kernel timing (CUDA events on the launching stream) + launch count
+  int timing;
+  int nev;                  // event pairs in use
+  cudaEvent_t ev[kMaxEv][2];
+  int ev_kind[kMaxEv];
+  double t_ms[kKinds];
+  long long t_count[kKinds];
+  long long launches;
   // launch shapes
   int txA, txC, Lb;
   int thA, thB, thC;
   size_t smA, smB, smC;
+};
+
+// Harvest recorded event pairs into the per-kind totals (synchronises on
+// the last recorded event).
+static int harvest(Solver* s) {
+  if (s->nev == 0) return GBS_OK;
+  GBS_CUDA_TRY(cudaEventSynchronize(s->ev[s->nev - 1][1]));
+  for (int i = 0; i < s->nev; ++i) {
+    float ms = 0.f;
+    GBS_CUDA_TRY(cudaEventElapsedTime(&ms, s->ev[i][0], s->ev[i][1]));
+    s->t_ms[s->ev_kind[i]] += ms;
+    s->t_count[s->ev_kind[i]] += 1;
+  }
+  s->nev = 0;
+  return GBS_OK;
+}
+
+struct LaunchScope {
+  Solver* s;
+  int slot;
+  cudaStream_t st;
+  LaunchScope(Solver* s_, int kind, cudaStream_t st_) : s(s_), slot(-1), st(st_) {
+    s->launches += 1;
+    if (!s->timing) return;
+    if (s->nev == kMaxEv) harvest(s);
+    slot = s->nev++;
+    s->ev_kind[slot] = kind;
+    cudaEventRecord(s->ev[slot][0], st);
+  }
+  ~LaunchScope() {
+    if (slot >= 0) cudaEventRecord(s->ev[slot][1], st);
+  }
 };
 
 template <typename T>
@@ -569,30 +612,48 @@ static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
   if (s->p.ndim == 3) {
     q.TX = s->txA;
     q.LP = 6 * q.TX;
-    k3_inv_z_curl<T><<<dim3(ceil_div(q.nkx, q.TX), q.ny), s->thA, s->smA, st>>>(
-        static_cast<const C*>(in), W, q, twz);
+    {
+      LaunchScope ls(s, 0, st);
+      k3_inv_z_curl<T><<<dim3(ceil_div(q.nkx, q.TX), q.ny), s->thA, s->smA, st>>>(
+          static_cast<const C*>(in), W, q, twz);
+    }
     GBS_CHECK_LAUNCH();
-    rc = launch_col<T, 1>(W, W, q.ny, q.nkx, q.nz, 6, q.nkx,
-                          (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    {
+      LaunchScope ls(s, 1, st);
+      rc = launch_col<T, 1>(W, W, q.ny, q.nkx, q.nz, 6, q.nkx,
+                            (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    }
     if (rc) return rc;
     q.L = s->Lb;
     q.LP = 6 * q.L + 1;
-    k3_x_product<T><<<ceil_div((int64_t)q.nz * q.ny, q.L), s->thB, s->smB, st>>>(
-        W, F, q, twx, vmax);
+    {
+      LaunchScope ls(s, 2, st);
+      k3_x_product<T><<<ceil_div((int64_t)q.nz * q.ny, q.L), s->thB, s->smB, st>>>(
+          W, F, q, twx, vmax);
+    }
     GBS_CHECK_LAUNCH();
-    rc = launch_col<T, -1>(F, F, q.ny, q.nkx, q.nz, 3, q.nkx,
-                           (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    {
+      LaunchScope ls(s, 3, st);
+      rc = launch_col<T, -1>(F, F, q.ny, q.nkx, q.nz, 3, q.nkx,
+                             (int64_t)q.ny * q.nkx, s->nK, twy, T(1), st);
+    }
     if (rc) return rc;
     return GBS_OK;
   }
   q.TX = s->txA;
   q.LP = 4 * q.TX;
-  k2_inv_y<T><<<ceil_div(q.nkx, q.TX), s->thA, s->smA, st>>>(
-      static_cast<const C*>(in), W, q, twy);
+  {
+    LaunchScope ls(s, 0, st);
+    k2_inv_y<T><<<ceil_div(q.nkx, q.TX), s->thA, s->smA, st>>>(
+        static_cast<const C*>(in), W, q, twy);
+  }
   GBS_CHECK_LAUNCH();
   q.L = s->Lb;
   q.LP = 4 * q.L + 1;
-  k2_x_product<T><<<ceil_div(q.ny, q.L), s->thB, s->smB, st>>>(W, F, q, twx, vmax);
+  {
+    LaunchScope ls(s, 2, st);
+    k2_x_product<T><<<ceil_div(q.ny, q.L), s->thB, s->smB, st>>>(W, F, q, twx, vmax);
+  }
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
@@ -602,6 +663,7 @@ static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st) {
   using C = cplx<T>;
   NSK q = s->q;
   const C* F = static_cast<const C*>(s->F);
+  LaunchScope ls(s, 4, st);
   if (s->p.ndim == 3) {
     q.TX = s->txC;
     q.LP = 3 * q.TX;
@@ -835,6 +897,12 @@ struct gbs_ns {
 };
 
 static void free_solver(Solver* s) {
+  if (s->timing >= 0 && s->ev[0][0]) {
+    for (int i = 0; i < gbs::kMaxEv; ++i) {
+      cudaEventDestroy(s->ev[i][0]);
+      cudaEventDestroy(s->ev[i][1]);
+    }
+  }
   for (void* t : s->tw)
     if (t) cudaFree(t);
   void* ptrs[] = {s->W, s->F, s->tmp, s->tmp1, s->dmax, s->dflag, s->dred};
@@ -991,6 +1059,48 @@ int gbs_ns_spatial_means(gbs_ns* h, const void* S, double* out, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (h->s.p.dtype == GBS_F64) return gbs::spatial_means<double>(&h->s, S, out, st);
   return gbs::spatial_means<float>(&h->s, S, out, st);
+}
+
+int gbs_ns_timing(gbs_ns* h, int enable) {
+  gbs::clear_error();
+  if (!h) {
+    gbs::set_error("gbs_ns_timing: null solver");
+    return GBS_EINVAL;
+  }
+  Solver* s = &h->s;
+  if (enable && !s->ev[0][0]) {
+    for (int i = 0; i < gbs::kMaxEv; ++i) {
+      GBS_CUDA_TRY(cudaEventCreate(&s->ev[i][0]));
+      GBS_CUDA_TRY(cudaEventCreate(&s->ev[i][1]));
+    }
+  }
+  if (enable) {
+    s->nev = 0;
+    for (int k = 0; k < gbs::kKinds; ++k) {
+      s->t_ms[k] = 0;
+      s->t_count[k] = 0;
+    }
+  }
+  s->timing = enable ? 1 : 0;
+  return GBS_OK;
+}
+
+int gbs_ns_timing_report(gbs_ns* h, double* ms, int64_t* count, int nkinds,
+                         int64_t* launches) {
+  gbs::clear_error();
+  if (!h || nkinds < 0) {
+    gbs::set_error("gbs_ns_timing_report: invalid argument");
+    return GBS_EINVAL;
+  }
+  Solver* s = &h->s;
+  int rc = gbs::harvest(s);
+  if (rc) return rc;
+  for (int k = 0; k < nkinds && k < gbs::kKinds; ++k) {
+    if (ms) ms[k] = s->t_ms[k];
+    if (count) count[k] = s->t_count[k];
+  }
+  if (launches) *launches = s->launches;
+  return GBS_OK;
 }
 
 int gbs_ns_spectrum_size(gbs_ns* h, int64_t* nk) {

@@ -127,6 +127,18 @@ double gbs_cfl_update(double dt, double tmp, double cfl_coef,
 int gbs_ns_spatial_means(gbs_ns* solver, const void* state_spect, double* out,
                          void* stream);
 
+/* Per-kernel timing of a solver's launches with CUDA events recorded on the
+ * launching stream (no counterpart in the reference, which times whole runs
+ * with time(): fluidsim/util/console/util.py:329-390).  enable = 1 clears
+ * the totals and starts recording, 0 stops.  Kinds: 0 = inverse z pass with
+ * the curl (ns2d: inverse y), 1 = inverse y pass (ns3d), 2 = x pass with the
+ * products, 3 = forward y pass (ns3d), 4 = last forward pass with the RK4
+ * stage.  The report synchronises on the recorded events; *launches counts
+ * every kernel the solver launched since creation. */
+int gbs_ns_timing(gbs_ns* solver, int enable);
+int gbs_ns_timing_report(gbs_ns* solver, double* ms, int64_t* count,
+                         int nkinds, int64_t* launches);
+
 /* Shell energy spectrum in FP64 (device output spectrum[nk], nk from
  * gbs_ns_spectrum_size): bins round(|k| / dk_min), E summed with Hermitian
  * weights, divided by dk_min. */
