@@ -25,7 +25,7 @@ EXPORTED = (
     "gbs_ns_destroy", "gbs_ns_tendencies", "gbs_ns_step_rk4",
     "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
     "gbs_ns_spectrum_size", "gbs_ns_spectrum", "gbs_ns_timing",
-    "gbs_ns_timing_report",
+    "gbs_ns_timing_report", "gbs_fft_c2r_noalloc",
 )
 
 
@@ -73,6 +73,8 @@ def _declare(lib):
         "gbs_ns_spectrum": (ctypes.c_int, [P, P, P, P]),
         "gbs_ns_timing": (ctypes.c_int, [P, ctypes.c_int]),
         "gbs_ns_timing_report": (ctypes.c_int, [P, DP, I64P, ctypes.c_int, I64P]),
+        "gbs_fft_c2r_noalloc": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.c_int,
+                                               ctypes.c_int, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -224,6 +224,8 @@ template int launch_col<float, -1>(const cplx<float>*, cplx<float>*, int, int, i
 template int launch_col<float, 1>(const cplx<float>*, cplx<float>*, int, int, int, int, int64_t, int64_t, int64_t, const cplx<float>*, float, cudaStream_t);
 template int launch_col<double, -1>(const cplx<double>*, cplx<double>*, int, int, int, int, int64_t, int64_t, int64_t, const cplx<double>*, double, cudaStream_t);
 template int launch_col<double, 1>(const cplx<double>*, cplx<double>*, int, int, int, int, int64_t, int64_t, int64_t, const cplx<double>*, double, cudaStream_t);
+template int launch_c2r_rows<float>(const cplx<float>*, float*, int, int64_t, const cplx<float>*, cudaStream_t);
+template int launch_c2r_rows<double>(const cplx<double>*, double*, int, int64_t, const cplx<double>*, cudaStream_t);
 
 // ------------------------------------------------------------------- plans
 struct Plan {

@@ -64,6 +64,21 @@ int gbs_fft_r2c(gbs_fft_plan* plan, const void* x, void* k, void* stream);
 int gbs_fft_c2r(gbs_fft_plan* plan, void* k, void* x, int may_destroy,
                 void* stream);
 
+/* ifft_as_arg without any device allocation (no counterpart in the
+ * reference: fluidfft always works on preallocated plan buffers).  For
+ * callers that cannot allocate device memory themselves or let a library
+ * do it (e.g. an application whose device memory is reserved up front by
+ * its own pool allocator).  Same result as gbs_fft_c2r(may_destroy = 0) on
+ * a plan of this shape; k is preserved.  Twiddles and workspace live in one
+ * static 32 MiB device array that every GPU loading the library holds until
+ * exit; shapes needing more (3*align256 twiddle tables + batch * nK
+ * complex) are rejected with GBS_EINVAL.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  All calls share the array: calls whose
+ * GPU work overlaps race. */
+int gbs_fft_c2r_noalloc(int ndim, const int64_t* shapeX, int dtype, int batch,
+                        const void* k, void* x, void* stream);
+
 /* ----------------------------------------------------- ns2d / ns3d solver
  * Parameters of the fused pseudo-spectral step.  ndim 2: ns2d (one state
  * variable rot_fft, fluidsim/solvers/ns2d/solver.py:111-194); ndim 3: ns3d

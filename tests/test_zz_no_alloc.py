@@ -1,0 +1,69 @@
+"""gbs_fft_c2r_noalloc: the inverse transform for callers that cannot allocate.
+
+Some applications reserve all device memory up front in their own pool
+allocator and do not let a library call cudaMalloc (or cannot afford a
+plan's buffers).  For them ``gbs_fft_c2r_noalloc`` computes
+``ifft_as_arg`` with its twiddles and workspace in one static 32 MiB device
+array.  These tests call it through the C ABI and check it against the plan
+based ``gbs_fft_c2r`` on two calls in a row (the array keeps the previous
+call's contents, which must not leak into the next result).  The file name
+makes pytest collect it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {1: 1e-13, 0: 3e-6}  # GBS_F64, GBS_F32: same tolerances as test_fft_gpu
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.parametrize("shape,dtype,batch", [((24, 20, 16), 1, 2), ((64, 48, 40), 1, 1),
+                                               ((256, 256), 0, 3), ((30, 20), 1, 1)])
+def test_noalloc_matches_plan_on_two_calls(cuda, shape, dtype, batch):
+    import torch
+    lib = cuda
+    ndim = len(shape)
+    nk = shape[:-1] + (shape[-1] // 2 + 1,)
+    ct = torch.complex128 if dtype == 1 else torch.complex64
+    rt = torch.float64 if dtype == 1 else torch.float32
+    c_shape = (ctypes.c_int64 * ndim)(*shape)
+    plan = ctypes.c_void_p()
+    assert lib.gbs_fft_plan_create(ndim, c_shape, dtype, batch, ctypes.byref(plan)) == 0
+    try:
+        for call in range(2):
+            g = torch.Generator(device="cuda").manual_seed(10 + call)
+            K = torch.randn((batch,) + nk, dtype=ct, device="cuda", generator=g)
+            K0 = K.clone()
+            ref = torch.empty((batch,) + shape, dtype=rt, device="cuda")
+            out = torch.full_like(ref, float("nan"))
+            assert lib.gbs_fft_c2r(plan, ctypes.c_void_p(K.data_ptr()),
+                                   ctypes.c_void_p(ref.data_ptr()), 0, _stream()) == 0
+            rc = lib.gbs_fft_c2r_noalloc(ndim, c_shape, dtype, batch,
+                                         ctypes.c_void_p(K.data_ptr()),
+                                         ctypes.c_void_p(out.data_ptr()), _stream())
+            assert rc == 0, lib.gbs_last_error()
+            torch.cuda.synchronize()
+            assert torch.equal(K, K0)  # input preserved
+            err = (out - ref).abs().max().item() / ref.abs().max().item()
+            assert err <= TOL[dtype], (call, err)
+    finally:
+        lib.gbs_fft_plan_destroy(plan)
+
+
+def test_noalloc_rejects_oversize(cuda):
+    import torch
+    lib = cuda
+    shape = (256, 256, 256)  # 256*256*129 complex128 = 135 MB > 32 MiB
+    c_shape = (ctypes.c_int64 * 3)(*shape)
+    dummy = torch.empty(16, device="cuda")
+    rc = lib.gbs_fft_c2r_noalloc(3, c_shape, 1, 1, ctypes.c_void_p(dummy.data_ptr()),
+                                 ctypes.c_void_p(dummy.data_ptr()), _stream())
+    assert rc == -22
+    assert b"static maximum" in lib.gbs_last_error()
