@@ -18,6 +18,8 @@ GBS_ECUDA = -5
 GBS_ENAN = -33
 GBS_F32 = 0
 GBS_F64 = 1
+GBS_STEP_CHECK_NAN = 1
+GBS_STEP_DEALIASED = 2
 
 EXPORTED = (
     "gbs_last_error", "gbs_version", "gbs_fft_plan_create",

@@ -1,0 +1,596 @@
+// Compile-time-size kernels for power-of-two grids (the production path).
+//
+// Every line of length N = 2^LOGN is transformed by N/8 threads holding 8
+// complex values each: the first Stockham stage runs on values loaded
+// straight from global memory, the last one leaves its outputs in registers
+// at the positions that were loaded, and the stages in between exchange
+// through shared memory (two exchanges for N = 256 or 512).  All index
+// arithmetic is shifts and masks.
+//
+// Pruning (`pr`): when the input state is known to be dealiased (true after
+// every completed step), the passes skip what the 2/3 rule makes zero:
+// columns with kx >= kcut_x, inverse-transform inputs with |k| >= kcut,
+// forward-transform outputs that the dealiasing would zero.  Kept modes get
+// exactly the same arithmetic as without pruning.
+#pragma once
+
+#include "gbs_internal.cuh"
+#include "gbs_ns.cuh"
+
+namespace gbs {
+namespace fast {
+
+extern __shared__ __align__(16) unsigned char g_smem_fast[];
+
+// min blocks per SM so that a CTA of `th` threads keeps <= 64 registers
+constexpr int min_blocks(int th) { return th >= 1024 ? 1 : 1024 / th; }
+
+template <int LOGN>
+struct Line {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int N8 = N >> 3;
+  static constexpr int S8 = LOGN / 3;
+  static constexpr int REM = LOGN % 3;
+  static constexpr int NST = S8 + (REM ? 1 : 0);
+  static constexpr int RL = REM == 0 ? 8 : (1 << REM);
+  // register idx -> output position jt + outm(idx) * N8 after the last stage
+  static __device__ __forceinline__ constexpr int outm(int idx) {
+    return REM == 0 ? idx : (idx / RL) + (idx % RL) * (8 / RL);
+  }
+};
+
+__device__ __forceinline__ bool kept(int p, int n, int kc) {
+  return p < kc || p > n - kc;
+}
+
+// Stockham FFT of one line whose stage-0 inputs v[r] = x[jt + r N/8] are in
+// registers; `acc(p)` addresses position p of this line in shared memory.
+// Every thread of the CTA must call it (it contains barriers); `active`
+// threads compute, the others only take part in the barriers.
+template <int DIR, int LOGN, typename C, typename Acc>
+__device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
+                                    const C* __restrict__ tw, int tws) {
+  using P = Line<LOGN>;
+  constexpr int N = P::N, N8 = P::N8;
+  if (active) dft8<DIR>(v);
+#pragma unroll
+  for (int s = 1; s < P::NST; ++s) {
+    const int Ns = 1 << (3 * (s - 1));  // radix-8 stage s-1 wrote with this Ns
+    if (active) {
+      const int d = ((jt / Ns) * Ns << 3) + (jt % Ns);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) acc(d + r * Ns) = v[r];
+    }
+    __syncthreads();
+    const int Nsn = Ns << 3;
+    if (active) {
+      if (s < P::S8) {
+        const int bm = jt & (Nsn - 1);
+        const int tm = (N / (Nsn * 8)) * tws;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          C x = acc(jt + r * N8);
+          if (r) x = cmul(x, twid<DIR>(tw, r * bm * tm));
+          v[r] = x;
+        }
+        dft8<DIR>(v);
+      } else {
+        constexpr int RL = P::RL;
+        const int tm = (N / (Nsn * RL)) * tws;
+#pragma unroll
+        for (int g = 0; g < 8 / RL; ++g) {
+          const int b = jt + g * N8;
+          const int bm = b & (Nsn - 1);
+#pragma unroll
+          for (int r = 0; r < RL; ++r) {
+            C x = acc(b + r * (N / RL));
+            if (r) x = cmul(x, twid<DIR>(tw, r * bm * tm));
+            v[g * RL + r] = x;
+          }
+          dftR<RL, DIR>(&v[g * RL]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------- plain column pass
+// Lines along a strided axis (element p of column col of outer block o of
+// field z at z*fs + o*os + p*es + col).  Rows with |k| >= kc_in are read as
+// zero; rows with |k| >= kc_out are not stored.
+struct ColArgs {
+  int ncols;
+  int kc_in, kc_out;
+  int64_t es, os, fs;
+};
+
+template <typename T, int LOGN, int TX, int DIR>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ tw,
+       T scale) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  const int col = blockIdx.x * TX + c;
+  const bool valid = col < a.ncols;
+  const int64_t base = blockIdx.z * a.fs + blockIdx.y * a.os + col;
+  C v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int p = jt + r * P::N8;
+    v[r] = (valid && kept(p, P::N, a.kc_in)) ? in[base + p * a.es] : mk<C>(0, 0);
+  }
+  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  run<DIR, LOGN>(v, jt, true, acc, tw, 1);
+  if (!valid) return;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int p = jt + P::outm(i) * P::N8;
+    if (kept(p, P::N, a.kc_out)) out[base + p * a.es] = cscale(v[i], scale);
+  }
+}
+
+// Row slots in shared memory hold M + M/8 complex: one pad element every 8
+// spreads the radix-8 stage writes (stride 8) over the banks.
+template <int LOGM>
+__device__ __forceinline__ int padp(int p) { return p + (p >> 3); }
+
+// ------------------------------------------------------- plain row passes
+// nrows rows of nx = 2M reals <-> nx/2+1 complex.  L rows per CTA, M/8
+// threads per row (consecutive threads on consecutive elements of a row).
+template <typename T, int LOGM, int L>
+__global__ void __launch_bounds__(L * (1 << LOGM) / 8, 2)
+kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
+           const cplx<T>* __restrict__ twx, T scale) {
+  using C = cplx<T>;
+  using P = Line<LOGM>;
+  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8, NKX = M + 1;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % M8, l = threadIdx.x / M8;
+  const int64_t row = (int64_t)blockIdx.x * L + l;
+  const bool valid = row < nrows;
+  const C* xc = reinterpret_cast<const C*>(x) + row * M;
+  C v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = valid ? xc[jt + r * M8] : mk<C>(0, 0);
+  C* slot = buf + l * LS;
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  run<-1, LOGM>(v, jt, true, acc, twx, 2);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  __syncthreads();
+  const T h = T(0.5);
+  for (int idx = threadIdx.x; idx < L * NKX; idx += blockDim.x) {
+    const int k = idx % NKX, ll = idx / NKX;
+    const int64_t rr = (int64_t)blockIdx.x * L + ll;
+    if (rr >= nrows) continue;
+    const C* sl = buf + ll * LS;
+    C a = sl[padp<LOGM>(k == M ? 0 : k)];
+    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
+    const C s = cadd(a, b), d = csub(a, b);
+    const C wd = cmul(twx[k], d);
+    out[rr * NKX + k] = cscale(mk<C>(h * (s.x + wd.y), h * (s.y - wd.x)), scale);
+  }
+}
+
+template <typename T, int LOGM, int L>
+__global__ void __launch_bounds__(L * (1 << LOGM) / 8, 2)
+kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
+           const cplx<T>* __restrict__ twx) {
+  using C = cplx<T>;
+  using P = Line<LOGM>;
+  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8, NKX = M + 1;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % M8, l = threadIdx.x / M8;
+  const int64_t row = (int64_t)blockIdx.x * L + l;
+  const bool valid = row < nrows;
+  const C* rowp = in + row * NKX;
+  C v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int j = jt + r * M8;
+    C Z = mk<C>(0, 0);
+    if (valid) {
+      C a = rowp[j];
+      C b = cconj(rowp[M - j]);
+      if (j == 0) { a.y = 0; b.y = 0; }
+      const C s = cadd(a, b), d = csub(a, b);
+      const C wd = cmulc(d, twx[j]);
+      Z = mk<C>(s.x - wd.y, s.y + wd.x);
+    }
+    v[r] = Z;
+  }
+  C* slot = buf + l * LS;
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+  if (!valid) return;
+  C* xc = reinterpret_cast<C*>(x) + row * M;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) xc[jt + P::outm(i) * M8] = v[i];
+}
+
+// ----------------------------------------------------- ns3d geometry
+struct Geo {
+  int nx, ny, nz, nkx, M;
+  int kcx, kcy, kcz;
+  int ncx;        // columns along x that are processed
+  int nky_keep;   // rows along y that are processed (A, C)
+  int pr;         // input dealiased: prune
+  double dkx, dky, dkz;
+  double nu2, nu4, nu8, num4, beta, f, inv_n, k2_hypo0;
+  int has_f;
+};
+
+__device__ __forceinline__ Phys phys_of(const Geo& g) {
+  Phys q;
+  q.nu2 = g.nu2;
+  q.nu4 = g.nu4;
+  q.nu8 = g.nu8;
+  q.num4 = g.num4;
+  q.k2_hypo0 = g.k2_hypo0;
+  return q;
+}
+
+__device__ __forceinline__ int iy_of(const Geo& g, int b) {
+  return (g.nky_keep == g.ny || b < g.kcy) ? b : b + (g.ny - g.nky_keep);
+}
+
+// A: inverse z pass with the curl (6 output fields, one after the other).
+template <typename T, int LOGN, int TX>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
+          const cplx<T>* __restrict__ twz) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  const int ix = blockIdx.x * TX + c;
+  const int iy = iy_of(g, blockIdx.y);
+  const bool valid = ix < g.ncx;
+  const int64_t plane = (int64_t)g.ny * g.nkx;
+  const int64_t nK = plane * g.nz;
+  const int64_t base = (int64_t)iy * g.nkx + ix;
+  const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
+  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+    C v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int p = jt + r * P::N8;
+      C x = mk<C>(0, 0);
+      if (valid && (!g.pr || kept(p, P::N, g.kcz))) {
+        const int64_t i = base + p * plane;
+        if (f < 3) {
+          x = S[i + f * nK];
+        } else {
+          const T kz = T(g.dkz * kadim(p, P::N));
+          C a, b;
+          T ka, kb;
+          // omega = i k x v: (ky vz - kz vy, kz vx - kx vz, kx vy - ky vx)
+          if (f == 3) { a = S[i + 2 * nK]; b = S[i + nK]; ka = ky; kb = kz; }
+          else if (f == 4) { a = S[i]; b = S[i + 2 * nK]; ka = kz; kb = kx; }
+          else { a = S[i + nK]; b = S[i]; ka = kx; kb = ky; }
+          const C d = mk<C>(ka * a.x - kb * b.x, ka * a.y - kb * b.y);
+          x = mk<C>(-d.y, d.x);
+          if (f == 5 && g.has_f && ix == 0 && iy == 0 && p == 0) x.x += T(g.f);
+        }
+      }
+      v[r] = x;
+    }
+    run<+1, LOGN>(v, jt, true, acc, twz, 1);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int p = jt + P::outm(i) * P::N8;
+        W[f * nK + base + p * plane] = v[i];
+      }
+    }
+  }
+}
+
+// B: x pass.  6 fields x L rows; C2R, v x omega, R2C of the 3 products.
+
+template <typename T, int LOGM, int L>
+__global__ void __launch_bounds__(6 * L * (1 << LOGM) / 8, 2)
+kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
+      const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  using P = Line<LOGM>;
+  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % M8;
+  const int l = (threadIdx.x / M8) % L;
+  const int f = threadIdx.x / (M8 * L);
+  const int64_t nrows = (int64_t)g.nz * g.ny;
+  const int64_t nK = nrows * g.nkx;
+  const int64_t row = (int64_t)blockIdx.x * L + l;
+  const bool valid = row < nrows;
+  C* slot = buf + (f * L + l) * LS;
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  const int kcx = g.pr ? g.kcx : g.nkx + 1;
+  C v[8];
+  {
+    const C* rowp = W + f * nK + row * g.nkx;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int j = jt + r * M8;
+      C Z = mk<C>(0, 0);
+      if (valid) {
+        C a = j < kcx ? rowp[j] : mk<C>(0, 0);
+        C b = (M - j) < kcx ? cconj(rowp[M - j]) : mk<C>(0, 0);
+        if (j == 0) { a.y = 0; b.y = 0; }
+        const C s = cadd(a, b), d = csub(a, b);
+        const C wd = cmulc(d, twx[j]);
+        Z = mk<C>(s.x - wd.y, s.y + wd.x);
+      }
+      v[r] = Z;
+    }
+  }
+  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  __syncthreads();
+  // products (each position of each row handled by one thread)
+  T mx = 0, my = 0, mz = 0;
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int ll = idx / M, j = idx % M;
+    C* p0 = buf + ll * LS + padp<LOGM>(j);
+    const C vx = p0[0], vy = p0[L * LS], vz = p0[2 * L * LS];
+    const C ox = p0[3 * L * LS], oy = p0[4 * L * LS], oz = p0[5 * L * LS];
+    p0[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
+    p0[L * LS] = mk<C>(vz.x * ox.x - vx.x * oz.x, vz.y * ox.y - vx.y * oz.y);
+    p0[2 * L * LS] = mk<C>(vx.x * oy.x - vy.x * ox.x, vx.y * oy.y - vy.y * ox.y);
+    if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
+      mx = fmax(mx, fmax(fabs(vx.x), fabs(vx.y)));
+      my = fmax(my, fmax(fabs(vy.x), fabs(vy.y)));
+      mz = fmax(mz, fmax(fabs(vz.x), fabs(vz.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, mz, vmax);
+  const bool act = f < 3;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
+  run<-1, LOGM>(v, jt, act, acc, twx, 2);
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  }
+  __syncthreads();
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  for (int idx = threadIdx.x; idx < 3 * L * nout; idx += blockDim.x) {
+    const int k = idx % nout;
+    const int fl = idx / nout;  // field * L + row
+    const int ff = fl / L, ll = fl % L;
+    const int64_t rr = (int64_t)blockIdx.x * L + ll;
+    if (rr >= nrows) continue;
+    const C* sl = buf + fl * LS;
+    C a = sl[padp<LOGM>(k == M ? 0 : k)];
+    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
+    const C s = cadd(a, b), d = csub(a, b);
+    const C wd = cmul(twx[k], d);
+    const T h = T(0.5);
+    F[ff * nK + rr * g.nkx + k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+  }
+}
+
+// C: forward z pass + 1/N + projection + dealiasing + RK4 stage.
+template <typename T, int LOGN, int TX>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
+          int mode, RKArgs a) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  constexpr int N = P::N, N8 = P::N8;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  const int ix = blockIdx.x * TX + c;
+  const int iy = iy_of(g, blockIdx.y);
+  const bool valid = ix < g.ncx;
+  const int64_t plane = (int64_t)g.ny * g.nkx;
+  const int64_t nK = plane * g.nz;
+  const int64_t base = (int64_t)iy * g.nkx + ix;
+#pragma unroll 1
+  for (int f = 0; f < 3; ++f) {
+    C v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+      v[r] = valid ? F[f * nK + base + (jt + r * N8) * plane] : mk<C>(0, 0);
+    C* slot = buf + f * N * TX;
+    auto acc = [&](int p) -> C& { return slot[p * TX + c]; };
+    run<-1, LOGN>(v, jt, true, acc, twz, 1);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = v[i];
+  }
+  __syncthreads();
+  if (!valid) return;
+  const int kyi = kadim(iy, g.ny);
+  const T kx = T(g.dkx * ix), ky = T(g.dky * kyi);
+  const T inv_n = T(g.inv_n);
+  const Phys q = phys_of(g);
+#pragma unroll 1
+  for (int r = 0; r < 8; ++r) {
+    const int iz = jt + r * N8;
+    const int kzi = kadim(iz, N);
+    const bool rm = (ix >= g.kcx) || (iabs(kyi) >= g.kcy) || (iabs(kzi) >= g.kcz);
+    if (g.pr && rm) continue;  // stays zero in S, tmp and tmp1
+    const int64_t i = base + iz * plane;
+    const T kz = T(g.dkz * kzi);
+    C N3[3];
+#pragma unroll
+    for (int ff = 0; ff < 3; ++ff) N3[ff] = cscale(buf[ff * N * TX + iz * TX + c], inv_n);
+    const T k2 = kx * kx + ky * ky + kz * kz;
+    const bool k0 = (ix == 0 && kyi == 0 && kzi == 0);
+    stage_epilogue3<C, T>(mode, a, i, nK, N3, kx, ky, kz, k2, k0, rm, q);
+  }
+}
+
+// ----------------------------------------------------- ns2d kernels
+// A: inverse y pass; fields ux, uy, d_x rot, d_y rot.
+template <typename T, int LOGN, int TX>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
+          const cplx<T>* __restrict__ twy) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  const int ix = blockIdx.x * TX + c;
+  const bool valid = ix < g.ncx;
+  const int64_t nK = (int64_t)g.ny * g.nkx;
+  const T kx = T(g.dkx * ix);
+  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+#pragma unroll 1
+  for (int f = 0; f < 4; ++f) {
+    C v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int p = jt + r * P::N8;
+      C x = mk<C>(0, 0);
+      if (valid && (!g.pr || kept(p, P::N, g.kcy))) {
+        const C w = S[(int64_t)p * g.nkx + ix];
+        const int kyi = kadim(p, P::N);
+        const T ky = T(g.dky * kyi);
+        T cc;
+        if (f == 0 || f == 1) {
+          const T k2 = kx * kx + ky * ky;
+          const T inv = (ix == 0 && kyi == 0) ? T(0) : T(1) / k2;
+          cc = f == 0 ? ky * inv : -(kx * inv);
+        } else {
+          cc = f == 2 ? kx : ky;
+        }
+        x = mk<C>(-cc * w.y, cc * w.x);
+      }
+      v[r] = x;
+    }
+    run<+1, LOGN>(v, jt, true, acc, twy, 1);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        W[f * nK + (int64_t)(jt + P::outm(i) * P::N8) * g.nkx + ix] = v[i];
+    }
+  }
+}
+
+// B: x pass, compute_Frot = -ux d_x rot - uy (d_y rot + beta).
+template <typename T, int LOGM, int L>
+__global__ void __launch_bounds__(4 * L * (1 << LOGM) / 8, 2)
+kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
+      const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  using P = Line<LOGM>;
+  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % M8;
+  const int l = (threadIdx.x / M8) % L;
+  const int f = threadIdx.x / (M8 * L);
+  const int64_t nrows = g.ny;
+  const int64_t nK = nrows * g.nkx;
+  const int64_t row = (int64_t)blockIdx.x * L + l;
+  const bool valid = row < nrows;
+  C* slot = buf + (f * L + l) * LS;
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  const int kcx = g.pr ? g.kcx : g.nkx + 1;
+  C v[8];
+  {
+    const C* rowp = W + f * nK + row * g.nkx;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int j = jt + r * M8;
+      C Z = mk<C>(0, 0);
+      if (valid) {
+        C a = j < kcx ? rowp[j] : mk<C>(0, 0);
+        C b = (M - j) < kcx ? cconj(rowp[M - j]) : mk<C>(0, 0);
+        if (j == 0) { a.y = 0; b.y = 0; }
+        const C s = cadd(a, b), d = csub(a, b);
+        const C wd = cmulc(d, twx[j]);
+        Z = mk<C>(s.x - wd.y, s.y + wd.x);
+      }
+      v[r] = Z;
+    }
+  }
+  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  __syncthreads();
+  T mx = 0, my = 0;
+  const T beta = T(g.beta);
+  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
+    const int ll = idx / M, j = idx % M;
+    C* p0 = buf + ll * LS + padp<LOGM>(j);
+    const C ux = p0[0], uy = p0[L * LS], px = p0[2 * L * LS], py = p0[3 * L * LS];
+    C res;
+    if (g.beta == 0)
+      res = mk<C>(-ux.x * px.x - uy.x * py.x, -ux.y * px.y - uy.y * py.y);
+    else
+      res = mk<C>(-ux.x * px.x - uy.x * (py.x + beta), -ux.y * px.y - uy.y * (py.y + beta));
+    p0[0] = res;
+    if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
+      mx = fmax(mx, fmax(fabs(ux.x), fabs(ux.y)));
+      my = fmax(my, fmax(fabs(uy.x), fabs(uy.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, T(0), vmax);
+  const bool act = f == 0;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
+  run<-1, LOGM>(v, jt, act, acc, twx, 2);
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  }
+  __syncthreads();
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  for (int idx = threadIdx.x; idx < L * nout; idx += blockDim.x) {
+    const int k = idx % nout, ll = idx / nout;
+    const int64_t rr = (int64_t)blockIdx.x * L + ll;
+    if (rr >= nrows) continue;
+    const C* sl = buf + ll * LS;
+    C a = sl[padp<LOGM>(k == M ? 0 : k)];
+    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
+    const C s = cadd(a, b), d = csub(a, b);
+    const C wd = cmul(twx[k], d);
+    const T h = T(0.5);
+    F[rr * g.nkx + k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+  }
+}
+
+// C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
+template <typename T, int LOGN, int TX>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
+          int mode, RKArgs a) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  const int ix = blockIdx.x * TX + c;
+  const bool valid = ix < g.ncx;
+  C v[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r)
+    v[r] = valid ? F[(int64_t)(jt + r * P::N8) * g.nkx + ix] : mk<C>(0, 0);
+  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  run<-1, LOGN>(v, jt, true, acc, twy, 1);
+  if (!valid) return;
+  const T kx = T(g.dkx * ix);
+  const T inv_n = T(g.inv_n);
+  const Phys q = phys_of(g);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int iy = jt + P::outm(i) * P::N8;
+    const int kyi = kadim(iy, P::N);
+    const bool rm = ix >= g.kcx || iabs(kyi) >= g.kcy;
+    if (g.pr && rm) continue;
+    const T ky = T(g.dky * kyi);
+    stage_epilogue1<C, T>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
+                          kx * kx + ky * ky, ix == 0 && kyi == 0, rm, q);
+  }
+}
+
+}  // namespace fast
+}  // namespace gbs

@@ -1,0 +1,265 @@
+// Launch shapes and runtime dispatch for the compile-time-size kernels.
+#pragma once
+
+#include "gbs_fast.cuh"
+#include "gbs_fast_api.h"
+
+namespace gbs {
+namespace fast {
+
+// columns per CTA for the strided passes: 64 B segments in FP32 and FP64
+template <typename T> constexpr int tx_cols() { return sizeof(T) == 4 ? 8 : 4; }
+// rows per CTA for the x passes
+template <typename T, int LOGM, int NF> constexpr int rows_x() {
+  constexpr int M8 = (1 << LOGM) / 8;
+  constexpr int budget = (sizeof(T) == 4 ? 384 : 192) / NF;
+  return budget / M8 > 0 ? budget / M8 : 1;
+}
+
+template <typename K>
+static int prep(K kernel, size_t smem) {
+  if (smem > 48 * 1024) {
+    GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  }
+  GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    cudaSharedmemCarveoutMaxShared));
+  return GBS_OK;
+}
+
+#define GBS_LOG_SWITCH(logv, BODY)                    \
+  switch (logv) {                                     \
+    case 5: { constexpr int LG = 5; BODY; } break;    \
+    case 6: { constexpr int LG = 6; BODY; } break;    \
+    case 7: { constexpr int LG = 7; BODY; } break;    \
+    case 8: { constexpr int LG = 8; BODY; } break;    \
+    case 9: { constexpr int LG = 9; BODY; } break;    \
+    case 10: { constexpr int LG = 10; BODY; } break;  \
+    default:                                          \
+      set_error("no compiled kernel for this size");  \
+      return GBS_EINVAL;                              \
+  }
+
+template <typename T, int LOGN, int DIR>
+static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, int nfields,
+                      const void* tw, double scale, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int TX = tx_cols<T>();
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
+  if (rc) return rc;
+  dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
+  kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
+                                                 static_cast<C*>(out), a,
+                                                 static_cast<const C*>(tw), T(scale));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int col(int n, const void* in, void* out, const ColArgs& a, int nouter, int nfields,
+        const void* tw, double scale, int dir, cudaStream_t st) {
+  const int lg = ilog2(n);
+  if (dir > 0) {
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, 1>(in, out, a, nouter, nfields, tw, scale, st)));
+  } else {
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, -1>(in, out, a, nouter, nfields, tw, scale, st)));
+  }
+  return GBS_OK;
+}
+
+template <typename T, int LOGM>
+static int r2c_launch(const void* x, void* k, int64_t nrows, const void* tw, double scale,
+                      cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int M = 1 << LOGM;
+  constexpr int L = (sizeof(T) == 4 ? 256 : 128) / (M / 8) > 0 ? (sizeof(T) == 4 ? 256 : 128) / (M / 8) : 1;
+  constexpr int TH = L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)L * (M + M / 8);
+  int rc = prep(kf_row_r2c<T, LOGM, L>, smem);
+  if (rc) return rc;
+  kf_row_r2c<T, LOGM, L><<<ceil_div(nrows, L), TH, smem, st>>>(
+      static_cast<const T*>(x), static_cast<C*>(k), nrows, static_cast<const C*>(tw), T(scale));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int r2c_rows(int nx, const void* x, void* k, int64_t nrows, const void* twx, double scale,
+             cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(nx / 2), return (r2c_launch<T, LG>(x, k, nrows, twx, scale, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGM>
+static int c2r_launch(const void* k, void* x, int64_t nrows, const void* tw, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int M = 1 << LOGM;
+  constexpr int L = (sizeof(T) == 4 ? 256 : 128) / (M / 8) > 0 ? (sizeof(T) == 4 ? 256 : 128) / (M / 8) : 1;
+  constexpr int TH = L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)L * (M + M / 8);
+  int rc = prep(kf_row_c2r<T, LOGM, L>, smem);
+  if (rc) return rc;
+  kf_row_c2r<T, LOGM, L><<<ceil_div(nrows, L), TH, smem, st>>>(
+      static_cast<const C*>(k), static_cast<T*>(x), nrows, static_cast<const C*>(tw));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int c2r_rows(int nx, const void* k, void* x, int64_t nrows, const void* twx, cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(nx / 2), return (c2r_launch<T, LG>(k, x, nrows, twx, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGN>
+static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int TX = tx_cols<T>();
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf3_inv_z<T, LOGN, TX>, smem);
+  if (rc) return rc;
+  dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);
+  kf3_inv_z<T, LOGN, TX><<<grid, TH, smem, st>>>(static_cast<const C*>(S),
+                                                static_cast<C*>(W), g,
+                                                static_cast<const C*>(tw));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int A3(const Geo& g, const void* S, void* W, const void* twz, cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.nz), return (A3_launch<T, LG>(g, S, W, twz, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGM>
+static int B3_launch(const Geo& g, const void* W, void* F, const void* tw,
+                     unsigned long long* vmax, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int L = rows_x<T, LOGM, 6>();
+  constexpr int M = 1 << LOGM;
+  constexpr int TH = 6 * L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)6 * L * (M + M / 8);
+  int rc = prep(kf3_x<T, LOGM, L>, smem);
+  if (rc) return rc;
+  kf3_x<T, LOGM, L><<<ceil_div((int64_t)g.nz * g.ny, L), TH, smem, st>>>(
+      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int B3(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
+       cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.M), return (B3_launch<T, LG>(g, W, F, twx, vmax, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGN>
+static int C3_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
+                     cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int TX = tx_cols<T>();
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)3 * (1 << LOGN) * TX;
+  int rc = prep(kf3_fwd_z<T, LOGN, TX>, smem);
+  if (rc) return rc;
+  dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);
+  kf3_fwd_z<T, LOGN, TX><<<grid, TH, smem, st>>>(static_cast<const C*>(F), g,
+                                                static_cast<const C*>(tw), mode, a);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int C3(const Geo& g, const void* F, const void* twz, int mode, const RKArgs& a,
+       cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG>(g, F, twz, mode, a, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGN>
+static int A2_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int TX = tx_cols<T>();
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf2_inv_y<T, LOGN, TX>, smem);
+  if (rc) return rc;
+  kf2_inv_y<T, LOGN, TX><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
+      static_cast<const C*>(S), static_cast<C*>(W), g, static_cast<const C*>(tw));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int A2(const Geo& g, const void* S, void* W, const void* twy, cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.ny), return (A2_launch<T, LG>(g, S, W, twy, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGM>
+static int B2_launch(const Geo& g, const void* W, void* F, const void* tw,
+                     unsigned long long* vmax, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int L = rows_x<T, LOGM, 4>();
+  constexpr int M = 1 << LOGM;
+  constexpr int TH = 4 * L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)4 * L * (M + M / 8);
+  int rc = prep(kf2_x<T, LOGM, L>, smem);
+  if (rc) return rc;
+  kf2_x<T, LOGM, L><<<ceil_div(g.ny, L), TH, smem, st>>>(
+      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int B2(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
+       cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.M), return (B2_launch<T, LG>(g, W, F, twx, vmax, st)));
+  return GBS_OK;
+}
+
+template <typename T, int LOGN>
+static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
+                     cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int TX = tx_cols<T>();
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf2_fwd_y<T, LOGN, TX>, smem);
+  if (rc) return rc;
+  kf2_fwd_y<T, LOGN, TX><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
+      static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <typename T>
+int C2(const Geo& g, const void* F, const void* twy, int mode, const RKArgs& a,
+       cudaStream_t st) {
+  GBS_LOG_SWITCH(ilog2(g.ny), return (C2_launch<T, LG>(g, F, twy, mode, a, st)));
+  return GBS_OK;
+}
+
+#define GBS_FAST_INSTANTIATE(T)                                                              \
+  template int r2c_rows<T>(int, const void*, void*, int64_t, const void*, double,            \
+                           cudaStream_t);                                                    \
+  template int c2r_rows<T>(int, const void*, void*, int64_t, const void*, cudaStream_t);     \
+  template int col<T>(int, const void*, void*, const ColArgs&, int, int, const void*, double, \
+                      int, cudaStream_t);                                                    \
+  template int A3<T>(const Geo&, const void*, void*, const void*, cudaStream_t);             \
+  template int B3<T>(const Geo&, const void*, void*, const void*, unsigned long long*,       \
+                     cudaStream_t);                                                          \
+  template int C3<T>(const Geo&, const void*, const void*, int, const RKArgs&, cudaStream_t); \
+  template int A2<T>(const Geo&, const void*, void*, const void*, cudaStream_t);             \
+  template int B2<T>(const Geo&, const void*, void*, const void*, unsigned long long*,       \
+                     cudaStream_t);                                                          \
+  template int C2<T>(const Geo&, const void*, const void*, int, const RKArgs&, cudaStream_t);
+
+}  // namespace fast
+}  // namespace gbs

@@ -13,6 +13,8 @@
 #include <new>
 
 #include "gbs_internal.cuh"
+#include "gbs_fast.cuh"
+#include "gbs_fast_api.h"
 
 namespace gbs {
 
@@ -238,6 +240,39 @@ struct Plan {
   void* work;      // batch * nK complex
 };
 
+// Axis passes: compile-time-size kernels where the length has one, the
+// generic kernels otherwise.
+template <typename T, int DIR>
+int axis_col(const cplx<T>* in, cplx<T>* out, int n, int ncols, int nouter, int nfields,
+             int64_t es, int64_t os, int64_t fs, const cplx<T>* tw, T scale,
+             cudaStream_t st) {
+  if (fast::supported_axis(n)) {
+    fast::ColArgs a;
+    a.ncols = ncols;
+    a.kc_in = n + 1;
+    a.kc_out = n + 1;
+    a.es = es;
+    a.os = os;
+    a.fs = fs;
+    return fast::col<T>(n, in, out, a, nouter, nfields, tw, (double)scale, DIR, st);
+  }
+  return launch_col<T, DIR>(in, out, n, ncols, nouter, nfields, es, os, fs, tw, scale, st);
+}
+
+template <typename T>
+int axis_r2c(const T* x, cplx<T>* k, int nx, int64_t nrows, const cplx<T>* twx, T scale,
+             cudaStream_t st) {
+  if (fast::supported_axis(nx / 2)) return fast::r2c_rows<T>(nx, x, k, nrows, twx, scale, st);
+  return launch_r2c_rows<T>(x, k, nx, nrows, twx, scale, st);
+}
+
+template <typename T>
+int axis_c2r(const cplx<T>* k, T* x, int nx, int64_t nrows, const cplx<T>* twx,
+             cudaStream_t st) {
+  if (fast::supported_axis(nx / 2)) return fast::c2r_rows<T>(nx, k, x, nrows, twx, st);
+  return launch_c2r_rows<T>(k, x, nx, nrows, twx, st);
+}
+
 template <typename T>
 int plan_r2c(Plan* p, const void* xv, void* kv, cudaStream_t st) {
   using C = cplx<T>;
@@ -251,17 +286,17 @@ int plan_r2c(Plan* p, const void* xv, void* kv, cudaStream_t st) {
   int rc;
   const int64_t rows = (int64_t)p->batch * p->nz * p->ny;
   if (p->ndim == 2) {
-    rc = launch_r2c_rows<T>(x, k, p->nx, rows, twx, T(1), st);
+    rc = axis_r2c<T>(x, k, p->nx, rows, twx, T(1), st);
     if (rc) return rc;
-    return launch_col<T, -1>(k, k, p->ny, nkx, 1, p->batch, nkx, 0, p->nK,
+    return axis_col<T, -1>(k, k, p->ny, nkx, 1, p->batch, nkx, 0, p->nK,
                              twy, inv, st);
   }
-  rc = launch_r2c_rows<T>(x, k, p->nx, rows, twx, T(1), st);
+  rc = axis_r2c<T>(x, k, p->nx, rows, twx, T(1), st);
   if (rc) return rc;
-  rc = launch_col<T, -1>(k, k, p->ny, nkx, p->nz, p->batch, nkx,
+  rc = axis_col<T, -1>(k, k, p->ny, nkx, p->nz, p->batch, nkx,
                          (int64_t)p->ny * nkx, p->nK, twy, T(1), st);
   if (rc) return rc;
-  return launch_col<T, -1>(k, k, p->nz, nkx, p->ny, p->batch,
+  return axis_col<T, -1>(k, k, p->nz, nkx, p->ny, p->batch,
                            (int64_t)p->ny * nkx, nkx, p->nK, twz, inv, st);
 }
 
@@ -278,18 +313,18 @@ int plan_c2r(Plan* p, void* kv, void* xv, int destroy, cudaStream_t st) {
   const int64_t rows = (int64_t)p->batch * p->nz * p->ny;
   int rc;
   if (p->ndim == 2) {
-    rc = launch_col<T, 1>(k, w, p->ny, nkx, 1, p->batch, nkx, 0, p->nK, twy,
+    rc = axis_col<T, 1>(k, w, p->ny, nkx, 1, p->batch, nkx, 0, p->nK, twy,
                           T(1), st);
     if (rc) return rc;
-    return launch_c2r_rows<T>(w, x, p->nx, rows, twx, st);
+    return axis_c2r<T>(w, x, p->nx, rows, twx, st);
   }
-  rc = launch_col<T, 1>(k, w, p->nz, nkx, p->ny, p->batch,
+  rc = axis_col<T, 1>(k, w, p->nz, nkx, p->ny, p->batch,
                         (int64_t)p->ny * nkx, nkx, p->nK, twz, T(1), st);
   if (rc) return rc;
-  rc = launch_col<T, 1>(w, w, p->ny, nkx, p->nz, p->batch, nkx,
+  rc = axis_col<T, 1>(w, w, p->ny, nkx, p->nz, p->batch, nkx,
                         (int64_t)p->ny * nkx, p->nK, twy, T(1), st);
   if (rc) return rc;
-  return launch_c2r_rows<T>(w, x, p->nx, rows, twx, st);
+  return axis_c2r<T>(w, x, p->nx, rows, twx, st);
 }
 
 int twiddle_alloc(void** out, int n, int dtype, cudaStream_t st) {

@@ -17,6 +17,9 @@
 #include <new>
 
 #include "gbs_internal.cuh"
+#include "gbs_ns.cuh"
+#include "gbs_fast.cuh"
+#include "gbs_fast_api.h"
 
 namespace gbs {
 
@@ -41,94 +44,18 @@ struct NSK {
   int TX, L, LP;
 };
 
-// RK4 stage selector for kernel C.
-enum Mode { kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4 };
-
-struct RKArgs {
-  const void* S;  // state (read) for kRK0..kRK2
-  void* Sout;     // state (write) for kRK3
-  void* tmp;      // _state_spect_tmp
-  void* tmp1;     // _state_spect_tmp1
-  void* tend;     // output for kTend
-  double dt;
-  int* nan_flag;
-};
-
 __device__ __forceinline__ bool removed(const NSK& q, int ix, int ky, int kz) {
   return ix >= q.kcx || iabs(ky) >= q.kcy || iabs(kz) >= q.kcz;
 }
 
-// sigma(k) = f_d + f_d_hypo, fluidsim/base/solvers/pseudo_spect.py:166-191
-template <typename T>
-__device__ __forceinline__ T freq_lin(const NSK& q, T k2, bool k0) {
-  T fd = q.nu2 > 0 ? T(q.nu2) * k2 : T(0);
-  if (q.nu4 > 0) fd += T(q.nu4) * (k2 * k2);
-  if (q.nu8 > 0) {
-    T k4 = k2 * k2;
-    fd += T(q.nu8) * (k4 * k4);
-  }
-  if (q.num4 != 0) {
-    T k2n0 = k0 ? T(q.k2_hypo0) : k2;
-    fd += T(q.num4) / (k2n0 * k2n0);
-  }
-  return fd;
-}
-
-__device__ __forceinline__ double dexp(double x) { return exp(x); }
-__device__ __forceinline__ float dexp(float x) { return expf(x); }
-
-// RK4 stage update at one mode, pseudo_spect.py:898-984 (same evaluation
-// order as the numpy expressions there).
-template <typename C, typename T>
-__device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
-                                         C N, T sigma) {
-  const T dt = T(a.dt);
-  C* tmp = static_cast<C*>(a.tmp);
-  C* tmp1 = static_cast<C*>(a.tmp1);
-  if (mode == kRK0) {
-    const C S = static_cast<const C*>(a.S)[i];
-    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
-    T c6 = dt / T(6), c2 = dt / T(2);
-    tmp[i] = cscale(mk<C>(S.x + c6 * N.x, S.y + c6 * N.y), E);
-    tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
-  } else if (mode == kRK1) {
-    const C S = static_cast<const C*>(a.S)[i];
-    T E2 = dexp(-dt / T(2) * sigma);
-    T c3 = dt / T(3) * E2, c2 = dt / T(2);
-    C t = tmp[i];
-    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
-    tmp1[i] = mk<C>(S.x * E2 + c2 * N.x, S.y * E2 + c2 * N.y);
-  } else if (mode == kRK2) {
-    const C S = static_cast<const C*>(a.S)[i];
-    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
-    T c3 = dt / T(3) * E2, c1 = dt * E2;
-    C t = tmp[i];
-    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
-    tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void block_max3(T a, T b, T c,
-                                           unsigned long long* dst) {
-  __shared__ double red[3][32];
-  double v[3] = {(double)a, (double)b, (double)c};
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    for (int o = 16; o; o >>= 1) v[k] = fmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
-    if (lane == 0) red[k][w] = v[k];
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double x = lane < nw ? red[k][lane] : 0.0;
-      for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-      if (lane == 0) atomicMax(dst + k, (unsigned long long)__double_as_longlong(x));
-    }
-  }
+__device__ __forceinline__ Phys phys(const NSK& q) {
+  Phys p;
+  p.nu2 = q.nu2;
+  p.nu4 = q.nu4;
+  p.nu8 = q.nu8;
+  p.num4 = q.num4;
+  p.k2_hypo0 = q.k2_hypo0;
+  return p;
 }
 
 // C2R pre-processing of row element j (see k_row_c2r in gbs_fft.cu).
@@ -328,7 +255,7 @@ k3_fwd_z_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
       for (int f = 0; f < 3; ++f) So[i + f * nK] = Sn[f];
       if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
     } else {
-      const T sig = freq_lin<T>(q, k2, k0);
+      const T sig = freq_lin<T>(phys(q), k2, k0);
 #pragma unroll
       for (int f = 0; f < 3; ++f) rk_update<C, T>(mode, a, i + f * nK, N[f], sig);
     }
@@ -467,7 +394,7 @@ k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
     } else {
       const T kx = T(q.dkx * ix), ky = T(q.dky * kyi);
       const T k2 = kx * kx + ky * ky;
-      const T sig = freq_lin<T>(q, k2, ix == 0 && kyi == 0);
+      const T sig = freq_lin<T>(phys(q), k2, ix == 0 && kyi == 0);
       rk_update<C, T>(mode, a, i, N, sig);
     }
   }
@@ -500,7 +427,10 @@ struct Solver {
   double t_ms[kKinds];
   long long t_count[kKinds];
   long long launches;
-  // launch shapes
+  // compile-time-size path (all axes powers of two in range)
+  int use_fast;
+  fast::Geo geo;
+  // launch shapes of the generic path
   int txA, txC, Lb;
   int thA, thB, thC;
   size_t smA, smB, smC;
@@ -597,9 +527,74 @@ static int setup_shapes(Solver* s) {
 }
 
 // One tendency evaluation from `in`; kernel C runs `mode`.
+static fast::Geo geo_for(const Solver* s, bool pruned) {
+  fast::Geo g = s->geo;
+  g.pr = pruned ? 1 : 0;
+  g.ncx = pruned ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  const int nkeep = 2 * g.kcy - 1;
+  g.nky_keep = (pruned && nkeep < g.ny) ? nkeep : g.ny;
+  return g;
+}
+
+// compile-time-size path: same passes as the generic one, optionally pruned
+template <typename T>
+static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, cudaStream_t st) {
+  const fast::Geo g = geo_for(s, pruned);
+  unsigned long long* vmax = want_max ? s->dmax : nullptr;
+  int rc;
+  const int kcy_in = pruned ? g.kcy : g.ny + 1;
+  if (s->p.ndim == 3) {
+    {
+      LaunchScope ls(s, 0, st);
+      rc = fast::A3<T>(g, in, s->W, s->tw[2], st);
+    }
+    if (rc) return rc;
+    fast::ColArgs ca;
+    ca.ncols = g.ncx;
+    ca.kc_in = kcy_in;
+    ca.kc_out = g.ny + 1;
+    ca.es = g.nkx;
+    ca.os = (int64_t)g.ny * g.nkx;
+    ca.fs = s->nK;
+    {
+      LaunchScope ls(s, 1, st);
+      rc = fast::col<T>(g.ny, s->W, s->W, ca, g.nz, 6, s->tw[1], 1.0, +1, st);
+    }
+    if (rc) return rc;
+    {
+      LaunchScope ls(s, 2, st);
+      rc = fast::B3<T>(g, s->W, s->F, s->tw[0], vmax, st);
+    }
+    if (rc) return rc;
+    ca.kc_in = g.ny + 1;
+    ca.kc_out = kcy_in;
+    {
+      LaunchScope ls(s, 3, st);
+      rc = fast::col<T>(g.ny, s->F, s->F, ca, g.nz, 3, s->tw[1], 1.0, -1, st);
+    }
+    return rc;
+  }
+  {
+    LaunchScope ls(s, 0, st);
+    rc = fast::A2<T>(g, in, s->W, s->tw[1], st);
+  }
+  if (rc) return rc;
+  LaunchScope ls(s, 2, st);
+  return fast::B2<T>(g, s->W, s->F, s->tw[0], vmax, st);
+}
+
+template <typename T>
+static int finish_fast(Solver* s, int mode, const RKArgs& a, bool pruned, cudaStream_t st) {
+  const fast::Geo g = geo_for(s, pruned);
+  LaunchScope ls(s, 4, st);
+  if (s->p.ndim == 3) return fast::C3<T>(g, s->F, s->tw[2], mode, a, st);
+  return fast::C2<T>(g, s->F, s->tw[1], mode, a, st);
+}
+
 template <typename T>
 static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
-                bool want_max, cudaStream_t st) {
+                bool want_max, cudaStream_t st, bool pruned = false) {
+  if (s->use_fast) return eval_fast<T>(s, in, pruned, want_max, st);
   using C = cplx<T>;
   NSK q = s->q;
   const C* twx = static_cast<const C*>(s->tw[0]);
@@ -659,7 +654,9 @@ static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
 }
 
 template <typename T>
-static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st) {
+static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st,
+                  bool pruned = false) {
+  if (s->use_fast) return finish_fast<T>(s, mode, a, pruned, st);
   using C = cplx<T>;
   NSK q = s->q;
   const C* F = static_cast<const C*>(s->F);
@@ -705,8 +702,10 @@ static double cfl_tmp(const Solver* s, const double* m) {
 }
 
 template <typename T>
-static int step(Solver* s, void* S, double* dt, const double* cfl,
-                int check_nan, cudaStream_t st) {
+static int step(Solver* s, void* S, double* dt, const double* cfl, int flags,
+                cudaStream_t st) {
+  const int check_nan = flags & GBS_STEP_CHECK_NAN;
+  const bool pr = (flags & GBS_STEP_DEALIASED) != 0;
   RKArgs a{};
   a.S = S;
   a.Sout = S;
@@ -716,7 +715,7 @@ static int step(Solver* s, void* S, double* dt, const double* cfl,
   int rc;
   if (cfl) GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
   if (check_nan) GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
-  rc = eval<T>(s, S, kRK0, a, cfl != nullptr, st);
+  rc = eval<T>(s, S, kRK0, a, cfl != nullptr, st, pr);
   if (rc) return rc;
   if (cfl) {
     GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
@@ -725,12 +724,12 @@ static int step(Solver* s, void* S, double* dt, const double* cfl,
     *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
   }
   a.dt = *dt;
-  rc = finish<T>(s, kRK0, a, st);
+  rc = finish<T>(s, kRK0, a, st, pr);
   if (rc) return rc;
   for (int m = kRK1; m <= kRK3; ++m) {
-    rc = eval<T>(s, s->tmp1, m, a, false, st);
+    rc = eval<T>(s, s->tmp1, m, a, false, st, pr);
     if (rc) return rc;
-    rc = finish<T>(s, m, a, st);
+    rc = finish<T>(s, m, a, st, pr);
     if (rc) return rc;
   }
   if (check_nan) {
@@ -988,6 +987,33 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   }
   if (!rc) rc = p.dtype == GBS_F64 ? gbs::setup_shapes<double>(s) : gbs::setup_shapes<float>(s);
   if (!rc) {
+    s->use_fast = gbs::fast::supported(p.ndim, q.nx, q.ny, q.nz) ? 1 : 0;
+    gbs::fast::Geo& g = s->geo;
+    g.nx = q.nx;
+    g.ny = q.ny;
+    g.nz = q.nz;
+    g.nkx = q.nkx;
+    g.M = q.M;
+    g.kcx = q.kcx;
+    g.kcy = q.kcy;
+    g.kcz = q.kcz;
+    g.ncx = q.nkx;
+    g.nky_keep = q.ny;
+    g.pr = 0;
+    g.dkx = q.dkx;
+    g.dky = q.dky;
+    g.dkz = q.dkz;
+    g.nu2 = q.nu2;
+    g.nu4 = q.nu4;
+    g.nu8 = q.nu8;
+    g.num4 = q.num4;
+    g.beta = q.beta;
+    g.f = q.f;
+    g.inv_n = q.inv_n;
+    g.k2_hypo0 = q.k2_hypo0;
+    g.has_f = q.has_f;
+  }
+  if (!rc) {
     // tmp / tmp1 start at zero so that modes never written stay zero
     if (cudaMemset(s->tmp, 0, fb * s->nvar) != cudaSuccess ||
         cudaMemset(s->tmp1, 0, fb * s->nvar) != cudaSuccess ||
@@ -1024,7 +1050,7 @@ int gbs_ns_tendencies(gbs_ns* h, const void* S, void* tend, void* stream) {
 }
 
 int gbs_ns_step_rk4(gbs_ns* h, void* S, double* dt, const double* cfl,
-                    int check_nan, void* stream) {
+                    int flags, void* stream) {
   gbs::clear_error();
   if (!h || !S || !dt || !(*dt > 0)) {
     gbs::set_error("gbs_ns_step_rk4: invalid argument");
@@ -1035,8 +1061,8 @@ int gbs_ns_step_rk4(gbs_ns* h, void* S, double* dt, const double* cfl,
     return GBS_EINVAL;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (h->s.p.dtype == GBS_F64) return gbs::step<double>(&h->s, S, dt, cfl, check_nan, st);
-  return gbs::step<float>(&h->s, S, dt, cfl, check_nan, st);
+  if (h->s.p.dtype == GBS_F64) return gbs::step<double>(&h->s, S, dt, cfl, flags, st);
+  return gbs::step<float>(&h->s, S, dt, cfl, flags, st);
 }
 
 int gbs_ns_max_velocity(gbs_ns* h, const void* S, double* out, void* stream) {

@@ -1,0 +1,173 @@
+// Device helpers shared by the generic and the compile-time-size ns kernels:
+// RK4 stage selector and arguments, dissipation frequency, the per-mode RK4
+// update, the fused projection / dealiasing / stage epilogue, and the block
+// max reduction used for the CFL condition.
+#pragma once
+
+#include "gbs_core.cuh"
+
+namespace gbs {
+
+// RK4 stage selector for the last pass of a tendency evaluation.
+enum Mode { kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4 };
+
+struct RKArgs {
+  const void* S;  // state (read) for kRK0..kRK2
+  void* Sout;     // state (write) for kRK3
+  void* tmp;      // _state_spect_tmp
+  void* tmp1;     // _state_spect_tmp1
+  void* tend;     // output for kTend
+  double dt;
+  int* nan_flag;
+};
+
+// Viscosities for sigma(k) = f_d + f_d_hypo.
+struct Phys {
+  double nu2, nu4, nu8, num4;
+  double k2_hypo0;  // K2 at (0, .., 1): the value f_d_hypo[0, .., 0] copies
+};
+
+// fluidsim/base/solvers/pseudo_spect.py:166-191
+template <typename T>
+__device__ __forceinline__ T freq_lin(const Phys& q, T k2, bool k0) {
+  T fd = q.nu2 > 0 ? T(q.nu2) * k2 : T(0);
+  if (q.nu4 > 0) fd += T(q.nu4) * (k2 * k2);
+  if (q.nu8 > 0) {
+    T k4 = k2 * k2;
+    fd += T(q.nu8) * (k4 * k4);
+  }
+  if (q.num4 != 0) {
+    T k2n0 = k0 ? T(q.k2_hypo0) : k2;
+    fd += T(q.num4) / (k2n0 * k2n0);
+  }
+  return fd;
+}
+
+__device__ __forceinline__ double dexp(double x) { return exp(x); }
+__device__ __forceinline__ float dexp(float x) { return expf(x); }
+
+// RK4 stage update at one mode, pseudo_spect.py:898-984 (same evaluation
+// order as the numpy expressions there).
+template <typename C, typename T>
+__device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
+                                         C N, T sigma) {
+  const T dt = T(a.dt);
+  C* tmp = static_cast<C*>(a.tmp);
+  C* tmp1 = static_cast<C*>(a.tmp1);
+  if (mode == kRK0) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c6 = dt / T(6), c2 = dt / T(2);
+    tmp[i] = cscale(mk<C>(S.x + c6 * N.x, S.y + c6 * N.y), E);
+    tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
+  } else if (mode == kRK1) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c2 = dt / T(2);
+    C t = tmp[i];
+    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1[i] = mk<C>(S.x * E2 + c2 * N.x, S.y * E2 + c2 * N.y);
+  } else if (mode == kRK2) {
+    const C S = static_cast<const C*>(a.S)[i];
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c1 = dt * E2;
+    C t = tmp[i];
+    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  }
+}
+
+// project_perpk3d: v -= k (k.v)/|k|^2; the k = 0 mode is left unchanged
+template <typename C, typename T>
+__device__ __forceinline__ void project3(C (&v)[3], T kx, T ky, T kz, T k2, bool k0) {
+  if (k0) return;
+  const T inv = T(1) / k2;
+  C t = mk<C>((kx * v[0].x + ky * v[1].x + kz * v[2].x) * inv,
+              (kx * v[0].y + ky * v[1].y + kz * v[2].y) * inv);
+  v[0] = csub(v[0], cscale(t, kx));
+  v[1] = csub(v[1], cscale(t, ky));
+  v[2] = csub(v[2], cscale(t, kz));
+}
+
+// ns3d epilogue at one mode: N (already scaled by 1/N) -> projection,
+// dealiasing, then the stage `mode` (ns3d/solver.py:251-252,
+// ns3d/time_stepping.py:12-20).
+template <typename C, typename T>
+__device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64_t i,
+                                                int64_t nK, C (&N)[3], T kx, T ky,
+                                                T kz, T k2, bool k0, bool rm,
+                                                const Phys& q) {
+  project3(N, kx, ky, kz, k2, k0);
+  if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
+  if (mode == kTend) {
+    C* o = static_cast<C*>(a.tend);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
+  } else if (mode == kRK3) {
+    const C* tmp = static_cast<const C*>(a.tmp);
+    const T c6 = T(a.dt) / T(6);
+    C Sn[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      C t = tmp[i + f * nK];
+      Sn[f] = mk<C>(t.x + c6 * N[f].x, t.y + c6 * N[f].y);
+    }
+    project3(Sn, kx, ky, kz, k2, k0);
+    if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
+    C* So = static_cast<C*>(a.Sout);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) So[i + f * nK] = Sn[f];
+    if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
+  } else {
+    const T sig = freq_lin<T>(q, k2, k0);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) rk_update<C, T>(mode, a, i + f * nK, N[f], sig);
+  }
+}
+
+// ns2d epilogue at one mode (no projection).
+template <typename C, typename T>
+__device__ __forceinline__ void stage_epilogue1(int mode, const RKArgs& a, int64_t i,
+                                                C N, T k2, bool k0, bool rm,
+                                                const Phys& q) {
+  if (rm) N = mk<C>(0, 0);
+  if (mode == kTend) {
+    static_cast<C*>(a.tend)[i] = N;
+  } else if (mode == kRK3) {
+    const C t = static_cast<const C*>(a.tmp)[i];
+    const T c6 = T(a.dt) / T(6);
+    C Sn = mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
+    if (rm) Sn = mk<C>(0, 0);
+    static_cast<C*>(a.Sout)[i] = Sn;
+    if (isnan(Sn.x) || isnan(Sn.y)) atomicOr(a.nan_flag, 1);
+  } else {
+    rk_update<C, T>(mode, a, i, N, freq_lin<T>(q, k2, k0));
+  }
+}
+
+// Block-wide max of three non-negative values, folded into dst[0..2] (the
+// bit patterns of non-negative doubles order like the values).  Every
+// thread of the block must call it.
+template <typename T>
+__device__ __forceinline__ void block_max3(T a, T b, T c, unsigned long long* dst) {
+  __shared__ double red[3][32];
+  double v[3] = {(double)a, (double)b, (double)c};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o; o >>= 1) v[k] = fmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if (lane == 0) red[k][w] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double x = lane < nw ? red[k][lane] : 0.0;
+      for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+      if (lane == 0) atomicMax(dst + k, (unsigned long long)__double_as_longlong(x));
+    }
+  }
+}
+
+}  // namespace gbs

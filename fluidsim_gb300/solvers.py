@@ -112,6 +112,9 @@ class TimeSteppingPseudoSpectral:
         self.deltat = pts.deltat0
         self.deltat_max = pts.deltat_max
         self._nan_check = True
+        # state_spect._version right after our last step: while it is
+        # unchanged the state is the dealiased output of that step
+        self._dealiased_version = None
 
         def handler(signum, stack):
             self._stop_signal_received = signum
@@ -158,10 +161,15 @@ class TimeSteppingPseudoSpectral:
         pts = self.params.time_stepping
         dt = ctypes.c_double(self.deltat)
         cfl = (ctypes.c_double * 2)(self.CFL, self.deltat_max) if pts.USE_CFL else None
+        S = self.sim.state.state_spect
+        flags = _lib.GBS_STEP_CHECK_NAN if self._nan_check else 0
+        if self._dealiased_version is not None and S._version == self._dealiased_version:
+            flags |= _lib.GBS_STEP_DEALIASED
         rc = self.sim._lib.gbs_ns_step_rk4(
-            self.sim._solver, ctypes.c_void_p(self.sim.state.state_spect.data_ptr()),
-            ctypes.byref(dt), cfl, int(self._nan_check), current_stream_handle())
+            self.sim._solver, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt), cfl,
+            flags, current_stream_handle())
         self.deltat = dt.value
+        self._dealiased_version = S._version
         self.sim.state._phys = None
         if rc == _lib.GBS_ENAN:
             raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")

@@ -108,6 +108,12 @@ int gbs_ns_destroy(gbs_ns* solver);
 int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
                       void* stream);
 
+/* flags of gbs_ns_step_rk4 */
+#define GBS_STEP_CHECK_NAN 1 /* check state_spect[0] for NaN (synchronises)  */
+#define GBS_STEP_DEALIASED 2 /* state_spect is zero at every mode removed by
+                                the truncation (true after any completed
+                                step): lets the passes skip those modes     */
+
 /* One RK4 step with exact integrating factor, followed by projection
  * (ns3d), dealiasing and the NaN check: TimeSteppingPseudoSpectral
  * ._time_step_RK4 (fluidsim/base/time_stepping/pseudo_spect.py:798-984) +
@@ -117,11 +123,12 @@ int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
  * fluidsim/base/time_stepping/base.py:320-354 is applied first (from the
  * velocity of the current state, which the step computes anyway) and *dt is
  * updated: cfl[0] = CFL coefficient, cfl[1] = deltat_max.  That path
- * synchronises the stream once.  Returns GBS_ENAN (after completing the
- * step) when state_spect[0] holds a NaN; the NaN check synchronises the
- * stream unless check_nan = 0. */
+ * synchronises the stream once.  With GBS_STEP_CHECK_NAN, returns GBS_ENAN
+ * (after completing the step) when state_spect[0] holds a NaN.  With
+ * GBS_STEP_DEALIASED the caller asserts that the state is dealiased; the
+ * result is the same, the transforms skip the modes the 2/3 rule zeroes. */
 int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
-                    const double* cfl, int check_nan, void* stream);
+                    const double* cfl, int flags, void* stream);
 
 /* max |u_i| over the physical grid of state_spect (ns2d: ux, uy; ns3d: vx,
  * vy, vz) into out[ndim] (host).  Synchronises the stream. */

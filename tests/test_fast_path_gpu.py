@@ -1,0 +1,117 @@
+"""Compile-time-size kernels (power-of-two grids) against the oracle.
+
+The golden fixtures mostly use odd or small grids (generic kernels); these
+cases use sizes served by the fast path.  Step 1 runs unpruned (the state was
+set from outside), later steps run pruned (state known to be dealiased), so
+both variants are compared with the float64 oracle run live.
+"""
+from math import pi
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return max(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i]) for i in range(len(b)))
+
+
+def run_3d(shape, precision, steps, **kw):
+    import torch
+    from fluidsim_gb300.init_fields import isotropic_3d
+    from fluidsim_gb300.solvers import SimulNS3D
+    from oracle.solvers import NS3DOracle
+    from oracle.spectral import OperNumpy3D
+    nz, ny, nx = shape
+    L = (2 * pi, 2 * pi * ny / nx, 2 * pi * nz / nx)
+    p = SimulNS3D.create_default_params()
+    p.precision = precision
+    p.oper.nx, p.oper.ny, p.oper.nz = nx, ny, nz
+    p.oper.Lx, p.oper.Ly, p.oper.Lz = L
+    p.nu_2 = kw.get("nu_2", 2e-3)
+    p.nu_4 = kw.get("nu_4", 0.0)
+    p.nu_m4 = kw.get("nu_m4", 0.0)
+    p.f = kw.get("f")
+    ts = p.time_stepping
+    ts.USE_CFL = kw.get("USE_CFL", False)
+    ts.cfl_coef = kw.get("cfl_coef")
+    ts.deltat0 = kw.get("dt", 5e-3)
+    ts.USE_T_END = False
+    ts.it_end = steps
+    sim = SimulNS3D(p)
+    v0 = isotropic_3d(nx, ny, nz, *L, seed=11)
+    sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2])
+    sim.time_stepping.start()
+    orc = NS3DOracle(OperNumpy3D(nx, ny, nz, *L), f=kw.get("f"), nu_2=p.nu_2,
+                     nu_4=p.nu_4, nu_m4=p.nu_m4, USE_CFL=ts.USE_CFL,
+                     cfl_coef=ts.cfl_coef, deltat0=ts.deltat0)
+    orc.state_spect[:] = v0
+    orc.statephys_from_statespect()
+    orc.run(it_end=steps)
+    return sim, orc
+
+
+@pytest.mark.parametrize("shape,kw", [
+    ((64, 64, 64), {}),
+    ((32, 64, 128), {"USE_CFL": True, "cfl_coef": 0.5, "f": 0.7}),
+    ((64, 32, 64), {"nu_4": 1e-6, "nu_m4": 1e-3}),
+])
+def test_ns3d_fast_fp64_matches_oracle(cuda, shape, kw):
+    sim, orc = run_3d(shape, "float64", 4, **kw)
+    got = sim.state.state_spect.cpu().numpy()
+    assert rel(got, orc.state_spect) < 1e-12
+    assert abs(sim.time_stepping.deltat - orc.deltat) <= 1e-12 * orc.deltat
+    # pruned steps keep the state dealiased
+    assert np.abs(got[:, orc.oper.where_dealiased.astype(bool)]).max() == 0
+
+
+def test_ns3d_fast_fp32_error(cuda):
+    sim, orc = run_3d((64, 64, 64), "float32", 6)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
+
+
+def test_ns3d_fast_tendency_matches_oracle(cuda):
+    import torch
+    from fluidsim_gb300.init_fields import isotropic_3d
+    from fluidsim_gb300.solvers import SimulNS3D
+    from oracle.solvers import NS3DOracle
+    from oracle.spectral import OperNumpy3D
+    n = 64
+    p = SimulNS3D.create_default_params()
+    p.oper.nx = p.oper.ny = p.oper.nz = n
+    sim = SimulNS3D(p)
+    v0 = isotropic_3d(n, n, n, seed=5, coef_dealiasing=1.0)  # not dealiased
+    S = torch.from_numpy(v0).cuda()
+    tend = sim.tendencies_nonlin(S).cpu().numpy()
+    orc = NS3DOracle(OperNumpy3D(n, n, n))
+    ref = orc.tendencies_nonlin(v0.copy())
+    assert rel(tend, ref) < 1e-12
+
+
+@pytest.mark.parametrize("shape,beta,cfl", [((128, 128), 0.0, False), ((64, 256), 2.0, True),
+                                            ((512, 512), 0.0, False)])
+def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl):
+    from fluidsim_gb300.init_fields import noise_rot_2d
+    from fluidsim_gb300.solvers import SimulNS2D
+    from oracle.solvers import NS2DOracle
+    from oracle.spectral import OperNumpy2D
+    ny, nx = shape
+    L = (2 * pi, 2 * pi * ny / nx)
+    p = SimulNS2D.create_default_params()
+    p.oper.nx, p.oper.ny = nx, ny
+    p.oper.Lx, p.oper.Ly = L
+    p.nu_2, p.nu_8, p.beta = 1e-3, 1e-14, beta
+    ts = p.time_stepping
+    ts.USE_CFL, ts.cfl_coef, ts.deltat0 = cfl, 0.5, 2e-3
+    ts.USE_T_END, ts.it_end = False, 5
+    sim = SimulNS2D(p)
+    rot = noise_rot_2d(nx, ny, *L, kmin=3, kmax=10, seed=4)
+    sim.init_from_rotfft(rot)
+    sim.time_stepping.start()
+    orc = NS2DOracle(OperNumpy2D(nx, ny, *L), beta=beta, nu_2=1e-3, nu_8=1e-14,
+                     USE_CFL=cfl, cfl_coef=0.5, deltat0=2e-3)
+    orc.init_from_rotfft(rot)
+    orc.run(it_end=5)
+    assert rel(sim.state.state_spect.cpu().numpy(), orc.state_spect) < 1e-12
