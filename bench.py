@@ -35,10 +35,26 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "ns3d 512^3 RK4 steps/s"
 KINDS = ("inv_z_curl", "inv_y", "x_product", "fwd_y", "fwd_z_rk")
-# algorithmic HBM traffic per launch, in units of one spectral field
-# (nz*ny*(nx/2+1) complex): reads + writes of the fused passes
-FIELDS_PER_LAUNCH = {"inv_z_curl": 9, "inv_y": 12, "x_product": 9, "fwd_y": 6,
-                     "fwd_z_rk": (12 + 15 + 15 + 9) / 4}
+
+
+def fields_per_launch(nx, ny, nz, coef=2.0 / 3):
+    """Algorithmic HBM traffic per launch of each pass of a pruned step, in
+    units of one spectral field (nz*ny*(nx/2+1) complex): what the pass must
+    read and write given the 2/3 truncation (kept fractions fx, fy, fz)."""
+    from fluidsim_gb300.init_fields import cubic_dealias_cutoff
+    nkx = nx // 2 + 1
+    fx = min(cubic_dealias_cutoff(nx, 2 * pi, coef), nkx) / nkx
+    cy = cubic_dealias_cutoff(ny, 2 * pi, coef)
+    cz = cubic_dealias_cutoff(nz, 2 * pi, coef)
+    fy = min(2 * cy - 1, ny) / ny
+    fz = min(2 * cz - 1, nz) / nz
+    # stage average of the RK state traffic: reads+writes of S, tmp, tmp1
+    rk_state = ((3 + 6) + (6 + 6) + (6 + 6) + (3 + 3)) / 4
+    return {"inv_z_curl": 3 * fx * fy * fz + 6 * fx * fy,
+            "inv_y": 6 * fx * fy + 6 * fx,
+            "x_product": 6 * fx + 3 * fx,
+            "fwd_y": 3 * fx + 3 * fx * fy,
+            "fwd_z_rk": 3 * fx * fy + rk_state * fx * fy * fz}
 
 
 def parse():
@@ -48,6 +64,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--ny", type=int, default=None, help="override ny (profiling cases)")
+    ap.add_argument("--nz", type=int, default=None, help="override nz (profiling cases)")
+    ap.add_argument("--no-fft", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -58,9 +77,11 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def initial_state(n):
+def initial_state(n, ny=None, nz=None):
     from fluidsim_gb300.init_fields import isotropic_3d
-    return isotropic_3d(n, n, n, k0=4.0, energy=0.5, seed=0)
+    ny, nz = ny or n, nz or n
+    return isotropic_3d(n, ny, nz, 2 * pi, 2 * pi * ny / n, 2 * pi * nz / n,
+                        k0=4.0, energy=0.5, seed=0)
 
 
 def cfl_dt(vmax, n, cfl=0.5, dtmax=0.2):
@@ -75,7 +96,9 @@ def make_sim(n, precision, v0):
     from fluidsim_gb300.solvers import SimulNS3D
     p = SimulNS3D.create_default_params()
     p.precision = precision
-    p.oper.nx = p.oper.ny = p.oper.nz = n
+    nz, ny = v0.shape[1], v0.shape[2]
+    p.oper.nx, p.oper.ny, p.oper.nz = n, ny, nz
+    p.oper.Ly, p.oper.Lz = 2 * pi * ny / n, 2 * pi * nz / n
     p.nu_2 = 5e-4
     p.time_stepping.USE_CFL = False
     p.time_stepping.USE_T_END = False
@@ -198,6 +221,53 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def fft_throughput(n, reps=20):
+    """FP32 512^3 R2C + C2R through the plugin class (HBM GB/s), cuFFT beside it."""
+    import torch
+    from fluidsim_gb300 import FFT3DGB300
+    op = FFT3DGB300(n, n, n, precision="float32")
+    x = torch.randn((n, n, n), dtype=torch.float32, device="cuda")
+    k = op.create_arrayK()
+    x2 = torch.empty_like(x)
+    for _ in range(3):
+        op.fft_as_arg(x, k)
+        op.ifft_as_arg(k, x2)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        op.fft_as_arg(x, k)
+    ev[1].record()
+    for _ in range(reps):
+        op.ifft_as_arg(k, x2)
+    ev[2].record()
+    torch.cuda.synchronize()
+    r2c_ms = ev[0].elapsed_time(ev[1]) / reps
+    c2r_ms = ev[1].elapsed_time(ev[2]) / reps
+    sr = x.numel() * 4
+    sk = k.numel() * 8
+    # x pass reads S_r writes S_k; y and z passes read and write S_k
+    alg = sr + 5 * sk
+    out = {"r2c_ms": r2c_ms, "c2r_ms": c2r_ms,
+           "r2c_hbm_gbs": alg / r2c_ms / 1e6, "c2r_hbm_gbs": alg / c2r_ms / 1e6,
+           "alg_bytes_per_transform": alg}
+    # comparison only: cuFFT through torch (not part of the product)
+    for _ in range(3):
+        torch.fft.rfftn(x)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        torch.fft.rfftn(x)
+    ev[1].record()
+    for _ in range(reps):
+        torch.fft.irfftn(k, s=x.shape)
+    ev[2].record()
+    torch.cuda.synchronize()
+    out["cufft_compare"] = {"rfftn_ms": ev[0].elapsed_time(ev[1]) / reps,
+                            "irfftn_ms": ev[1].elapsed_time(ev[2]) / reps}
+    return out
+
+
 def rel_l2(a, b):
     return max(float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(len(b)))
 
@@ -216,7 +286,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     n = args.n
-    v0 = initial_state(n)
+    v0 = initial_state(n, args.ny, args.nz)
     sim = make_sim(n, "float32", v0)
     dt = cfl_dt(sim.max_velocity(), n)
     sim.time_stepping.deltat = dt
@@ -254,16 +324,19 @@ def main():
     steps_per_s = world * args.steps / (elapsed_ms / 1000.0)
 
     # roofline of the dominant kernel (largest share of the timed region)
-    field_bytes = n * n * (n // 2 + 1) * 8  # complex64
+    field_bytes = v0.shape[1] * v0.shape[2] * (n // 2 + 1) * 8  # complex64
     kinds = {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(KINDS)}
     dom = max(kinds, key=lambda k: kinds[k]["ms"])
     avg_s = kinds[dom]["ms"] / max(kinds[dom]["launches"], 1) / 1000.0
-    alg_bytes = FIELDS_PER_LAUNCH[dom] * field_bytes
+    fpl = fields_per_launch(n, v0.shape[2], v0.shape[1])
+    alg_bytes = fpl[dom] * field_bytes
     peak, peak_src = measured_peak()
     achieved = alg_bytes / avg_s / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
                 "traffic": ncu_traffic(dom, n), "alg_bytes_per_launch": alg_bytes,
+                "kernel_gbs": {k: fpl[k] * field_bytes / (v["ms"] / max(v["launches"], 1)) / 1e6
+                               for k, v in kinds.items() if v["ms"] > 0},
                 "kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in kinds.items()},
                 "kernel_share": {k: v["ms"] / sum(x["ms"] for x in kinds.values())
                                  for k, v in kinds.items()}}
@@ -302,6 +375,9 @@ def main():
                     "d2h_bytes_per_step": state_bytes,
                     "note": "state copied host->device and back around every step"},
             "clocks": clocks.summary()}
+
+    if not args.no_fft and args.ny is None and args.nz is None:
+        line["fft"] = fft_throughput(n)
 
     if not args.no_fp64:
         sim32 = make_sim(n, "float32", v0)

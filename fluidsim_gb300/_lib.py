@@ -27,7 +27,7 @@ EXPORTED = (
     "gbs_ns_destroy", "gbs_ns_tendencies", "gbs_ns_step_rk4",
     "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
     "gbs_ns_spectrum_size", "gbs_ns_spectrum", "gbs_ns_timing",
-    "gbs_ns_timing_report", "gbs_fft_c2r_noalloc",
+    "gbs_ns_timing_report", "gbs_fft_c2r_noalloc", "gbs_ns_set_turb_model",
 )
 
 
@@ -46,6 +46,13 @@ class NSParams(ctypes.Structure):
         ("kcut_z", ctypes.c_int64),
         ("dtype", ctypes.c_int),
     ]
+
+
+class MLPWeights(ctypes.Structure):
+    """Mirror of ``gbs_mlp_weights`` (device pointers)."""
+
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("W1", "W2", "W3", "b1", "b2", "b3", "in_scale", "out_scale")]
 
 
 _lock = threading.Lock()
@@ -77,6 +84,8 @@ def _declare(lib):
         "gbs_ns_timing_report": (ctypes.c_int, [P, DP, I64P, ctypes.c_int, I64P]),
         "gbs_fft_c2r_noalloc": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.c_int,
                                                ctypes.c_int, P, P, P]),
+        "gbs_ns_set_turb_model": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.POINTER(MLPWeights)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

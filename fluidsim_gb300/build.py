@@ -17,7 +17,8 @@ CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libgbspec.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gbs_fft.cu", "gbs_ns.cu", "gbs_noalloc.cu", "gbs_fast_f32.cu", "gbs_fast_f64.cu"]
+SOURCES = ["gbs_fft.cu", "gbs_ns.cu", "gbs_noalloc.cu", "gbs_fast_f32.cu", "gbs_fast_f64.cu",
+           "gbs_turb.cu"]
 
 
 def nvcc_path():

@@ -39,6 +39,18 @@ struct Line {
   }
 };
 
+// Shared-memory swizzle: XOR the element index inside each 128-byte bank
+// sweep (E = 128 / sizeof(C) elements) with the index of the sweep, so the
+// strided Stockham writes, the unit-stride reads and the column-tile
+// accesses all spread over the 32 banks.  A permutation inside every
+// E-aligned group, so any E-aligned slot keeps its extent.
+template <typename C>
+__device__ __forceinline__ int swz(int q) {
+  constexpr int E = 128 / sizeof(C);
+  constexpr int LG = E == 16 ? 4 : 3;
+  return q ^ ((q >> LG) & (E - 1));
+}
+
 __device__ __forceinline__ bool kept(int p, int n, int kc) {
   return p < kc || p > n - kc;
 }
@@ -122,7 +134,7 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
     const int p = jt + r * P::N8;
     v[r] = (valid && kept(p, P::N, a.kc_in)) ? in[base + p * a.es] : mk<C>(0, 0);
   }
-  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
   run<DIR, LOGN>(v, jt, true, acc, tw, 1);
   if (!valid) return;
 #pragma unroll
@@ -132,10 +144,9 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
   }
 }
 
-// Row slots in shared memory hold M + M/8 complex: one pad element every 8
-// spreads the radix-8 stage writes (stride 8) over the banks.
-template <int LOGM>
-__device__ __forceinline__ int padp(int p) { return p + (p >> 3); }
+// Row slots in shared memory hold M complex, addressed through swz().
+template <int LOGM, typename C>
+__device__ __forceinline__ int padp(int p) { return swz<C>(p); }
 
 // ------------------------------------------------------- plain row passes
 // nrows rows of nx = 2M reals <-> nx/2+1 complex.  L rows per CTA, M/8
@@ -146,7 +157,7 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
            const cplx<T>* __restrict__ twx, T scale) {
   using C = cplx<T>;
   using P = Line<LOGM>;
-  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8, NKX = M + 1;
+  constexpr int M = P::N, M8 = P::N8, LS = M, NKX = M + 1;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int jt = threadIdx.x % M8, l = threadIdx.x / M8;
   const int64_t row = (int64_t)blockIdx.x * L + l;
@@ -156,7 +167,7 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = valid ? xc[jt + r * M8] : mk<C>(0, 0);
   C* slot = buf + l * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   run<-1, LOGM>(v, jt, true, acc, twx, 2);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
@@ -167,8 +178,8 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
     const int64_t rr = (int64_t)blockIdx.x * L + ll;
     if (rr >= nrows) continue;
     const C* sl = buf + ll * LS;
-    C a = sl[padp<LOGM>(k == M ? 0 : k)];
-    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
+    C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
+    C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
     const C s = cadd(a, b), d = csub(a, b);
     const C wd = cmul(twx[k], d);
     out[rr * NKX + k] = cscale(mk<C>(h * (s.x + wd.y), h * (s.y - wd.x)), scale);
@@ -181,7 +192,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
            const cplx<T>* __restrict__ twx) {
   using C = cplx<T>;
   using P = Line<LOGM>;
-  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8, NKX = M + 1;
+  constexpr int M = P::N, M8 = P::N8, LS = M, NKX = M + 1;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int jt = threadIdx.x % M8, l = threadIdx.x / M8;
   const int64_t row = (int64_t)blockIdx.x * L + l;
@@ -203,7 +214,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
     v[r] = Z;
   }
   C* slot = buf + l * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   run<+1, LOGM>(v, jt, true, acc, twx, 2);
   if (!valid) return;
   C* xc = reinterpret_cast<C*>(x) + row * M;
@@ -253,7 +264,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const int64_t nK = plane * g.nz;
   const int64_t base = (int64_t)iy * g.nkx + ix;
   const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
-  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
 #pragma unroll 1
   for (int f = 0; f < 6; ++f) {
     C v[8];
@@ -299,7 +310,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
   using C = cplx<T>;
   using P = Line<LOGM>;
-  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8;
+  constexpr int M = P::N, M8 = P::N8, LS = M;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int jt = threadIdx.x % M8;
   const int l = (threadIdx.x / M8) % L;
@@ -309,7 +320,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int64_t row = (int64_t)blockIdx.x * L + l;
   const bool valid = row < nrows;
   C* slot = buf + (f * L + l) * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
   {
@@ -337,7 +348,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   T mx = 0, my = 0, mz = 0;
   for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
     const int ll = idx / M, j = idx % M;
-    C* p0 = buf + ll * LS + padp<LOGM>(j);
+    C* p0 = buf + ll * LS + padp<LOGM, C>(j);
     const C vx = p0[0], vy = p0[L * LS], vz = p0[2 * L * LS];
     const C ox = p0[3 * L * LS], oy = p0[4 * L * LS], oz = p0[5 * L * LS];
     p0[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
@@ -361,19 +372,20 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
   __syncthreads();
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
-  for (int idx = threadIdx.x; idx < 3 * L * nout; idx += blockDim.x) {
-    const int k = idx % nout;
-    const int fl = idx / nout;  // field * L + row
-    const int ff = fl / L, ll = fl % L;
-    const int64_t rr = (int64_t)blockIdx.x * L + ll;
-    if (rr >= nrows) continue;
-    const C* sl = buf + fl * LS;
-    C a = sl[padp<LOGM>(k == M ? 0 : k)];
-    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
-    const C s = cadd(a, b), d = csub(a, b);
-    const C wd = cmul(twx[k], d);
+  if (act && valid) {
+    const C* sl = buf + (f * L + l) * LS;
+    C* Fo = F + f * nK + row * g.nkx;
     const T h = T(0.5);
-    F[ff * nK + rr * g.nkx + k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+#pragma unroll
+    for (int r = 0; r <= 8; ++r) {
+      const int k = r < 8 ? jt + r * M8 : M;
+      if ((r == 8 && jt != 0) || k >= nout) continue;
+      C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
+      C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
+      const C s = cadd(a, b), d = csub(a, b);
+      const C wd = cmul(twx[k], d);
+      Fo[k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+    }
   }
 }
 
@@ -400,7 +412,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
     for (int r = 0; r < 8; ++r)
       v[r] = valid ? F[f * nK + base + (jt + r * N8) * plane] : mk<C>(0, 0);
     C* slot = buf + f * N * TX;
-    auto acc = [&](int p) -> C& { return slot[p * TX + c]; };
+    auto acc = [&](int p) -> C& { return slot[swz<C>(p * TX + c)]; };
     run<-1, LOGN>(v, jt, true, acc, twz, 1);
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = v[i];
@@ -421,7 +433,11 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
     const T kz = T(g.dkz * kzi);
     C N3[3];
 #pragma unroll
-    for (int ff = 0; ff < 3; ++ff) N3[ff] = cscale(buf[ff * N * TX + iz * TX + c], inv_n);
+    for (int ff = 0; ff < 3; ++ff) N3[ff] = cscale(buf[ff * N * TX + swz<C>(iz * TX + c)], inv_n);
+    if (a.add) {
+#pragma unroll
+      for (int ff = 0; ff < 3; ++ff) N3[ff] = cadd(N3[ff], static_cast<const C*>(a.add)[i + ff * nK]);
+    }
     const T k2 = kx * kx + ky * ky + kz * kz;
     const bool k0 = (ix == 0 && kyi == 0 && kzi == 0);
     stage_epilogue3<C, T>(mode, a, i, nK, N3, kx, ky, kz, k2, k0, rm, q);
@@ -442,7 +458,7 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const bool valid = ix < g.ncx;
   const int64_t nK = (int64_t)g.ny * g.nkx;
   const T kx = T(g.dkx * ix);
-  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
 #pragma unroll 1
   for (int f = 0; f < 4; ++f) {
     C v[8];
@@ -482,7 +498,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
   using C = cplx<T>;
   using P = Line<LOGM>;
-  constexpr int M = P::N, M8 = P::N8, LS = M + M / 8;
+  constexpr int M = P::N, M8 = P::N8, LS = M;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int jt = threadIdx.x % M8;
   const int l = (threadIdx.x / M8) % L;
@@ -492,7 +508,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int64_t row = (int64_t)blockIdx.x * L + l;
   const bool valid = row < nrows;
   C* slot = buf + (f * L + l) * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM>(p)]; };
+  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
   {
@@ -520,7 +536,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const T beta = T(g.beta);
   for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
     const int ll = idx / M, j = idx % M;
-    C* p0 = buf + ll * LS + padp<LOGM>(j);
+    C* p0 = buf + ll * LS + padp<LOGM, C>(j);
     const C ux = p0[0], uy = p0[L * LS], px = p0[2 * L * LS], py = p0[3 * L * LS];
     C res;
     if (g.beta == 0)
@@ -550,8 +566,8 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
     const int64_t rr = (int64_t)blockIdx.x * L + ll;
     if (rr >= nrows) continue;
     const C* sl = buf + ll * LS;
-    C a = sl[padp<LOGM>(k == M ? 0 : k)];
-    C b = cconj(sl[padp<LOGM>(k == 0 ? 0 : M - k)]);
+    C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
+    C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
     const C s = cadd(a, b), d = csub(a, b);
     const C wd = cmul(twx[k], d);
     const T h = T(0.5);
@@ -574,7 +590,7 @@ kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
 #pragma unroll
   for (int r = 0; r < 8; ++r)
     v[r] = valid ? F[(int64_t)(jt + r * P::N8) * g.nkx + ix] : mk<C>(0, 0);
-  auto acc = [&](int p) -> C& { return buf[p * TX + c]; };
+  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
   run<-1, LOGN>(v, jt, true, acc, twy, 1);
   if (!valid) return;
   const T kx = T(g.dkx * ix);

@@ -76,7 +76,7 @@ static int r2c_launch(const void* x, void* k, int64_t nrows, const void* tw, dou
   constexpr int M = 1 << LOGM;
   constexpr int L = (sizeof(T) == 4 ? 256 : 128) / (M / 8) > 0 ? (sizeof(T) == 4 ? 256 : 128) / (M / 8) : 1;
   constexpr int TH = L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)L * (M + M / 8);
+  const size_t smem = sizeof(C) * (size_t)L * M;
   int rc = prep(kf_row_r2c<T, LOGM, L>, smem);
   if (rc) return rc;
   kf_row_r2c<T, LOGM, L><<<ceil_div(nrows, L), TH, smem, st>>>(
@@ -98,7 +98,7 @@ static int c2r_launch(const void* k, void* x, int64_t nrows, const void* tw, cud
   constexpr int M = 1 << LOGM;
   constexpr int L = (sizeof(T) == 4 ? 256 : 128) / (M / 8) > 0 ? (sizeof(T) == 4 ? 256 : 128) / (M / 8) : 1;
   constexpr int TH = L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)L * (M + M / 8);
+  const size_t smem = sizeof(C) * (size_t)L * M;
   int rc = prep(kf_row_c2r<T, LOGM, L>, smem);
   if (rc) return rc;
   kf_row_c2r<T, LOGM, L><<<ceil_div(nrows, L), TH, smem, st>>>(
@@ -142,7 +142,7 @@ static int B3_launch(const Geo& g, const void* W, void* F, const void* tw,
   constexpr int L = rows_x<T, LOGM, 6>();
   constexpr int M = 1 << LOGM;
   constexpr int TH = 6 * L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)6 * L * (M + M / 8);
+  const size_t smem = sizeof(C) * (size_t)6 * L * M;
   int rc = prep(kf3_x<T, LOGM, L>, smem);
   if (rc) return rc;
   kf3_x<T, LOGM, L><<<ceil_div((int64_t)g.nz * g.ny, L), TH, smem, st>>>(
@@ -208,7 +208,7 @@ static int B2_launch(const Geo& g, const void* W, void* F, const void* tw,
   constexpr int L = rows_x<T, LOGM, 4>();
   constexpr int M = 1 << LOGM;
   constexpr int TH = 4 * L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)4 * L * (M + M / 8);
+  const size_t smem = sizeof(C) * (size_t)4 * L * M;
   int rc = prep(kf2_x<T, LOGM, L>, smem);
   if (rc) return rc;
   kf2_x<T, LOGM, L><<<ceil_div(g.ny, L), TH, smem, st>>>(

@@ -20,6 +20,7 @@
 #include "gbs_ns.cuh"
 #include "gbs_fast.cuh"
 #include "gbs_fast_api.h"
+#include "gbs_turb.h"
 
 namespace gbs {
 
@@ -218,6 +219,10 @@ k3_fwd_z_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
     C N[3];
 #pragma unroll
     for (int f = 0; f < 3; ++f) N[f] = cscale(buf[iz * LP + f * TX + c], inv_n);
+    if (a.add) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f) N[f] = cadd(N[f], static_cast<const C*>(a.add)[i + f * nK]);
+    }
     // project_perpk3d: N -= k (k.N)/|k|^2 ; k = 0 untouched
     if (!k0) {
       const T inv = T(1) / k2;
@@ -427,6 +432,9 @@ struct Solver {
   double t_ms[kKinds];
   long long t_count[kKinds];
   long long launches;
+  // turbulence model (ns3d): forcing buffer and its pipeline
+  TurbCtx turb;
+  void* turbF;
   // compile-time-size path (all axes powers of two in range)
   int use_fast;
   fast::Geo geo;
@@ -676,11 +684,24 @@ static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st,
   return GBS_OK;
 }
 
+// turbulence-model forcing of the stage input `in` (null when disabled)
+template <typename T>
+static int turb_stage(Solver* s, const void* in, RKArgs& a, cudaStream_t st) {
+  a.add = nullptr;
+  if (s->turb.type == kTurbNone) return GBS_OK;
+  int rc = turb_forcing<T>(s->turb, in, s->turbF, st);
+  if (rc) return rc;
+  a.add = s->turbF;
+  return GBS_OK;
+}
+
 template <typename T>
 static int tendencies(Solver* s, const void* S, void* tend, cudaStream_t st) {
   RKArgs a{};
   a.tend = tend;
   int rc = eval<T>(s, S, kTend, a, false, st);
+  if (rc) return rc;
+  rc = turb_stage<T>(s, S, a, st);
   if (rc) return rc;
   return finish<T>(s, kTend, a, st);
 }
@@ -724,10 +745,14 @@ static int step(Solver* s, void* S, double* dt, const double* cfl, int flags,
     *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
   }
   a.dt = *dt;
+  rc = turb_stage<T>(s, S, a, st);
+  if (rc) return rc;
   rc = finish<T>(s, kRK0, a, st, pr);
   if (rc) return rc;
   for (int m = kRK1; m <= kRK3; ++m) {
     rc = eval<T>(s, s->tmp1, m, a, false, st, pr);
+    if (rc) return rc;
+    rc = turb_stage<T>(s, s->tmp1, a, st);
     if (rc) return rc;
     rc = finish<T>(s, m, a, st, pr);
     if (rc) return rc;
@@ -895,7 +920,19 @@ struct gbs_ns {
   Solver s;
 };
 
+static void free_turb(Solver* s) {
+  gbs::TurbCtx& t = s->turb;
+  if (t.plan9) gbs_fft_plan_destroy(t.plan9);
+  if (t.plan6) gbs_fft_plan_destroy(t.plan6);
+  void* ptrs[] = {t.Gk, t.Gx, t.Tx, t.Tk, s->turbF};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  memset(&t, 0, sizeof(t));
+  s->turbF = nullptr;
+}
+
 static void free_solver(Solver* s) {
+  free_turb(s);
   if (s->timing >= 0 && s->ev[0][0]) {
     for (int i = 0; i < gbs::kMaxEv; ++i) {
       cudaEventDestroy(s->ev[i][0]);
@@ -1085,6 +1122,60 @@ int gbs_ns_spatial_means(gbs_ns* h, const void* S, double* out, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (h->s.p.dtype == GBS_F64) return gbs::spatial_means<double>(&h->s, S, out, st);
   return gbs::spatial_means<float>(&h->s, S, out, st);
+}
+
+int gbs_ns_set_turb_model(gbs_ns* h, int type, double C,
+                          const gbs_mlp_weights* w) {
+  gbs::clear_error();
+  if (!h || type < 0 || type > 2 || (type == 2 && !w)) {
+    gbs::set_error("gbs_ns_set_turb_model: invalid argument");
+    return GBS_EINVAL;
+  }
+  Solver* s = &h->s;
+  if (s->p.ndim != 3 && type != 0) {
+    gbs::set_error("gbs_ns_set_turb_model: turbulence models are for ns3d");
+    return GBS_EINVAL;
+  }
+  GBS_CUDA_TRY(cudaDeviceSynchronize());
+  free_turb(s);
+  if (type == 0) return GBS_OK;
+  gbs::TurbCtx& t = s->turb;
+  t.type = type;
+  t.nx = s->q.nx;
+  t.ny = s->q.ny;
+  t.nz = s->q.nz;
+  t.dkx = s->q.dkx;
+  t.dky = s->q.dky;
+  t.dkz = s->q.dkz;
+  t.C_nu_T = C * (s->p.Lx / s->p.nx) * (s->p.Lx / s->p.nx) * sqrt(2.0);
+  if (type == 2) {
+    t.w.W1 = static_cast<const __nv_bfloat16*>(w->W1);
+    t.w.W2 = static_cast<const __nv_bfloat16*>(w->W2);
+    t.w.W3 = static_cast<const __nv_bfloat16*>(w->W3);
+    t.w.b1 = w->b1;
+    t.w.b2 = w->b2;
+    t.w.b3 = w->b3;
+    t.w.in_scale = w->in_scale;
+    t.w.out_scale = w->out_scale;
+  }
+  const int64_t shape[3] = {s->p.nz, s->p.ny, s->p.nx};
+  int rc = gbs_fft_plan_create(3, shape, s->p.dtype, 9, &t.plan9);
+  if (!rc) rc = gbs_fft_plan_create(3, shape, s->p.dtype, 6, &t.plan6);
+  const size_t rs = s->p.dtype == GBS_F64 ? sizeof(double) : sizeof(float);
+  const size_t nX = (size_t)s->p.nx * s->p.ny * s->p.nz;
+  if (!rc && (cudaMalloc(&t.Gk, s->csize * s->nK * 9) != cudaSuccess ||
+              cudaMalloc(&t.Gx, rs * nX * 9) != cudaSuccess ||
+              cudaMalloc(&t.Tx, rs * nX * 6) != cudaSuccess ||
+              cudaMalloc(&t.Tk, s->csize * s->nK * 6) != cudaSuccess ||
+              cudaMalloc(&s->turbF, s->csize * s->nK * 3) != cudaSuccess)) {
+    gbs::set_error("gbs_ns_set_turb_model: device allocation failed");
+    rc = GBS_ENOMEM;
+  }
+  if (rc) {
+    free_turb(s);
+    return rc;
+  }
+  return GBS_OK;
 }
 
 int gbs_ns_timing(gbs_ns* h, int enable) {

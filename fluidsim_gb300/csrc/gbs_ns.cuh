@@ -19,6 +19,8 @@ struct RKArgs {
   void* tend;     // output for kTend
   double dt;
   int* nan_flag;
+  const void* add;  // optional forcing (nvar spectral fields) added to the
+                    // tendency before projection and dealiasing
 };
 
 // Viscosities for sigma(k) = f_d + f_d_hypo.

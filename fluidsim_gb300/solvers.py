@@ -355,11 +355,34 @@ class SimulNS3D(_SimulBase):
     @staticmethod
     def _complete_params_with_default(params):
         params._set_attribs({"f": None, "no_vz_kz0": False, "projection": None})
+        # fluidsim/base/turb_model/base.py:36-70 (+ smagorinsky.py:46-47)
+        tm = params._set_child("turb_model", attribs={"enable": False, "type": ""})
+        tm._set_child("smagorinsky", attribs={"C": 0.18})
 
     def __init__(self, params):
         if params.no_vz_kz0 or params.projection is not None:
             raise NotImplementedError("no_vz_kz0 / toroidal / poloidal projections")
         super().__init__(params)
+        self.is_turb_model_enabled = False
+        self._closure = None
+        tm = params.turb_model
+        if tm.enable:
+            if tm.type == "smagorinsky":
+                _lib.check(self._lib.gbs_ns_set_turb_model(
+                    self._solver, 1, float(tm.smagorinsky.C), None), "turb_model")
+                self.is_turb_model_enabled = True
+            elif tm.type != "mlp_closure":
+                raise ValueError(
+                    f"Wrong value ('{tm.type}') of params.turb_model.type. "
+                    "It should be in ('smagorinsky', 'mlp_closure')")
+
+    def set_closure(self, closure):
+        """Use a trained ``fluidsim_gb300.closure.ClosureMLP`` as turb model."""
+        self._closure = closure  # keeps the device weights alive
+        w = closure.c_weights()
+        _lib.check(self._lib.gbs_ns_set_turb_model(self._solver, 2, 0.0, ctypes.byref(w)),
+                   "turb_model")
+        self.is_turb_model_enabled = True
 
     def _ns_params(self):
         p = super()._ns_params()

@@ -130,6 +130,30 @@ int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
 int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
                     const double* cfl, int flags, void* stream);
 
+/* Turbulence model added to the ns3d tendencies before projection and
+ * dealiasing, in every stage (fluidsim/solvers/ns3d/solver.py:246-249,
+ * TurbModel.get_forcing fluidsim/base/turb_model/base.py:87-88).
+ *   type 0: none;
+ *   type 1: Smagorinsky with constant C (turb_model/smagorinsky.py:56-110,
+ *           Delta = Lx / nx);
+ *   type 2: learned closure, tau_ij = MLP(d_j u_i) (9 -> 64 -> 64 -> 6, tanh,
+ *           BF16 weights, FP32 accumulation), forcing -d_j tau_ij.
+ * The weights are device pointers owned by the caller, read at every step.
+ * Allocates the model's work buffers (synchronises the device). */
+typedef struct gbs_mlp_weights {
+  const void* W1;  /* bf16 [64][9]  */
+  const void* W2;  /* bf16 [64][64] */
+  const void* W3;  /* bf16 [6][64]  */
+  const float* b1; /* [64] */
+  const float* b2; /* [64] */
+  const float* b3; /* [6]  */
+  const float* in_scale;  /* [9]: network input = d_j u_i * in_scale   */
+  const float* out_scale; /* [6]: tau = network output * out_scale     */
+} gbs_mlp_weights;
+
+int gbs_ns_set_turb_model(gbs_ns* solver, int type, double C,
+                          const gbs_mlp_weights* weights);
+
 /* max |u_i| over the physical grid of state_spect (ns2d: ux, uy; ns3d: vx,
  * vy, vz) into out[ndim] (host).  Synchronises the stream. */
 int gbs_ns_max_velocity(gbs_ns* solver, const void* state_spect, double* out,

@@ -223,6 +223,23 @@ def load_reference(root):
                               fs / "solvers" / "ns3d" / "state.py")
     m["ns3d_ts"] = _module("fluidsim.solvers.ns3d.time_stepping",
                            fs / "solvers" / "ns3d" / "time_stepping.py")
+
+    # turbulence model: the reference's Smagorinsky + stress tensor, with the
+    # SimulExtender plumbing of turb_model/base.py replaced by a stand-in
+    _module("fluidsim.base.turb_model", package=True)
+    tb = _module("fluidsim.base.turb_model.base")
+
+    class SpecificTurbModelSpectral:
+        def __init__(self, sim):
+            self.sim = sim
+            self.forcing_fft = SetOfVariables(like=sim.state.state_spect,
+                                              info="forcing_fft", value=0.0)
+
+    tb.SpecificTurbModelSpectral = SpecificTurbModelSpectral
+    m["stress_tensor"] = _module("fluidsim.base.turb_model.stress_tensor",
+                                 fs / "base" / "turb_model" / "stress_tensor.py")
+    m["smagorinsky"] = _module("fluidsim.base.turb_model.smagorinsky",
+                               fs / "base" / "turb_model" / "smagorinsky.py")
     return m
 
 
@@ -262,7 +279,7 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
 
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
-              cfl_coef=None):
+              cfl_coef=None, smagorinsky_C=None):
     """A reference ns3d ``Simul`` (RK4) wired around ``oper``."""
     Simul = mods["ns3d_solver"].Simul
     sim = object.__new__(Simul)
@@ -279,5 +296,12 @@ def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
     sim.state.state_spect[:] = 0.0
     sim.state.state_phys[:] = 0.0
     sim._init_projection()
+    if smagorinsky_C is not None:
+        sim.params.oper = _Container(Lx=oper.Lx, nx=oper.nx)
+        sim.params.turb_model = _Container(
+            enable=True, type="smagorinsky",
+            smagorinsky=_Container(C=smagorinsky_C))
+        sim.is_turb_model_enabled = True
+        sim.turb_model = mods["smagorinsky"].SmagorinskyModel(sim)
     sim.time_stepping = mods["ns3d_ts"].TimeSteppingPseudoSpectralNS3D(sim)
     return sim

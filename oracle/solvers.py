@@ -208,8 +208,10 @@ class NS3DOracle(_SolverBase):
     nvar = 3
     keys_phys = ("vx", "vy", "vz")  # ns3d/state.py:20
 
-    def __init__(self, oper: OperNumpy3D, f=None, **kw):
+    def __init__(self, oper: OperNumpy3D, f=None, turb_model=None, **kw):
         self.f = f
+        # callable (oper, vx_fft, vy_fft, vz_fft) -> forcing (3, *shapeK)
+        self.turb_model = turb_model
         super().__init__(oper, **kw)
 
     def statephys_from_statespect(self):
@@ -256,6 +258,8 @@ class NS3DOracle(_SolverBase):
         F[0] = oper.fft(fx)
         F[1] = oper.fft(fy)
         F[2] = oper.fft(fz)
+        if self.turb_model is not None:  # ns3d/solver.py:246-249
+            F += self.turb_model(oper, vx_fft, vy_fft, vz_fft)
         self.project_state_spect(F)
         oper.dealiasing(F)
         return F

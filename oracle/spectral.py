@@ -190,6 +190,10 @@ class OperNumpy3D:
     def divfft_from_vecfft(self, vx, vy, vz):
         return 1j * (self.Kx * vx + self.Ky * vy + self.Kz * vz)
 
+    def grad_fft_from_arr_fft(self, arr_fft):
+        """fluidfft gradient used by ``turb_model/stress_tensor.py:22-26``."""
+        return 1j * self.Kx * arr_fft, 1j * self.Ky * arr_fft, 1j * self.Kz * arr_fft
+
     def project_perpk3d(self, vx, vy, vz):
         """In place ``v -= k (k.v)/|k|^2``; the k=0 mode is unchanged."""
         tmp = (self.Kx * vx + self.Ky * vy + self.Kz * vz) * self.inv_K_square_nozero

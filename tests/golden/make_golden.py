@@ -25,6 +25,7 @@ sys.path.insert(0, str(HERE.parent.parent))
 from oracle import refshim  # noqa: E402
 from oracle.spectral import OperNumpy2D, OperNumpy3D  # noqa: E402
 from oracle.solvers import NS2DOracle, NS3DOracle  # noqa: E402
+from oracle.turb import smagorinsky_forcing  # noqa: E402
 from fluidsim_gb300.init_fields import (  # noqa: E402
     isotropic_3d, noise_rot_2d, taylor_green_3d)
 
@@ -48,6 +49,9 @@ CASES_3D = [
          deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, init="tgv", steps=10),
     dict(name="ns3d_iso_24x16x32_f", nx=24, ny=16, nz=32, nu_2=5e-3, f=1.0,
          USE_CFL=False, deltat0=5e-3, init="iso", seed=4, steps=10),
+    dict(name="ns3d_smag_20x24x16", nx=20, ny=24, nz=16, nu_2=1e-3,
+         smagorinsky_C=0.18, USE_CFL=True, deltat0=0.2, deltat_max=0.2,
+         cfl_coef=0.5, init="iso", seed=6, steps=10),
 ]
 
 
@@ -97,12 +101,19 @@ def run_3d(mods, case):
         v0 = isotropic_3d(nx, ny, nz, *L, seed=case["seed"])
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef"])
-    sim = refshim.make_ns3d(mods, oper, f=case.get("f"), **kw)
+    sim = refshim.make_ns3d(mods, oper, f=case.get("f"),
+                            smagorinsky_C=case.get("smagorinsky_C"), **kw)
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
     tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
-    orc = NS3DOracle(oper, f=case.get("f"), **kw)
+    turb = None
+    if case.get("smagorinsky_C") is not None:
+        C = case["smagorinsky_C"]
+
+        def turb(o, vx, vy, vz):
+            return smagorinsky_forcing(o, vx, vy, vz, C=C)
+    orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **kw)
     orc.init_from_vxvyvzfft(*[c.copy() for c in v0])
     assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
@@ -126,7 +137,8 @@ def run_3d(mods, case):
 
 def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
-            "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps"]
+            "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
+            "smagorinsky_C"]
     return {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
                                    dtype=np.float64)
             for k in keys if k in case}

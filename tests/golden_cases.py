@@ -6,7 +6,7 @@ import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES_2D = ["ns2d_32_cfl", "ns2d_48x40_beta", "ns2d_256_c1"]
-CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f"]
+CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20x24x16"]
 
 
 def load(name):

@@ -29,6 +29,10 @@ def make_sim(name, precision="float64"):
         params.oper.nz = int(p["nz"])
         params.oper.Lz = L[2]
         params.f = p.get("f")
+        if p.get("smagorinsky_C") is not None:
+            params.turb_model.enable = True
+            params.turb_model.type = "smagorinsky"
+            params.turb_model.smagorinsky.C = p["smagorinsky_C"]
     else:
         params.beta = p.get("beta") or 0.0
     for k in ("nu_2", "nu_4", "nu_8", "nu_m4"):

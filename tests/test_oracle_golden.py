@@ -9,6 +9,7 @@ import pytest
 from golden_cases import CASES_2D, CASES_3D, lengths, load, solver_kwargs
 from oracle.spectral import OperNumpy2D, OperNumpy3D
 from oracle.solvers import NS2DOracle, NS3DOracle
+from oracle.turb import smagorinsky_forcing
 
 
 def make_oracle(name):
@@ -18,7 +19,13 @@ def make_oracle(name):
         orc = NS2DOracle(oper, beta=p.get("beta") or 0.0, **solver_kwargs(p))
     else:
         oper = OperNumpy3D(int(p["nx"]), int(p["ny"]), int(p["nz"]), *lengths(p, 3))
-        orc = NS3DOracle(oper, f=p.get("f"), **solver_kwargs(p))
+        turb = None
+        if p.get("smagorinsky_C") is not None:
+            C = p["smagorinsky_C"]
+
+            def turb(o, vx, vy, vz):
+                return smagorinsky_forcing(o, vx, vy, vz, C=C)
+        orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **solver_kwargs(p))
     orc.state_spect[:] = d["S_init"]
     orc.state_phys[:] = d["phys_init"]
     return orc, d, p
@@ -53,6 +60,8 @@ def test_reference_tendency_conserves_energy(name):
     """``ns2d/test_solver.py:49-69`` and ``ns3d/test_solver.py:73-96``."""
     if name == "ns3d_tgv_32":
         pytest.skip("Taylor-Green at t=0: the tendency is round-off only")
+    if "smag" in name:
+        pytest.skip("with a turbulence model the tendency dissipates energy")
     orc, d, _ = make_oracle(name)
     S, F = d["S_init"], d["tend0"]
     T = np.real(np.conj(F) * S).sum(axis=0)
