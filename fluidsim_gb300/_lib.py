@@ -28,6 +28,10 @@ EXPORTED = (
     "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
     "gbs_ns_spectrum_size", "gbs_ns_spectrum", "gbs_ns_timing",
     "gbs_ns_timing_report", "gbs_fft_c2r_noalloc", "gbs_ns_set_turb_model",
+    "gbs_mlp_grad_workspace", "gbs_mlp_forward", "gbs_mlp_grad", "gbs_mlp_adam",
+    "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
+    "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
+    "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
 )
 
 
@@ -86,6 +90,27 @@ def _declare(lib):
                                                ctypes.c_int, P, P, P]),
         "gbs_ns_set_turb_model": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double,
                                                  ctypes.POINTER(MLPWeights)]),
+        "gbs_mlp_grad_workspace": (ctypes.c_int64, [ctypes.c_int64]),
+        "gbs_ns_set_forcing": (ctypes.c_int, [P, P]),
+        "gbs_ens2d_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
+                                            ctypes.c_int64, ctypes.c_double, PP]),
+        "gbs_ens2d_destroy": (ctypes.c_int, [P]),
+        "gbs_ens2d_set_params": (ctypes.c_int, [P, DP, DP, DP]),
+        "gbs_ens2d_set_tuning": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "gbs_ens2d_step": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, P]),
+        "gbs_ens2d_nan_flag": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "gbs_spectral_resample": (ctypes.c_int, [I64P, I64P, ctypes.c_int, DP,
+                                                 ctypes.c_double, ctypes.c_int, P, P, P]),
+        "gbs_products6": (ctypes.c_int, [P, P, ctypes.c_int64, P, ctypes.c_int, P]),
+        "gbs_velocity_gradients": (ctypes.c_int, [I64P, DP, I64P, ctypes.c_int, P, P, P]),
+        "gbs_mlp_forward": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, ctypes.c_int64, P,
+                                           ctypes.c_int64, P]),
+        "gbs_mlp_grad": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, P, ctypes.c_int64, P,
+                                        ctypes.c_int64, P, P, P, P]),
+        "gbs_mlp_adam": (ctypes.c_int, [P, P, P, P, ctypes.c_int64, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.POINTER(MLPWeights), P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

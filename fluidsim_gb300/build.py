@@ -18,7 +18,8 @@ BUILD = HERE / "_build"
 LIB = HERE / "libgbspec.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gbs_fft.cu", "gbs_ns.cu", "gbs_noalloc.cu", "gbs_fast_f32.cu", "gbs_fast_f64.cu",
-           "gbs_turb.cu"]
+           "gbs_turb.cu", "gbs_mlp.cu", "gbs_les.cu",
+           "gbs_ensemble.cu"]
 
 
 def nvcc_path():
@@ -31,6 +32,9 @@ def nvcc_path():
 def _needs_rebuild(obj, src):
     if not obj.exists():
         return True
+    stamp = obj.with_suffix(".flags")
+    if not stamp.exists() or stamp.read_text() != os.environ.get("GBS_NVCC_FLAGS", ""):
+        return True
     deps = [src] + list(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "gbspec.h"]
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps)
 
@@ -40,6 +44,8 @@ def build(verbose=False, force=False):
     BUILD.mkdir(exist_ok=True)
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                     "-I", str(HERE.parent / "include")]
+    extra = os.environ.get("GBS_NVCC_FLAGS", "").split()
+    flags += extra
 
     def compile_one(name):
         src = CSRC / name
@@ -52,6 +58,7 @@ def build(verbose=False, force=False):
             raise RuntimeError(f"nvcc failed for {name}:\n{res.stderr}")
         if verbose:
             print(res.stderr, file=sys.stderr)
+        obj.with_suffix(".flags").write_text(os.environ.get("GBS_NVCC_FLAGS", ""))
         return obj
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:

@@ -1,0 +1,290 @@
+// Batched ns2d ensembles: many independent runs of one grid size advanced
+// together, one launch per pass for the whole batch (the run index is a
+// grid dimension), each run with its own viscosities and time step.  The
+// column width of the y passes and the rows per CTA of the x pass are
+// runtime choices among compiled variants, picked by the autotuner of
+// fluidsim_gb300.ensemble.  Float32 (the ensemble configuration's
+// precision); single runs and float64 go through gbs_ns.
+#include <new>
+
+#include "gbs_fast_launch.cuh"
+#include "gbs_internal.cuh"
+
+namespace gbs {
+
+template <typename T> int make_twiddles(cplx<T>* tw, int n, cudaStream_t st);
+
+namespace fast {
+
+template <int LOGN, int TX>
+static int ensA(const Geo& g, const void* S, void* W, const void* tw, int nb, cudaStream_t st) {
+  using C = cplx<float>;
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf2_inv_y<float, LOGN, TX>, smem);
+  if (rc) return rc;
+  kf2_inv_y<float, LOGN, TX><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
+      static_cast<const C*>(S), static_cast<C*>(W), g, static_cast<const C*>(tw));
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <int LOGM, int L>
+static int ensB(const Geo& g, const void* W, void* F, const void* tw, int nb, cudaStream_t st) {
+  using C = cplx<float>;
+  constexpr int M = 1 << LOGM;
+  constexpr int TH = 4 * L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)4 * L * M;
+  int rc = prep(kf2_x<float, LOGM, L>, smem);
+  if (rc) return rc;
+  kf2_x<float, LOGM, L><<<dim3(ceil_div(g.ny, L), nb), TH, smem, st>>>(
+      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), nullptr);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+template <int LOGN, int TX>
+static int ensC(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
+                const PerRun& pr, int nb, cudaStream_t st) {
+  using C = cplx<float>;
+  constexpr int TH = TX * (1 << LOGN) / 8;
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf2_fwd_y<float, LOGN, TX>, smem);
+  if (rc) return rc;
+  kf2_fwd_y<float, LOGN, TX><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
+      static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a, pr);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+#define GBS_ENS_LOG(logv, BODY)                       \
+  switch (logv) {                                     \
+    case 6: { constexpr int LG = 6; BODY; } break;    \
+    case 7: { constexpr int LG = 7; BODY; } break;    \
+    case 8: { constexpr int LG = 8; BODY; } break;    \
+    case 9: { constexpr int LG = 9; BODY; } break;    \
+    default:                                          \
+      set_error("ensemble: size not compiled");       \
+      return GBS_EINVAL;                              \
+  }
+
+#define GBS_ENS_TX(tx, BODY)                          \
+  switch (tx) {                                       \
+    case 4: { constexpr int TXV = 4; BODY; } break;   \
+    case 8: { constexpr int TXV = 8; BODY; } break;   \
+    case 16: { constexpr int TXV = 16; BODY; } break; \
+    default:                                          \
+      set_error("ensemble: tile width not compiled"); \
+      return GBS_EINVAL;                              \
+  }
+
+#define GBS_ENS_L(lv, BODY)                           \
+  switch (lv) {                                       \
+    case 1: { constexpr int LV = 1; BODY; } break;    \
+    case 2: { constexpr int LV = 2; BODY; } break;    \
+    case 4: { constexpr int LV = 4; BODY; } break;    \
+    case 8: { constexpr int LV = 8; BODY; } break;    \
+    default:                                          \
+      set_error("ensemble: rows per CTA not compiled"); \
+      return GBS_EINVAL;                              \
+  }
+
+}  // namespace fast
+
+struct Ensemble {
+  int nx, ny, nkx, nruns;
+  int64_t nK;
+  fast::Geo geo;
+  void *twx, *twy;
+  void *W, *F, *tmp, *tmp1;
+  double *nu2, *nu8, *dt;  // device, per run
+  int* dflag;
+  int txA, Lb, txC;
+};
+
+static void ens_free(Ensemble* e) {
+  void* p[] = {e->twx, e->twy, e->W, e->F, e->tmp, e->tmp1, e->nu2, e->nu8, e->dt, e->dflag};
+  for (void* q : p)
+    if (q) cudaFree(q);
+}
+
+}  // namespace gbs
+
+struct gbs_ens2d {
+  gbs::Ensemble e;
+};
+
+namespace gbs {
+
+static int ens_eval(Ensemble* e, const void* in, int mode, const RKArgs& a, bool pr,
+                    cudaStream_t st) {
+  fast::Geo g = e->geo;
+  g.pr = pr ? 1 : 0;
+  g.ncx = pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  const int lgy = ilog2(e->ny), lgm = ilog2(e->nx / 2);
+  const int nb = e->nruns;
+  int rc = GBS_OK;
+  GBS_ENS_LOG(lgy, GBS_ENS_TX(e->txA, rc = (fast::ensA<LG, TXV>(g, in, e->W, e->twy, nb, st))));
+  if (rc) return rc;
+  GBS_ENS_LOG(lgm, GBS_ENS_L(e->Lb, rc = (fast::ensB<LG, LV>(g, e->W, e->F, e->twx, nb, st))));
+  if (rc) return rc;
+  fast::PerRun prr{e->nu2, e->nu8, e->dt};
+  GBS_ENS_LOG(lgy, GBS_ENS_TX(e->txC, rc = (fast::ensC<LG, TXV>(g, e->F, e->twy, mode, a, prr,
+                                                               nb, st))));
+  return rc;
+}
+
+}  // namespace gbs
+
+extern "C" {
+
+int gbs_ens2d_create(int64_t nx, int64_t ny, double Lx, double Ly, int64_t nruns,
+                     int64_t kcut_x, int64_t kcut_y, double beta, gbs_ens2d** out) {
+  gbs::clear_error();
+  if (!out || nruns < 1 || nruns > 65535 || nx % 2 || !gbs::is_pow2((int)ny) ||
+      !gbs::is_pow2((int)(nx / 2)) || ny < 64 || ny > 512 || nx / 2 < 64 || nx / 2 > 512 ||
+      !(Lx > 0) || !(Ly > 0)) {
+    gbs::set_error("gbs_ens2d_create: invalid argument (power-of-two 128..1024 x 64..512)");
+    return GBS_EINVAL;
+  }
+  *out = nullptr;
+  gbs_ens2d* h = new (std::nothrow) gbs_ens2d();
+  if (!h) return GBS_ENOMEM;
+  gbs::Ensemble* e = &h->e;
+  memset(e, 0, sizeof(*e));
+  e->nx = (int)nx;
+  e->ny = (int)ny;
+  e->nkx = (int)(nx / 2 + 1);
+  e->nruns = (int)nruns;
+  e->nK = (int64_t)ny * e->nkx;
+  gbs::fast::Geo& g = e->geo;
+  g.nx = e->nx;
+  g.ny = e->ny;
+  g.nz = 1;
+  g.nkx = e->nkx;
+  g.M = e->nx / 2;
+  g.kcx = (int)(kcut_x < nx ? kcut_x : nx + 1);
+  g.kcy = (int)(kcut_y < ny ? kcut_y : ny + 1);
+  g.kcz = 1 << 30;
+  g.ncx = e->nkx;
+  g.nky_keep = e->ny;
+  const double pi2 = 6.283185307179586;
+  g.dkx = pi2 / Lx;
+  g.dky = pi2 / Ly;
+  g.beta = beta;
+  g.inv_n = 1.0 / ((double)nx * ny);
+  g.k2_hypo0 = g.dkx * g.dkx;
+  e->txA = 8;
+  e->Lb = 2;
+  e->txC = 8;
+  const size_t fb = sizeof(float2) * e->nK * nruns;
+  int rc = 0;
+  if (cudaMalloc(&e->twx, sizeof(float2) * nx) != cudaSuccess ||
+      cudaMalloc(&e->twy, sizeof(float2) * ny) != cudaSuccess ||
+      cudaMalloc(&e->W, fb * 4) != cudaSuccess || cudaMalloc(&e->F, fb) != cudaSuccess ||
+      cudaMalloc(&e->tmp, fb) != cudaSuccess || cudaMalloc(&e->tmp1, fb) != cudaSuccess ||
+      cudaMalloc(&e->nu2, sizeof(double) * nruns) != cudaSuccess ||
+      cudaMalloc(&e->nu8, sizeof(double) * nruns) != cudaSuccess ||
+      cudaMalloc(&e->dt, sizeof(double) * nruns) != cudaSuccess ||
+      cudaMalloc(&e->dflag, sizeof(int)) != cudaSuccess) {
+    gbs::set_error("gbs_ens2d_create: device allocation failed");
+    rc = GBS_ENOMEM;
+  }
+  if (!rc) rc = gbs::make_twiddles<float>(static_cast<float2*>(e->twx), e->nx, 0);
+  if (!rc) rc = gbs::make_twiddles<float>(static_cast<float2*>(e->twy), e->ny, 0);
+  if (!rc && (cudaMemset(e->tmp, 0, fb) != cudaSuccess ||
+              cudaMemset(e->tmp1, 0, fb) != cudaSuccess ||
+              cudaMemset(e->dflag, 0, sizeof(int)) != cudaSuccess ||
+              cudaDeviceSynchronize() != cudaSuccess)) {
+    gbs::set_error("gbs_ens2d_create: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = GBS_ECUDA;
+  }
+  if (rc) {
+    gbs::ens_free(e);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GBS_OK;
+}
+
+int gbs_ens2d_destroy(gbs_ens2d* h) {
+  if (!h) return GBS_OK;
+  gbs::ens_free(&h->e);
+  delete h;
+  return GBS_OK;
+}
+
+int gbs_ens2d_set_params(gbs_ens2d* h, const double* nu2, const double* nu8, const double* dt) {
+  gbs::clear_error();
+  if (!h || !nu2 || !nu8 || !dt) {
+    gbs::set_error("gbs_ens2d_set_params: null argument");
+    return GBS_EINVAL;
+  }
+  gbs::Ensemble* e = &h->e;
+  const size_t b = sizeof(double) * e->nruns;
+  GBS_CUDA_TRY(cudaMemcpy(e->nu2, nu2, b, cudaMemcpyHostToDevice));
+  GBS_CUDA_TRY(cudaMemcpy(e->nu8, nu8, b, cudaMemcpyHostToDevice));
+  GBS_CUDA_TRY(cudaMemcpy(e->dt, dt, b, cudaMemcpyHostToDevice));
+  return GBS_OK;
+}
+
+int gbs_ens2d_set_tuning(gbs_ens2d* h, int tx_inverse, int rows_x, int tx_forward) {
+  gbs::clear_error();
+  auto okt = [](int t) { return t == 4 || t == 8 || t == 16; };
+  auto okl = [](int l) { return l == 1 || l == 2 || l == 4 || l == 8; };
+  if (!h || !okt(tx_inverse) || !okt(tx_forward) || !okl(rows_x)) {
+    gbs::set_error("gbs_ens2d_set_tuning: tile width in {4, 8, 16}, rows in {1, 2, 4, 8}");
+    return GBS_EINVAL;
+  }
+  h->e.txA = tx_inverse;
+  h->e.Lb = rows_x;
+  h->e.txC = tx_forward;
+  return GBS_OK;
+}
+
+// nsteps RK4 steps of every run (state: nruns x (ny, nx/2+1) complex64).
+// Enqueue only (no host synchronisation): the calls can be captured into a
+// CUDA graph.  Dealiasing of the state is followed by the NaN flag.
+int gbs_ens2d_step(gbs_ens2d* h, void* S, int nsteps, int flags, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || nsteps < 1) {
+    gbs::set_error("gbs_ens2d_step: invalid argument");
+    return GBS_EINVAL;
+  }
+  gbs::Ensemble* e = &h->e;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool pr = (flags & GBS_STEP_DEALIASED) != 0;
+  gbs::RKArgs a{};
+  a.S = S;
+  a.Sout = S;
+  a.tmp = e->tmp;
+  a.tmp1 = e->tmp1;
+  a.nan_flag = e->dflag;
+  a.dt = 0.0;  // per run
+  for (int it = 0; it < nsteps; ++it) {
+    // a step that starts from an arbitrary state runs unpruned; the next ones
+    // start from the dealiased output of the previous step
+    const bool p = pr || it > 0;
+    int rc = gbs::ens_eval(e, S, gbs::kRK0, a, p, st);
+    if (rc) return rc;
+    for (int m = gbs::kRK1; m <= gbs::kRK3; ++m) {
+      rc = gbs::ens_eval(e, e->tmp1, m, a, p, st);
+      if (rc) return rc;
+    }
+  }
+  return GBS_OK;
+}
+
+int gbs_ens2d_nan_flag(gbs_ens2d* h, int* flag) {
+  gbs::clear_error();
+  if (!h || !flag) {
+    gbs::set_error("gbs_ens2d_nan_flag: null argument");
+    return GBS_EINVAL;
+  }
+  GBS_CUDA_TRY(cudaMemcpy(flag, h->e.dflag, sizeof(int), cudaMemcpyDeviceToHost));
+  GBS_CUDA_TRY(cudaMemset(h->e.dflag, 0, sizeof(int)));
+  return GBS_OK;
+}
+
+}  // extern "C"

@@ -22,8 +22,16 @@ namespace fast {
 
 extern __shared__ __align__(16) unsigned char g_smem_fast[];
 
-// min blocks per SM so that a CTA of `th` threads keeps <= 64 registers
-constexpr int min_blocks(int th) { return th >= 1024 ? 1 : 1024 / th; }
+// min blocks per SM so that GBS_OCC_THREADS threads can be resident
+// (1536: <= 42 registers per thread; 1024: <= 64)
+#ifndef GBS_OCC_THREADS
+#define GBS_OCC_THREADS 1536
+#endif
+constexpr int min_blocks(int th) {
+  return th >= GBS_OCC_THREADS ? 1 : GBS_OCC_THREADS / th;
+}
+// for kernels that would spill at the tighter bound (<= 64 registers)
+constexpr int min_blocks_lo(int th) { return th >= 1024 ? 1 : 1024 / th; }
 
 template <int LOGN>
 struct Line {
@@ -59,7 +67,9 @@ __device__ __forceinline__ bool kept(int p, int n, int kc) {
 // registers; `acc(p)` addresses position p of this line in shared memory.
 // Every thread of the CTA must call it (it contains barriers); `active`
 // threads compute, the others only take part in the barriers.
-template <int DIR, int LOGN, typename C, typename Acc>
+// WARP: every line lies inside one warp (rows with N/8 <= 32 threads and
+// the line index above jt), so the exchanges only need __syncwarp().
+template <int DIR, int LOGN, bool WARP = false, typename C, typename Acc>
 __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
                                     const C* __restrict__ tw, int tws) {
   using P = Line<LOGN>;
@@ -73,7 +83,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
 #pragma unroll
       for (int r = 0; r < 8; ++r) acc(d + r * Ns) = v[r];
     }
-    __syncthreads();
+    if (WARP) __syncwarp(); else __syncthreads();
     const int Nsn = Ns << 3;
     if (active) {
       if (s < P::S8) {
@@ -103,7 +113,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
         }
       }
     }
-    __syncthreads();
+    if (WARP) __syncwarp(); else __syncthreads();
   }
 }
 
@@ -168,7 +178,7 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
   for (int r = 0; r < 8; ++r) v[r] = valid ? xc[jt + r * M8] : mk<C>(0, 0);
   C* slot = buf + l * LS;
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
-  run<-1, LOGM>(v, jt, true, acc, twx, 2);
+  run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
   __syncthreads();
@@ -215,7 +225,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
   }
   C* slot = buf + l * LS;
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
-  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+  run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
   if (!valid) return;
   C* xc = reinterpret_cast<C*>(x) + row * M;
 #pragma unroll
@@ -234,6 +244,13 @@ struct Geo {
   int has_f;
 };
 
+// Per-run parameters of a batched ensemble (null pointers: single run).
+struct PerRun {
+  const double* nu2;
+  const double* nu8;
+  const double* dt;
+};
+
 __device__ __forceinline__ Phys phys_of(const Geo& g) {
   Phys q;
   q.nu2 = g.nu2;
@@ -250,7 +267,7 @@ __device__ __forceinline__ int iy_of(const Geo& g, int b) {
 
 // A: inverse z pass with the curl (6 output fields, one after the other).
 template <typename T, int LOGN, int TX>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks_lo(TX * (1 << LOGN) / 8))
 kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           const cplx<T>* __restrict__ twz) {
   using C = cplx<T>;
@@ -305,7 +322,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 // B: x pass.  6 fields x L rows; C2R, v x omega, R2C of the 3 products.
 
 template <typename T, int LOGM, int L>
-__global__ void __launch_bounds__(6 * L * (1 << LOGM) / 8, 2)
+__global__ void __launch_bounds__(6 * L * (1 << LOGM) / 8, min_blocks(6 * L * (1 << LOGM) / 8))
 kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
   using C = cplx<T>;
@@ -340,7 +357,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       v[r] = Z;
     }
   }
-  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+  run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
   __syncthreads();
@@ -365,7 +382,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const bool act = f < 3;
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
-  run<-1, LOGM>(v, jt, act, acc, twx, 2);
+  run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
@@ -457,6 +474,8 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const int ix = blockIdx.x * TX + c;
   const bool valid = ix < g.ncx;
   const int64_t nK = (int64_t)g.ny * g.nkx;
+  S += blockIdx.z * nK;  // run of a batched ensemble
+  W += blockIdx.z * 4 * nK;
   const T kx = T(g.dkx * ix);
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
 #pragma unroll 1
@@ -507,6 +526,8 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int64_t nK = nrows * g.nkx;
   const int64_t row = (int64_t)blockIdx.x * L + l;
   const bool valid = row < nrows;
+  W += blockIdx.y * 4 * nK;  // run of a batched ensemble
+  F += blockIdx.y * nK;
   C* slot = buf + (f * L + l) * LS;
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
@@ -528,7 +549,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       v[r] = Z;
     }
   }
-  run<+1, LOGM>(v, jt, true, acc, twx, 2);
+  run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
   __syncthreads();
@@ -554,7 +575,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const bool act = f == 0;
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
-  run<-1, LOGM>(v, jt, act, acc, twx, 2);
+  run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
@@ -579,13 +600,28 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 template <typename T, int LOGN, int TX>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
 kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
-          int mode, RKArgs a) {
+          int mode, RKArgs a, PerRun pr) {
   using C = cplx<T>;
   using P = Line<LOGN>;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
   const int ix = blockIdx.x * TX + c;
   const bool valid = ix < g.ncx;
+  {  // run of a batched ensemble: its fields and parameters
+    const int64_t off = blockIdx.z * (int64_t)g.ny * g.nkx;
+    F += off;
+    if (a.S) a.S = static_cast<const C*>(a.S) + off;
+    if (a.Sout) a.Sout = static_cast<C*>(a.Sout) + off;
+    if (a.tmp) a.tmp = static_cast<C*>(a.tmp) + off;
+    if (a.tmp1) a.tmp1 = static_cast<C*>(a.tmp1) + off;
+    if (a.tend) a.tend = static_cast<C*>(a.tend) + off;
+    if (a.add) a.add = static_cast<const C*>(a.add) + off;
+    if (pr.dt) {
+      a.dt = pr.dt[blockIdx.z];
+      g.nu2 = pr.nu2[blockIdx.z];
+      g.nu8 = pr.nu8[blockIdx.z];
+    }
+  }
   C v[8];
 #pragma unroll
   for (int r = 0; r < 8; ++r)

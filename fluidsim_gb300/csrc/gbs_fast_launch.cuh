@@ -234,7 +234,7 @@ static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, cons
   int rc = prep(kf2_fwd_y<T, LOGN, TX>, smem);
   if (rc) return rc;
   kf2_fwd_y<T, LOGN, TX><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
-      static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a);
+      static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a, PerRun{});
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }

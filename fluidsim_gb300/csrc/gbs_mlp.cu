@@ -1,0 +1,332 @@
+// Training and inference kernels of the learned subgrid-stress closure.
+//
+// Network: x = g * in_scale (9) -> h1 = tanh(W1 x + b1) (64)
+//          -> h2 = tanh(W2 h1 + b2) (64) -> y = W3 h2 + b3 (6),
+//          tau = y * out_scale.  Weights are read as BF16, arithmetic and
+//          accumulation are FP32.  Loss: mean over samples and outputs of
+//          (y - tau_target / out_scale)^2.
+//
+// Data are structure-of-arrays fields: g[c * ld + i] (9 rows), tau[o * ld + i]
+// (6 rows), so the gradient and stress fields of the LES / filtered DNS are
+// used in place.  A minibatch is a list of point indices.
+//
+// Gradient: one thread per sample computes the forward pass and the
+// back-propagated deltas and stores (x, h1, h2, dz1, dz2, dy) in a
+// workspace; the weight gradients are then reduced over the batch in
+// chunks (shared-memory tiles, fixed order, one partial row per block) and
+// summed over blocks in a fixed order, so the result is deterministic.
+#include <cuda_bf16.h>
+
+#include "gbs_internal.cuh"
+#include "gbs_turb.h"
+
+namespace gbs {
+
+constexpr int kNP = kH * kIn + kH + kH * kH + kH + kOut * kH + kOut;  // 5190
+constexpr int kFeat = kIn + kH + kH + kH + kH + kOut;                 // per-sample rows
+constexpr int kOffW1 = 0, kOffB1 = kH * kIn, kOffW2 = kOffB1 + kH;
+constexpr int kOffB2 = kOffW2 + kH * kH, kOffW3 = kOffB2 + kH, kOffB3 = kOffW3 + kOut * kH;
+// workspace rows (each of length B)
+constexpr int kRX = 0, kRH1 = kIn, kRH2 = kRH1 + kH, kRZ1 = kRH2 + kH, kRZ2 = kRZ1 + kH,
+              kRDY = kRZ2 + kH;
+constexpr int kChunk = 2048;  // samples per block in the weight-gradient reduction
+constexpr int kTile = 32;
+
+__device__ __forceinline__ void load_weights(float* W1, float* b1, float* W2, float* b2,
+                                             float* W3, float* b3, float* sin, float* sout,
+                                             const MLPWeights& w) {
+  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) W2[i] = __bfloat162float(w.W2[i]);
+  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) W1[i] = __bfloat162float(w.W1[i]);
+  for (int i = threadIdx.x; i < kOut * kH; i += blockDim.x) W3[i] = __bfloat162float(w.W3[i]);
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    b1[i] = w.b1[i];
+    b2[i] = w.b2[i];
+  }
+  if (threadIdx.x < kOut) {
+    b3[threadIdx.x] = w.b3[threadIdx.x];
+    sout[threadIdx.x] = w.out_scale[threadIdx.x];
+  }
+  if (threadIdx.x < kIn) sin[threadIdx.x] = w.in_scale[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256)
+k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict__ tau,
+              int64_t ld, const int64_t* __restrict__ idx, int64_t B, float* __restrict__ ws,
+              float* __restrict__ loss) {
+  __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
+  __shared__ float sin[kIn], sout[kOut];
+  __shared__ float red[8];
+  load_weights(W1, b1, W2, b2, W3, b3, sin, sout, w);
+  __syncthreads();
+  float lsum = 0.f;
+  const float inv = 2.f / (float)(B * kOut);
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx[b];
+    float x[kIn];
+#pragma unroll
+    for (int c = 0; c < kIn; ++c) {
+      x[c] = g[c * ld + i] * sin[c];
+      ws[(kRX + c) * B + b] = x[c];
+    }
+    float h1[kH];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) {
+      float z = b1[j];
+#pragma unroll
+      for (int c = 0; c < kIn; ++c) z = fmaf(W1[j * kIn + c], x[c], z);
+      h1[j] = tanhf(z);
+      ws[(kRH1 + j) * B + b] = h1[j];
+    }
+    float y[kOut];
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) y[o] = b3[o];
+#pragma unroll 4
+    for (int j = 0; j < kH; ++j) {
+      float z = b2[j];
+#pragma unroll
+      for (int c = 0; c < kH; ++c) z = fmaf(W2[j * kH + c], h1[c], z);
+      const float h2 = tanhf(z);
+      ws[(kRH2 + j) * B + b] = h2;
+#pragma unroll
+      for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
+    }
+    float dy[kOut];
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) {
+      const float d = y[o] - tau[o * ld + i] / sout[o];
+      lsum = fmaf(d, d, lsum);
+      dy[o] = inv * d;
+      ws[(kRDY + o) * B + b] = dy[o];
+    }
+    // dh1 = W2^T dz2, dz2 = (W3^T dy) * (1 - h2^2); h1 is reused as dh1
+#pragma unroll
+    for (int c = 0; c < kH; ++c) h1[c] = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < kH; ++j) {
+      float dh2 = 0.f;
+#pragma unroll
+      for (int o = 0; o < kOut; ++o) dh2 = fmaf(W3[o * kH + j], dy[o], dh2);
+      const float h2 = ws[(kRH2 + j) * B + b];
+      const float dz2 = dh2 * (1.f - h2 * h2);
+      ws[(kRZ2 + j) * B + b] = dz2;
+#pragma unroll
+      for (int c = 0; c < kH; ++c) h1[c] = fmaf(W2[j * kH + c], dz2, h1[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < kH; ++c) {
+      const float a = ws[(kRH1 + c) * B + b];
+      ws[(kRZ1 + c) * B + b] = h1[c] * (1.f - a * a);
+    }
+  }
+  // block reduction of the loss (fixed order inside the block)
+  for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float s = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    atomicAdd(loss, s / (float)(B * kOut));
+  }
+}
+
+// parameter p -> (row a of the left operand, row c of the right operand) of
+// the outer-product sum  sum_b left[a][b] * right[c][b]  (right row -1: 1)
+__device__ __forceinline__ void param_rows(int p, int& a, int& c) {
+  if (p < kOffB1) { a = kRZ1 + p / kIn; c = kRX + p % kIn; }
+  else if (p < kOffW2) { a = kRZ1 + (p - kOffB1); c = -1; }
+  else if (p < kOffB2) { const int q = p - kOffW2; a = kRZ2 + q / kH; c = kRH1 + q % kH; }
+  else if (p < kOffW3) { a = kRZ2 + (p - kOffB2); c = -1; }
+  else if (p < kOffB3) { const int q = p - kOffW3; a = kRDY + q / kH; c = kRH2 + q % kH; }
+  else { a = kRDY + (p - kOffB3); c = -1; }
+}
+
+__global__ void __launch_bounds__(256)
+k_mlp_wgrad(const float* __restrict__ ws, int64_t B, float* __restrict__ partial) {
+  __shared__ float tile[kFeat][kTile + 1];
+  constexpr int PPT = (kNP + 255) / 256;
+  float acc[PPT];
+  int ra[PPT], rc[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    acc[k] = 0.f;
+    const int p = threadIdx.x + k * 256;
+    if (p < kNP) param_rows(p, ra[k], rc[k]);
+    else { ra[k] = 0; rc[k] = -1; }
+  }
+  const int64_t b0 = (int64_t)blockIdx.x * kChunk;
+  const int64_t b1 = b0 + kChunk < B ? b0 + kChunk : B;
+  for (int64_t t0 = b0; t0 < b1; t0 += kTile) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kFeat * kTile; e += blockDim.x) {
+      const int r = e / kTile, s = e % kTile;
+      tile[r][s] = t0 + s < b1 ? ws[r * B + t0 + s] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (threadIdx.x + k * 256 >= kNP) continue;
+      float sacc = 0.f;
+      if (rc[k] < 0) {
+        for (int s = 0; s < kTile; ++s) sacc += tile[ra[k]][s];
+      } else {
+        for (int s = 0; s < kTile; ++s) sacc = fmaf(tile[ra[k]][s], tile[rc[k]][s], sacc);
+      }
+      acc[k] += sacc;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int p = threadIdx.x + k * 256;
+    if (p < kNP) partial[(int64_t)blockIdx.x * kNP + p] = acc[k];
+  }
+}
+
+__global__ void k_mlp_sum_partials(const float* __restrict__ partial, int nblocks,
+                                   float* __restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNP) return;
+  float s = 0.f;
+  for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)b * kNP + p];
+  grad[p] = s;
+}
+
+// Adam on the FP32 master weights, then the BF16 copies of W1, W2, W3.
+__global__ void k_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ grad, float lr, float beta1, float beta2,
+                       float eps, float bc1, float bc2, __nv_bfloat16* W1, __nv_bfloat16* W2,
+                       __nv_bfloat16* W3) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNP) return;
+  const float gr = grad[p];
+  const float mm = beta1 * m[p] + (1.f - beta1) * gr;
+  const float vv = beta2 * v[p] + (1.f - beta2) * gr * gr;
+  m[p] = mm;
+  v[p] = vv;
+  const float w = master[p] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+  master[p] = w;
+  if (p < kOffB1) W1[p - kOffW1] = __float2bfloat16(w);
+  else if (p >= kOffW2 && p < kOffB2) W2[p - kOffW2] = __float2bfloat16(w);
+  else if (p >= kOffW3 && p < kOffB3) W3[p - kOffW3] = __float2bfloat16(w);
+}
+
+// inference on SoA fields (float)
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mlp_forward(MLPWeights w, const T* __restrict__ g, int64_t ld, T* __restrict__ tau,
+              int64_t n) {
+  __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
+  __shared__ float sin[kIn], sout[kOut];
+  load_weights(W1, b1, W2, b2, W3, b3, sin, sout, w);
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x[kIn];
+#pragma unroll
+    for (int c = 0; c < kIn; ++c) x[c] = (float)g[c * ld + i] * sin[c];
+    float h1[kH];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) {
+      float z = b1[j];
+#pragma unroll
+      for (int c = 0; c < kIn; ++c) z = fmaf(W1[j * kIn + c], x[c], z);
+      h1[j] = tanhf(z);
+    }
+    float y[kOut];
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) y[o] = b3[o];
+#pragma unroll 4
+    for (int j = 0; j < kH; ++j) {
+      float z = b2[j];
+#pragma unroll
+      for (int c = 0; c < kH; ++c) z = fmaf(W2[j * kH + c], h1[c], z);
+      const float h2 = tanhf(z);
+#pragma unroll
+      for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) tau[o * ld + i] = T(y[o] * sout[o]);
+  }
+}
+
+static MLPWeights to_w(const gbs_mlp_weights* p) {
+  MLPWeights w;
+  w.W1 = static_cast<const __nv_bfloat16*>(p->W1);
+  w.W2 = static_cast<const __nv_bfloat16*>(p->W2);
+  w.W3 = static_cast<const __nv_bfloat16*>(p->W3);
+  w.b1 = p->b1;
+  w.b2 = p->b2;
+  w.b3 = p->b3;
+  w.in_scale = p->in_scale;
+  w.out_scale = p->out_scale;
+  return w;
+}
+
+}  // namespace gbs
+
+extern "C" {
+
+int64_t gbs_mlp_grad_workspace(int64_t batch) {
+  const int64_t nb = (batch + gbs::kChunk - 1) / gbs::kChunk;
+  return (int64_t)sizeof(float) * (gbs::kFeat * batch + nb * gbs::kNP);
+}
+
+int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float* tau,
+                    int64_t n, void* stream) {
+  gbs::clear_error();
+  if (!w || !g || !tau || n < 0 || ld < n) {
+    gbs::set_error("gbs_mlp_forward: invalid argument");
+    return GBS_EINVAL;
+  }
+  if (n == 0) return GBS_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int64_t nb = (n + 255) / 256;
+  if (nb > 152 * 16) nb = 152 * 16;
+  gbs::k_mlp_forward<float><<<(int)nb, 256, 0, st>>>(gbs::to_w(w), g, ld, tau, n);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau, int64_t ld,
+                 const int64_t* idx, int64_t batch, void* workspace, float* grad,
+                 float* loss, void* stream) {
+  gbs::clear_error();
+  if (!w || !g || !tau || !idx || batch < 1 || !workspace || !grad || !loss) {
+    gbs::set_error("gbs_mlp_grad: invalid argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  float* ws = static_cast<float*>(workspace);
+  const int nb = (int)((batch + gbs::kChunk - 1) / gbs::kChunk);
+  float* partial = ws + (int64_t)gbs::kFeat * batch;
+  GBS_CUDA_TRY(cudaMemsetAsync(loss, 0, sizeof(float), st));
+  int64_t g1 = (batch + 255) / 256;
+  if (g1 > 152 * 8) g1 = 152 * 8;
+  gbs::k_mlp_fwd_bwd<<<(int)g1, 256, 0, st>>>(gbs::to_w(w), g, tau, ld, idx, batch, ws, loss);
+  GBS_CHECK_LAUNCH();
+  gbs::k_mlp_wgrad<<<nb, 256, 0, st>>>(ws, batch, partial);
+  GBS_CHECK_LAUNCH();
+  gbs::k_mlp_sum_partials<<<(gbs::kNP + 255) / 256, 256, 0, st>>>(partial, nb, grad);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+int gbs_mlp_adam(float* master, float* m, float* v, const float* grad, int64_t step,
+                 double lr, double beta1, double beta2, double eps,
+                 const gbs_mlp_weights* w_bf16, void* stream) {
+  gbs::clear_error();
+  if (!master || !m || !v || !grad || step < 1 || !w_bf16) {
+    gbs::set_error("gbs_mlp_adam: invalid argument");
+    return GBS_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const float bc1 = (float)(1.0 - pow(beta1, (double)step));
+  const float bc2 = (float)(1.0 - pow(beta2, (double)step));
+  gbs::k_adam<<<(gbs::kNP + 255) / 256, 256, 0, st>>>(
+      master, m, v, grad, (float)lr, (float)beta1, (float)beta2, (float)eps, bc1, bc2,
+      (__nv_bfloat16*)w_bf16->W1, (__nv_bfloat16*)w_bf16->W2, (__nv_bfloat16*)w_bf16->W3);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
+}  // extern "C"

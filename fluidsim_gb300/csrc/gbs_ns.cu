@@ -435,6 +435,7 @@ struct Solver {
   // turbulence model (ns3d): forcing buffer and its pipeline
   TurbCtx turb;
   void* turbF;
+  const void* forcing;  // caller-owned forcing (nvar spectral fields) or null
   // compile-time-size path (all axes powers of two in range)
   int use_fast;
   fast::Geo geo;
@@ -687,9 +688,9 @@ static int finish(Solver* s, int mode, const RKArgs& a, cudaStream_t st,
 // turbulence-model forcing of the stage input `in` (null when disabled)
 template <typename T>
 static int turb_stage(Solver* s, const void* in, RKArgs& a, cudaStream_t st) {
-  a.add = nullptr;
+  a.add = s->forcing;
   if (s->turb.type == kTurbNone) return GBS_OK;
-  int rc = turb_forcing<T>(s->turb, in, s->turbF, st);
+  int rc = turb_forcing<T>(s->turb, in, s->turbF, s->forcing, st);
   if (rc) return rc;
   a.add = s->turbF;
   return GBS_OK;
@@ -1175,6 +1176,16 @@ int gbs_ns_set_turb_model(gbs_ns* h, int type, double C,
     free_turb(s);
     return rc;
   }
+  return GBS_OK;
+}
+
+int gbs_ns_set_forcing(gbs_ns* h, const void* forcing) {
+  gbs::clear_error();
+  if (!h) {
+    gbs::set_error("gbs_ns_set_forcing: null solver");
+    return GBS_EINVAL;
+  }
+  h->s.forcing = forcing;
   return GBS_OK;
 }
 

@@ -128,7 +128,7 @@ k_mlp_closure(const T* __restrict__ g, T* __restrict__ tau, int64_t n, MLPWeight
 // f_i = coef * 1j * sum_j K_j t_hat_{ij}
 template <typename T>
 __global__ void k_div_stress(const cplx<T>* __restrict__ Tk, cplx<T>* __restrict__ F, KGeo g,
-                             T coef) {
+                             T coef, const cplx<T>* __restrict__ extra) {
   using C = cplx<T>;
   const int64_t nK = (int64_t)g.nz * g.ny * g.nkx;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
@@ -146,7 +146,9 @@ __global__ void k_div_stress(const cplx<T>* __restrict__ Tk, cplx<T>* __restrict
         acc.x += k[j] * t.x;
         acc.y += k[j] * t.y;
       }
-      F[i + c * nK] = mk<C>(-coef * acc.y, coef * acc.x);
+      C f = mk<C>(-coef * acc.y, coef * acc.x);
+      if (extra) f = cadd(f, extra[i + c * nK]);
+      F[i + c * nK] = f;
     }
   }
 }
@@ -157,7 +159,8 @@ static int grid_for(int64_t n) {
 }
 
 template <typename T>
-int turb_forcing(const TurbCtx& t, const void* S, void* out, cudaStream_t st) {
+int turb_forcing(const TurbCtx& t, const void* S, void* out, const void* extra,
+                 cudaStream_t st) {
   using C = cplx<T>;
   KGeo g{t.nx, t.ny, t.nz, t.nx / 2 + 1, t.dkx, t.dky, t.dkz};
   const int64_t nK = (int64_t)t.nz * t.ny * (t.nx / 2 + 1);
@@ -178,12 +181,15 @@ int turb_forcing(const TurbCtx& t, const void* S, void* out, cudaStream_t st) {
   if (rc) return rc;
   const T coef = t.type == kTurbSmagorinsky ? T(2) : T(-1);
   k_div_stress<T><<<grid_for(nK), 256, 0, st>>>(static_cast<const C*>(t.Tk),
-                                                static_cast<C*>(out), g, coef);
+                                                static_cast<C*>(out), g, coef,
+                                                static_cast<const C*>(extra));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
 
-template int turb_forcing<float>(const TurbCtx&, const void*, void*, cudaStream_t);
-template int turb_forcing<double>(const TurbCtx&, const void*, void*, cudaStream_t);
+template int turb_forcing<float>(const TurbCtx&, const void*, void*, const void*,
+                                 cudaStream_t);
+template int turb_forcing<double>(const TurbCtx&, const void*, void*, const void*,
+                                  cudaStream_t);
 
 }  // namespace gbs

@@ -38,7 +38,9 @@ struct TurbCtx {
   void* Tk;              // 6 spectral fields
 };
 
+// out = turbulence-model forcing of S (+ extra when not null)
 template <typename T>
-int turb_forcing(const TurbCtx& t, const void* S, void* out, cudaStream_t st);
+int turb_forcing(const TurbCtx& t, const void* S, void* out, const void* extra,
+                 cudaStream_t st);
 
 }  // namespace gbs

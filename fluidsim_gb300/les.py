@@ -1,0 +1,245 @@
+"""Learned subgrid closure for coarse-grid LES, end to end on one GB300.
+
+1. ``forced_dns``: ns3d DNS (FP32) forced by ``TCRandomForcing3D`` in the
+   shells ``k in [2, 3]`` at power 1; snapshots of the spectral state.
+2. ``filtered_data``: for each snapshot, top-hat filter of width
+   Delta = L / n_les and resampling to the LES grid; targets
+   ``tau_ij = filt(u_i u_j) - filt(u_i) filt(u_j)`` and inputs
+   ``d_j filt(u_i)`` (the LES-dealiased filtered field), as 9 / 6 float32
+   fields on the LES grid.
+3. ``train_closure``: the 9 -> 64 -> 64 -> 6 network trained with the
+   hand-written gradient and Adam kernels (``closure.ClosureTrainer``).
+4. ``run_les``: forced LES on the coarse grid with no model, Smagorinsky or
+   the learned closure; time-averaged shell energy spectrum and wall time.
+5. ``spectral_error``: relative error of E(k) against the filtered DNS
+   spectrum over the LES-resolved shells.
+
+``python -m fluidsim_gb300.les --n-dns 512 --n-les 128`` runs the whole
+pipeline and prints one JSON line.
+"""
+
+import argparse
+import ctypes
+import json
+import time
+from math import pi
+
+import numpy as np
+import torch
+
+from . import _lib
+from .closure import ClosureMLP, ClosureTrainer
+from .fft import FFT3DGB300, current_stream_handle
+from .init_fields import cubic_dealias_cutoff, isotropic_3d
+from .solvers import SimulNS3D
+
+
+def make_sim(n, nu, cfl=0.5, precision="float32", turb=None, forcing=True, seed=0):
+    p = SimulNS3D.create_default_params()
+    p.precision = precision
+    p.oper.nx = p.oper.ny = p.oper.nz = n
+    p.nu_2 = nu
+    ts = p.time_stepping
+    ts.USE_CFL, ts.cfl_coef, ts.deltat0, ts.USE_T_END = True, cfl, 1e-3, False
+    if forcing:
+        p.forcing.enable, p.forcing.type, p.forcing.seed = True, "tcrandom", seed
+    if turb == "smagorinsky":
+        p.turb_model.enable, p.turb_model.type = True, "smagorinsky"
+    elif turb is not None:
+        p.turb_model.enable, p.turb_model.type = True, "mlp_closure"
+    sim = SimulNS3D(p)
+    if turb is not None and turb != "smagorinsky":
+        sim.set_closure(turb)
+    return sim
+
+
+def shell_spectrum(sim):
+    k, E = sim.output.compute_spectrum()
+    return k, E
+
+
+def forced_dns(n, nu=3e-4, steps_spinup=2000, n_snap=4, snap_every=200, seed=0):
+    """Forced DNS; returns (snapshots on the device, mean spectrum, stats)."""
+    sim = make_sim(n, nu, seed=seed)
+    v0 = isotropic_3d(n, n, n, k0=3.0, energy=0.5, seed=seed)
+    sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2])
+    ts = sim.time_stepping
+    t0 = time.perf_counter()
+    for _ in range(steps_spinup):
+        ts.one_time_step()
+    torch.cuda.synchronize()
+    t_spin = time.perf_counter() - t0
+    snaps, spectra = [], []
+    t0 = time.perf_counter()
+    t_sim0 = ts.t
+    nsteps = 0
+    for _ in range(n_snap):
+        for _ in range(snap_every):
+            ts.one_time_step()
+            nsteps += 1
+        snaps.append(sim.state.state_spect.clone())
+        spectra.append(shell_spectrum(sim)[1])
+    torch.cuda.synchronize()
+    t_run = time.perf_counter() - t0
+    k = shell_spectrum(sim)[0]
+    stats = {"n": n, "steps": steps_spinup + nsteps, "dt_last": ts.deltat,
+             "s_per_step": t_run / max(nsteps, 1), "t_spinup_s": t_spin,
+             "wall_per_time_unit_s": t_run / (ts.t - t_sim0),
+             "E": sim.output.compute_energy(), "t": ts.t}
+    return snaps, (k, np.mean(spectra, axis=0)), stats
+
+
+def filtered_data(snaps, n_dns, n_les):
+    """(G (9, N) float32, Tau (6, N) float32) on the LES grid, and the mean
+    shell spectrum of the filtered velocity."""
+    lib = _lib.load()
+    st = current_stream_handle()
+    delta = 2 * pi / n_les
+    L = (ctypes.c_double * 3)(2 * pi, 2 * pi, 2 * pi)
+    sin_ = (ctypes.c_int64 * 3)(n_dns, n_dns, n_dns)
+    sout = (ctypes.c_int64 * 3)(n_les, n_les, n_les)
+    dns = FFT3DGB300(n_dns, n_dns, n_dns, precision="float32")
+    les = FFT3DGB300(n_les, n_les, n_les, precision="float32")
+    kc = cubic_dealias_cutoff(n_les, 2 * pi)
+    kcut = (ctypes.c_int64 * 3)(kc, kc, kc)
+    Gs, Ts, specs = [], [], []
+    first = None
+    sim_les = make_sim(n_les, 1e-3, forcing=False)
+    for S in snaps:
+        u = torch.empty((3,) + dns.shapeX, dtype=torch.float32, device="cuda")
+        dns.ifft_as_arg(S.contiguous(), u)
+        uu = torch.empty((6,) + dns.shapeX, dtype=torch.float32, device="cuda")
+        _lib.check(lib.gbs_products6(ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(uu.data_ptr()),
+                                     u[0].numel(), None, _lib.GBS_F32, st))
+        del u
+        uu_k = torch.empty((6,) + dns.shapeK, dtype=torch.complex64, device="cuda")
+        dns.fft_as_arg(uu, uu_k)
+        del uu
+        ub_k = torch.empty((3,) + les.shapeK, dtype=torch.complex64, device="cuda")
+        uub_k = torch.empty((6,) + les.shapeK, dtype=torch.complex64, device="cuda")
+        for src, dst, nf in ((S, ub_k, 3), (uu_k, uub_k, 6)):
+            _lib.check(lib.gbs_spectral_resample(sin_, sout, nf, L, delta, _lib.GBS_F32,
+                                                 ctypes.c_void_p(src.data_ptr()),
+                                                 ctypes.c_void_p(dst.data_ptr()), st))
+        del uu_k
+        ub = torch.empty((3,) + les.shapeX, dtype=torch.float32, device="cuda")
+        les.ifft_as_arg(ub_k, ub)
+        uub = torch.empty((6,) + les.shapeX, dtype=torch.float32, device="cuda")
+        les.ifft_as_arg_destroy(uub_k, uub)
+        tau = torch.empty_like(uub)
+        _lib.check(lib.gbs_products6(ctypes.c_void_p(ub.data_ptr()), ctypes.c_void_p(tau.data_ptr()),
+                                     ub[0].numel(), ctypes.c_void_p(uub.data_ptr()),
+                                     _lib.GBS_F32, st))
+        gk = torch.empty((9,) + les.shapeK, dtype=torch.complex64, device="cuda")
+        _lib.check(lib.gbs_velocity_gradients(sout, L, kcut, _lib.GBS_F32,
+                                              ctypes.c_void_p(ub_k.data_ptr()),
+                                              ctypes.c_void_p(gk.data_ptr()), st))
+        g = torch.empty((9,) + les.shapeX, dtype=torch.float32, device="cuda")
+        les.ifft_as_arg_destroy(gk, g)
+        Gs.append(g.reshape(9, -1))
+        Ts.append(tau.reshape(6, -1))
+        sim_les.state.state_spect.copy_(ub_k)
+        specs.append(shell_spectrum(sim_les)[1])
+        if first is None:
+            sim_les.oper.dealiasing(ub_k)
+            first = ub_k.cpu().numpy()
+    k = shell_spectrum(sim_les)[0]
+    return torch.cat(Gs, dim=1).contiguous(), torch.cat(Ts, dim=1).contiguous(), (
+        k, np.mean(specs, axis=0)), first
+
+
+def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, seed=0):
+    net = ClosureMLP(seed=seed)
+    tr = ClosureTrainer(net, batch=batch, lr=lr, seed=seed)
+    tr.set_scales(G, Tau)
+    t0 = time.perf_counter()
+    hist = tr.train(G, Tau, steps, log_every=max(steps // 10, 1))
+    torch.cuda.synchronize()
+    return net, {"history": hist, "train_s": time.perf_counter() - t0, "steps": steps,
+                 "batch": batch, "samples": int(G.shape[1])}
+
+
+def run_les(n, model, nu=3e-4, steps=2000, avg_last=1000, init=None, seed=0):
+    """Forced LES; returns ((k, time-averaged E(k)), stats)."""
+    sim = make_sim(n, nu, turb=model, seed=seed)
+    if init is None:
+        init = isotropic_3d(n, n, n, k0=3.0, energy=0.5, seed=seed)
+    sim.state.init_statespect_from(**{k: init[i] for i, k in enumerate(sim.state.keys_state_spect)})
+    ts = sim.time_stepping
+    specs = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(steps):
+        ts.one_time_step()
+        if it >= steps - avg_last and (it - (steps - avg_last)) % 50 == 0:
+            specs.append(shell_spectrum(sim)[1])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    k = shell_spectrum(sim)[0]
+    return (k, np.mean(specs, axis=0)), {"n": n, "steps": steps, "wall_s": wall,
+                                          "s_per_step": wall / steps, "dt_last": ts.deltat,
+                                          "wall_per_time_unit_s": wall / ts.t,
+                                          "E": sim.output.compute_energy(), "t": ts.t}
+
+
+def spectral_error(k_les, E_les, k_ref, E_ref, kmin=1.0, kmax=None):
+    """Mean relative error of E(k) over shells kmin <= k <= kmax."""
+    n = min(len(E_les), len(E_ref))
+    k = k_les[:n]
+    sel = (k >= kmin) & (k <= (kmax if kmax is not None else k[n - 1]))
+    return float(np.mean(np.abs(E_les[:n][sel] - E_ref[:n][sel]) / E_ref[:n][sel]))
+
+
+def pipeline(n_dns=512, n_les=128, nu=3e-4, spinup=2000, n_snap=4, snap_every=200,
+             train_steps=3000, les_steps=2000, seed=0):
+    out = {"config": {"n_dns": n_dns, "n_les": n_les, "nu": nu, "forcing": "tcrandom k in [2,3], P=1",
+                      "closure": "MLP 9-64-64-6 tanh, BF16 weights, FP32 accumulation"}}
+    snaps, (k_dns, E_dns), st_dns = forced_dns(n_dns, nu, steps_spinup=spinup, n_snap=n_snap,
+                                              snap_every=snap_every, seed=seed)
+    out["dns"] = st_dns
+    G, Tau, (k_f, E_f), init_les = filtered_data(snaps, n_dns, n_les)
+    del snaps
+    torch.cuda.empty_cache()
+    net, st_train = train_closure(G, Tau, steps=train_steps, seed=seed)
+    out["train"] = st_train
+    from .closure import predict
+    pred = predict(net, G)
+    out["train"]["rel_mse"] = float(((pred - Tau) ** 2).mean() / (Tau**2).mean())
+    del G, Tau
+    kc = cubic_dealias_cutoff(n_les, 2 * pi) - 1
+    res = {}
+    for name, model in (("none", None), ("smagorinsky", "smagorinsky"), ("learned", net)):
+        (k_l, E_l), st = run_les(n_les, model, nu=nu, steps=les_steps, avg_last=les_steps // 2,
+                                 init=init_les, seed=seed)
+        st["spectral_error"] = spectral_error(k_l, E_l, k_f, E_f, kmin=1.0, kmax=kc)
+        res[name] = st
+        res[name]["E_k"] = [float(x) for x in E_l[:kc + 1]]
+    out["les"] = res
+    out["filtered_dns_E_k"] = [float(x) for x in E_f[:kc + 1]]
+    out["wall_time_ratio_dns_over_les_per_unit_time"] = (
+        st_dns["wall_per_time_unit_s"] / res["learned"]["wall_per_time_unit_s"])
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n-dns", type=int, default=512)
+    ap.add_argument("--n-les", type=int, default=128)
+    ap.add_argument("--spinup", type=int, default=2000)
+    ap.add_argument("--n-snap", type=int, default=4)
+    ap.add_argument("--snap-every", type=int, default=200)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--les-steps", type=int, default=2000)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    out = pipeline(a.n_dns, a.n_les, spinup=a.spinup, n_snap=a.n_snap,
+                   snap_every=a.snap_every, train_steps=a.train_steps, les_steps=a.les_steps)
+    line = json.dumps(out)
+    print(line)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(line + "\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -147,6 +147,16 @@ class TimeSteppingPseudoSpectral:
 
     def one_time_step(self):
         """``fluidsim/base/time_stepping/base.py:208-244``."""
+        forcing = getattr(self.sim, "forcing", None)
+        if forcing is not None:
+            # CFL first, then sim.forcing.compute() with that dt (base.py:210-213)
+            if self.params.time_stepping.USE_CFL:
+                vmax = self.sim.max_velocity()
+                o = self.sim.oper
+                tmp = sum(v / d for v, d in zip(vmax, (o.deltax, o.deltay, o.deltaz)))
+                self.deltat = self.sim._lib.gbs_cfl_update(self.deltat, tmp, self.CFL,
+                                                           self.deltat_max)
+            forcing.compute()
         if self.max_elapsed is not None and time() > self._time_should_stop:
             self._has_to_stop = True
         if self._stop_signal_received:
@@ -161,6 +171,8 @@ class TimeSteppingPseudoSpectral:
         pts = self.params.time_stepping
         dt = ctypes.c_double(self.deltat)
         cfl = (ctypes.c_double * 2)(self.CFL, self.deltat_max) if pts.USE_CFL else None
+        if getattr(self.sim, "forcing", None) is not None:
+            cfl = None  # dt already updated before the forcing was computed
         S = self.sim.state.state_spect
         flags = _lib.GBS_STEP_CHECK_NAN if self._nan_check else 0
         if self._dealiased_version is not None and S._version == self._dealiased_version:
@@ -239,7 +251,9 @@ class _SimulBase:
         TimeSteppingPseudoSpectral._complete_params_with_default(params)
         Output._complete_params_with_default(params)
         params._set_child("init_fields", attribs={"type": "in_script"})
-        params._set_child("forcing", attribs={"enable": False, "type": ""})
+        params._set_child("forcing", attribs={
+            "enable": False, "type": "", "forcing_rate": 1.0, "nkmin_forcing": 2,
+            "nkmax_forcing": 3, "seed": 0})
         cls._complete_params_with_default(params)
         return params
 
@@ -249,8 +263,8 @@ class _SimulBase:
 
     def __init__(self, params):
         self.params = params
-        if params.forcing.enable:
-            raise NotImplementedError("forcing is not implemented on GB300 yet")
+        if params.forcing.enable and (self.ndim != 3 or params.forcing.type != "tcrandom"):
+            raise NotImplementedError("forcing on GB300: ns3d with type 'tcrandom' only")
         if params.init_fields.type != "in_script":
             raise NotImplementedError("only init_fields.type = 'in_script' is supported")
         self._lib = _lib.load()
@@ -264,6 +278,7 @@ class _SimulBase:
                        "gbs_ns_create")
         self.time_stepping = TimeSteppingPseudoSpectral(self)
         self.is_forcing_enabled = False
+        self.forcing = None
 
     def __del__(self):
         lib = getattr(self, "_lib", None)
@@ -365,6 +380,12 @@ class SimulNS3D(_SimulBase):
         super().__init__(params)
         self.is_turb_model_enabled = False
         self._closure = None
+        if params.forcing.enable:
+            from .forcing import TCRandomForcing3D
+            pf = params.forcing
+            self.forcing = TCRandomForcing3D(self, pf.nkmin_forcing, pf.nkmax_forcing,
+                                             pf.forcing_rate, seed=pf.seed)
+            self.is_forcing_enabled = True
         tm = params.turb_model
         if tm.enable:
             if tm.type == "smagorinsky":

@@ -154,6 +154,79 @@ typedef struct gbs_mlp_weights {
 int gbs_ns_set_turb_model(gbs_ns* solver, int type, double C,
                           const gbs_mlp_weights* weights);
 
+/* Forcing added to the tendencies in every stage, before projection and
+ * dealiasing (`tendencies_fft += self.forcing.get_forcing()`,
+ * fluidsim/solvers/ns3d/solver.py:243-244, ns2d/solver.py:189-190):
+ * device pointer to nvar spectral fields owned by the caller and read at
+ * every stage (the caller updates it between steps, as
+ * sim.forcing.compute() does once per step); NULL disables. */
+int gbs_ns_set_forcing(gbs_ns* solver, const void* forcing);
+
+/* ------------------------------------------------ batched ns2d ensembles
+ * nruns independent ns2d runs of one grid (power-of-two nx/2, ny in
+ * 64..512), float32, advanced together: one launch per pass covers the
+ * whole batch, every run with its own nu_2, nu_8 and dt (host arrays of
+ * nruns).  The runs of fluidsim are independent simulations
+ * (fluidsim/solvers/ns2d/solver.py); there is no reference batching.
+ * gbs_ens2d_step enqueues nsteps RK4 steps of every run on `stream`
+ * without host synchronisation, so it can be captured in a CUDA graph;
+ * state: (nruns, ny, nx/2+1) complex64.  gbs_ens2d_set_tuning picks the
+ * compiled tile shapes (y-pass column widths 4/8/16, x-pass rows 1/2/4/8).
+ * gbs_ens2d_nan_flag reads and clears the flag set when a run's state holds
+ * a NaN (synchronises). */
+typedef struct gbs_ens2d gbs_ens2d;
+int gbs_ens2d_create(int64_t nx, int64_t ny, double Lx, double Ly, int64_t nruns,
+                     int64_t kcut_x, int64_t kcut_y, double beta, gbs_ens2d** ens);
+int gbs_ens2d_destroy(gbs_ens2d* ens);
+int gbs_ens2d_set_params(gbs_ens2d* ens, const double* nu_2, const double* nu_8,
+                         const double* dt);
+int gbs_ens2d_set_tuning(gbs_ens2d* ens, int tx_inverse, int rows_x,
+                         int tx_forward);
+int gbs_ens2d_step(gbs_ens2d* ens, void* state_spect, int nsteps, int flags,
+                   void* stream);
+int gbs_ens2d_nan_flag(gbs_ens2d* ens, int* flag);
+
+/* Filtered-DNS data for the learned closure (no reference counterpart):
+ *   gbs_spectral_resample: nfields spectral fields of shape_in (nz, ny, nx)
+ *     onto shape_out, keeping |k_a| < m_a / 2, multiplied by the top-hat
+ *     filter transfer prod_a sinc(k_a delta / 2) when delta > 0
+ *     (L = Lz, Ly, Lx);
+ *   gbs_products6: physical products (xx, yy, zz, xy, xz, yz) of 3 fields of
+ *     n points, or sub - products when sub != NULL;
+ *   gbs_velocity_gradients: 9 spectral fields 1j k_j v_i (index 3 i + j) of a
+ *     (3, nz, ny, nx/2+1) state, zero where |k_a| >= kcut_a (z, y, x). */
+int gbs_spectral_resample(const int64_t* shape_in, const int64_t* shape_out,
+                          int nfields, const double* L, double delta, int dtype,
+                          const void* in, void* out, void* stream);
+int gbs_products6(const void* u, void* out, int64_t n, const void* sub, int dtype,
+                  void* stream);
+int gbs_velocity_gradients(const int64_t* shape, const double* L,
+                           const int64_t* kcut, int dtype, const void* S,
+                           void* G, void* stream);
+
+/* Learned-closure network: inference and training (no reference
+ * counterpart; the reference's turbulence models are analytic).
+ * Fields are structure-of-arrays float32: g[c * ld + i] (9 rows, the
+ * velocity gradients d_j u_i with c = 3 i + j), tau[o * ld + i] (6 rows,
+ * xx yy zz xy xz yz).
+ *   gbs_mlp_forward: tau = MLP(g) for points 0..n-1.
+ *   gbs_mlp_grad: mean squared error of MLP(g) / out_scale against
+ *     tau / out_scale over the `batch` points idx[0..batch-1] (device int64),
+ *     its gradient w.r.t. the 5190 parameters (layout W1, b1, W2, b2, W3, b3)
+ *     into grad (device) and the loss into *loss (device); workspace of
+ *     gbs_mlp_grad_workspace(batch) bytes.  Deterministic.
+ *   gbs_mlp_adam: one Adam step on the FP32 master parameters (same layout)
+ *     with moments m, v; writes the BF16 copies W1, W2, W3 of w_bf16. */
+int64_t gbs_mlp_grad_workspace(int64_t batch);
+int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld,
+                    float* tau, int64_t n, void* stream);
+int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau,
+                 int64_t ld, const int64_t* idx, int64_t batch,
+                 void* workspace, float* grad, float* loss, void* stream);
+int gbs_mlp_adam(float* master, float* m, float* v, const float* grad,
+                 int64_t step, double lr, double beta1, double beta2,
+                 double eps, const gbs_mlp_weights* w_bf16, void* stream);
+
 /* max |u_i| over the physical grid of state_spect (ns2d: ux, uy; ns3d: vx,
  * vy, vz) into out[ndim] (host).  Synchronises the stream. */
 int gbs_ns_max_velocity(gbs_ns* solver, const void* state_spect, double* out,
