@@ -107,7 +107,7 @@ def _declare(lib):
         "gbs_mlp_forward": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, ctypes.c_int64, P,
                                            ctypes.c_int64, P]),
         "gbs_mlp_grad": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, P, ctypes.c_int64, P,
-                                        ctypes.c_int64, P, P, P, P]),
+                                        ctypes.c_int64, ctypes.c_double, P, P, P, P]),
         "gbs_mlp_adam": (ctypes.c_int, [P, P, P, P, ctypes.c_int64, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                         ctypes.POINTER(MLPWeights), P]),

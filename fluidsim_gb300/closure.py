@@ -101,8 +101,10 @@ class ClosureTrainer:
     """
 
     def __init__(self, net: ClosureMLP, batch=65536, lr=2e-3, betas=(0.9, 0.999),
-                 eps=1e-8, seed=0):
+                 eps=1e-8, seed=0, lambda_pi=0.0):
         self.net = net
+        self.lambda_pi = float(lambda_pi)
+        self.pi_weight = 0.0
         self.lib = _lib.load()
         self.batch = int(batch)
         self.lr, self.betas, self.eps = lr, betas, eps
@@ -118,15 +120,19 @@ class ClosureTrainer:
         self.gen.manual_seed(seed)
 
     def set_scales(self, G, Tau):
-        """Unit-variance inputs and outputs (per component)."""
+        """Unit-variance inputs and outputs (per component); the weight of
+        the dissipation term is lambda_pi / var(tau_ij S_ij)."""
         self.net.in_scale.copy_(1.0 / G.float().std(dim=1).clamp_min(1e-30))
         self.net.out_scale.copy_(Tau.float().std(dim=1).clamp_min(1e-30))
+        if self.lambda_pi > 0:
+            pi = subgrid_dissipation(G, Tau)
+            self.pi_weight = self.lambda_pi / max(float(pi.double().var()), 1e-300)
 
     def gradient(self, G, Tau, idx):
         w = self.net.c_weights()
         _lib.check(self.lib.gbs_mlp_grad(
             ctypes.byref(w), ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(Tau.data_ptr()),
-            G.shape[1], ctypes.c_void_p(idx.data_ptr()), idx.numel(),
+            G.shape[1], ctypes.c_void_p(idx.data_ptr()), idx.numel(), self.pi_weight,
             ctypes.c_void_p(self.ws.data_ptr()), ctypes.c_void_p(self.grad.data_ptr()),
             ctypes.c_void_p(self.loss.data_ptr()), current_stream_handle()), "gbs_mlp_grad")
         return self.grad, self.loss
@@ -151,6 +157,12 @@ class ClosureTrainer:
             if log_every and (it % log_every == 0 or it == steps - 1):
                 history.append((it, float(loss.item())))
         return history
+
+
+def subgrid_dissipation(G, Tau):
+    """tau_ij S_ij per point for (9, n) gradients and (6, n) stresses."""
+    return (G[0] * Tau[0] + G[4] * Tau[1] + G[8] * Tau[2] + (G[1] + G[3]) * Tau[3]
+            + (G[2] + G[6]) * Tau[4] + (G[5] + G[7]) * Tau[5])
 
 
 def predict(net: ClosureMLP, G):

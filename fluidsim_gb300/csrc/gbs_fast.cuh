@@ -232,6 +232,91 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
   for (int i = 0; i < 8; ++i) xc[jt + P::outm(i) * M8] = v[i];
 }
 
+// ------------------------------------------ pipelined (persistent) column pass
+// Asynchronous copies global -> shared (cp.async, L1-allocating); a copy with
+// src_size 0 writes zeros and reads nothing.
+template <typename C>
+__device__ __forceinline__ void cp_async_elem(C* smem, const C* gmem, bool valid) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  const int sz = valid ? (int)sizeof(C) : 0;
+  if (sizeof(C) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Same transform as kf_col, but each CTA walks over tiles (col tile fastest,
+// then outer block, then field) and prefetches the next tile into the other
+// of two staging buffers while it transforms the current one.  A thread
+// stages exactly its own stage-0 inputs (slot r * threads + tid), so it reads
+// them after its own wait_group; the staging buffer then serves as the
+// exchange buffer of run() once every thread has read it.
+template <typename T, int LOGN, int TX, int DIR>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf_colp(const cplx<T>* in, cplx<T>* out, ColArgs a, int ncol_tiles, int nouter, int ntiles,
+        const cplx<T>* __restrict__ tw, T scale) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  constexpr int NT = TX * P::N8;
+  C* const smem0 = reinterpret_cast<C*>(g_smem_fast);
+  auto stage = [&](int k) -> C* { return smem0 + k * (P::N * TX); };
+  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
+  auto locate = [&](int tile, int64_t& base, bool& valid) {
+    const int ct = tile % ncol_tiles;
+    const int rest = tile / ncol_tiles;
+    const int o = rest % nouter, z = rest / nouter;
+    const int col = ct * TX + c;
+    valid = col < a.ncols;
+    base = z * a.fs + o * a.os + col;
+  };
+  auto issue = [&](int tile, C* stg) {
+    int64_t base;
+    bool valid;
+    locate(tile, base, valid);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int p = jt + r * P::N8;
+      const bool ok = valid && kept(p, P::N, a.kc_in);
+      cp_async_elem(stg + r * NT + threadIdx.x, ok ? in + base + p * a.es : in, ok);
+    }
+    cp_async_commit();
+  };
+  int tile = blockIdx.x;
+  int b = 0;
+  if (tile < ntiles) issue(tile, stage(0));
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int next = tile + gridDim.x;
+    if (next < ntiles) {
+      issue(next, stage(b ^ 1));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    C v[8];
+#pragma unroll
+    C* buf = stage(b);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = buf[r * NT + threadIdx.x];
+    __syncthreads();
+    auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+    run<DIR, LOGN>(v, jt, true, acc, tw, 1);
+    int64_t base;
+    bool valid;
+    locate(tile, base, valid);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int p = jt + P::outm(i) * P::N8;
+        if (kept(p, P::N, a.kc_out)) out[base + p * a.es] = cscale(v[i], scale);
+      }
+    }
+    b ^= 1;
+  }
+}
+
 // ----------------------------------------------------- ns3d geometry
 struct Geo {
   int nx, ny, nz, nkx, M;

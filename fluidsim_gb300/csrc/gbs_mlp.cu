@@ -4,7 +4,10 @@
 //          -> h2 = tanh(W2 h1 + b2) (64) -> y = W3 h2 + b3 (6),
 //          tau = y * out_scale.  Weights are read as BF16, arithmetic and
 //          accumulation are FP32.  Loss: mean over samples and outputs of
-//          (y - tau_target / out_scale)^2.
+//          (y - tau_target / out_scale)^2, plus pi_weight times the mean over
+//          samples of (Pi(tau) - Pi(tau_target))^2 with the subgrid
+//          dissipation Pi(tau) = tau_ij S_ij, S_ij = (d_j u_i + d_i u_j) / 2
+//          (pointwise energy transfer to the unresolved scales).
 //
 // Data are structure-of-arrays fields: g[c * ld + i] (9 rows), tau[o * ld + i]
 // (6 rows), so the gradient and stress fields of the LES / filtered DNS are
@@ -49,10 +52,21 @@ __device__ __forceinline__ void load_weights(float* W1, float* b1, float* W2, fl
   if (threadIdx.x < kIn) sin[threadIdx.x] = w.in_scale[threadIdx.x];
 }
 
+// strain-rate component o (xx yy zz xy xz yz) of the gradient g[3 i + j],
+// times the multiplicity of tau_o in tau_ij S_ij (1 on the diagonal, 2 off)
+__device__ __forceinline__ void strain_weighted(const float* gr, float* s) {
+  s[0] = gr[0];
+  s[1] = gr[4];
+  s[2] = gr[8];
+  s[3] = gr[1] + gr[3];
+  s[4] = gr[2] + gr[6];
+  s[5] = gr[5] + gr[7];
+}
+
 __global__ void __launch_bounds__(256)
 k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict__ tau,
-              int64_t ld, const int64_t* __restrict__ idx, int64_t B, float* __restrict__ ws,
-              float* __restrict__ loss) {
+              int64_t ld, const int64_t* __restrict__ idx, int64_t B, float pi_weight,
+              float* __restrict__ ws, float* __restrict__ loss) {
   __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
   __shared__ float sin[kIn], sout[kOut];
   __shared__ float red[8];
@@ -60,14 +74,21 @@ k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict
   __syncthreads();
   float lsum = 0.f;
   const float inv = 2.f / (float)(B * kOut);
+  const float invB = 1.f / (float)B;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B;
        b += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = idx[b];
-    float x[kIn];
+    float x[kIn], sw[kOut];
+    {
+      float gr[kIn];
 #pragma unroll
-    for (int c = 0; c < kIn; ++c) {
-      x[c] = g[c * ld + i] * sin[c];
-      ws[(kRX + c) * B + b] = x[c];
+      for (int c = 0; c < kIn; ++c) gr[c] = g[c * ld + i];
+      strain_weighted(gr, sw);
+#pragma unroll
+      for (int c = 0; c < kIn; ++c) {
+        x[c] = gr[c] * sin[c];
+        ws[(kRX + c) * B + b] = x[c];
+      }
     }
     float h1[kH];
 #pragma unroll
@@ -92,11 +113,22 @@ k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict
       for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
     }
     float dy[kOut];
+    float dpi = 0.f;  // Pi(tau) - Pi(tau_target)
 #pragma unroll
     for (int o = 0; o < kOut; ++o) {
-      const float d = y[o] - tau[o * ld + i] / sout[o];
+      const float t = tau[o * ld + i];
+      const float d = y[o] - t / sout[o];
       lsum = fmaf(d, d, lsum);
       dy[o] = inv * d;
+      dpi = fmaf(sw[o], fmaf(y[o], sout[o], -t), dpi);
+    }
+    // the loss accumulates per output: the Pi term is folded in with weight
+    // kOut so that lsum / (B kOut) is the total loss
+    lsum = fmaf(pi_weight * (float)kOut * dpi, dpi, lsum);
+    const float cpi = 2.f * pi_weight * invB * dpi;
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) {
+      dy[o] = fmaf(cpi * sw[o], sout[o], dy[o]);
       ws[(kRDY + o) * B + b] = dy[o];
     }
     // dh1 = W2^T dz2, dz2 = (W3^T dy) * (1 - h2^2); h1 is reused as dh1
@@ -288,10 +320,11 @@ int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float*
 }
 
 int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau, int64_t ld,
-                 const int64_t* idx, int64_t batch, void* workspace, float* grad,
-                 float* loss, void* stream) {
+                 const int64_t* idx, int64_t batch, double pi_weight, void* workspace,
+                 float* grad, float* loss, void* stream) {
   gbs::clear_error();
-  if (!w || !g || !tau || !idx || batch < 1 || !workspace || !grad || !loss) {
+  if (!w || !g || !tau || !idx || batch < 1 || !workspace || !grad || !loss ||
+      !(pi_weight >= 0.0)) {
     gbs::set_error("gbs_mlp_grad: invalid argument");
     return GBS_EINVAL;
   }
@@ -302,7 +335,8 @@ int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau, int
   GBS_CUDA_TRY(cudaMemsetAsync(loss, 0, sizeof(float), st));
   int64_t g1 = (batch + 255) / 256;
   if (g1 > 152 * 8) g1 = 152 * 8;
-  gbs::k_mlp_fwd_bwd<<<(int)g1, 256, 0, st>>>(gbs::to_w(w), g, tau, ld, idx, batch, ws, loss);
+  gbs::k_mlp_fwd_bwd<<<(int)g1, 256, 0, st>>>(gbs::to_w(w), g, tau, ld, idx, batch,
+                                          (float)pi_weight, ws, loss);
   GBS_CHECK_LAUNCH();
   gbs::k_mlp_wgrad<<<nb, 256, 0, st>>>(ws, batch, partial);
   GBS_CHECK_LAUNCH();

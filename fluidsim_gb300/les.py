@@ -122,6 +122,10 @@ def filtered_data(snaps, n_dns, n_les):
                                                  ctypes.c_void_p(src.data_ptr()),
                                                  ctypes.c_void_p(dst.data_ptr()), st))
         del uu_k
+        # the LES represents only |k| < kcut: the effective filter is the box
+        # filter followed by the sharp truncation, applied to both terms of tau
+        sim_les.oper.dealiasing(ub_k)
+        sim_les.oper.dealiasing(uub_k)
         ub = torch.empty((3,) + les.shapeX, dtype=torch.float32, device="cuda")
         les.ifft_as_arg(ub_k, ub)
         uub = torch.empty((6,) + les.shapeX, dtype=torch.float32, device="cuda")
@@ -141,22 +145,21 @@ def filtered_data(snaps, n_dns, n_les):
         sim_les.state.state_spect.copy_(ub_k)
         specs.append(shell_spectrum(sim_les)[1])
         if first is None:
-            sim_les.oper.dealiasing(ub_k)
             first = ub_k.cpu().numpy()
     k = shell_spectrum(sim_les)[0]
     return torch.cat(Gs, dim=1).contiguous(), torch.cat(Ts, dim=1).contiguous(), (
         k, np.mean(specs, axis=0)), first
 
 
-def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, seed=0):
+def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, seed=0, lambda_pi=1.0):
     net = ClosureMLP(seed=seed)
-    tr = ClosureTrainer(net, batch=batch, lr=lr, seed=seed)
+    tr = ClosureTrainer(net, batch=batch, lr=lr, seed=seed, lambda_pi=lambda_pi)
     tr.set_scales(G, Tau)
     t0 = time.perf_counter()
     hist = tr.train(G, Tau, steps, log_every=max(steps // 10, 1))
     torch.cuda.synchronize()
     return net, {"history": hist, "train_s": time.perf_counter() - t0, "steps": steps,
-                 "batch": batch, "samples": int(G.shape[1])}
+                 "batch": batch, "samples": int(G.shape[1]), "lambda_pi": lambda_pi}
 
 
 def run_les(n, model, nu=3e-4, steps=2000, avg_last=1000, init=None, seed=0):
@@ -191,7 +194,7 @@ def spectral_error(k_les, E_les, k_ref, E_ref, kmin=1.0, kmax=None):
 
 
 def pipeline(n_dns=512, n_les=128, nu=3e-4, spinup=2000, n_snap=4, snap_every=200,
-             train_steps=3000, les_steps=2000, seed=0):
+             train_steps=3000, les_steps=2000, lambda_pi=1.0, seed=0):
     out = {"config": {"n_dns": n_dns, "n_les": n_les, "nu": nu, "forcing": "tcrandom k in [2,3], P=1",
                       "closure": "MLP 9-64-64-6 tanh, BF16 weights, FP32 accumulation"}}
     snaps, (k_dns, E_dns), st_dns = forced_dns(n_dns, nu, steps_spinup=spinup, n_snap=n_snap,
@@ -200,11 +203,16 @@ def pipeline(n_dns=512, n_les=128, nu=3e-4, spinup=2000, n_snap=4, snap_every=20
     G, Tau, (k_f, E_f), init_les = filtered_data(snaps, n_dns, n_les)
     del snaps
     torch.cuda.empty_cache()
-    net, st_train = train_closure(G, Tau, steps=train_steps, seed=seed)
+    net, st_train = train_closure(G, Tau, steps=train_steps, seed=seed, lambda_pi=lambda_pi)
     out["train"] = st_train
     from .closure import predict
     pred = predict(net, G)
     out["train"]["rel_mse"] = float(((pred - Tau) ** 2).mean() / (Tau**2).mean())
+    from .closure import subgrid_dissipation
+    pi_t, pi_p = subgrid_dissipation(G, Tau), subgrid_dissipation(G, pred)
+    out["train"]["mean_dissipation_target"] = float(pi_t.double().mean())
+    out["train"]["mean_dissipation_learned"] = float(pi_p.double().mean())
+    out["train"]["dissipation_corr"] = float(torch.corrcoef(torch.stack([pi_t, pi_p]).double())[0, 1])
     del G, Tau
     kc = cubic_dealias_cutoff(n_les, 2 * pi) - 1
     res = {}
@@ -230,10 +238,13 @@ def main():
     ap.add_argument("--snap-every", type=int, default=200)
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--les-steps", type=int, default=2000)
+    ap.add_argument("--nu", type=float, default=3e-4)
+    ap.add_argument("--lambda-pi", type=float, default=1.0)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
-    out = pipeline(a.n_dns, a.n_les, spinup=a.spinup, n_snap=a.n_snap,
-                   snap_every=a.snap_every, train_steps=a.train_steps, les_steps=a.les_steps)
+    out = pipeline(a.n_dns, a.n_les, nu=a.nu, spinup=a.spinup, n_snap=a.n_snap,
+                   snap_every=a.snap_every, train_steps=a.train_steps, les_steps=a.les_steps,
+                   lambda_pi=a.lambda_pi)
     line = json.dumps(out)
     print(line)
     if a.out:

@@ -210,10 +210,13 @@ int gbs_velocity_gradients(const int64_t* shape, const double* L,
  * velocity gradients d_j u_i with c = 3 i + j), tau[o * ld + i] (6 rows,
  * xx yy zz xy xz yz).
  *   gbs_mlp_forward: tau = MLP(g) for points 0..n-1.
- *   gbs_mlp_grad: mean squared error of MLP(g) / out_scale against
- *     tau / out_scale over the `batch` points idx[0..batch-1] (device int64),
- *     its gradient w.r.t. the 5190 parameters (layout W1, b1, W2, b2, W3, b3)
- *     into grad (device) and the loss into *loss (device); workspace of
+ *   gbs_mlp_grad: loss over the `batch` points idx[0..batch-1] (device
+ *     int64): mean squared error of MLP(g) / out_scale against
+ *     tau / out_scale, plus pi_weight (>= 0) times the mean of
+ *     (Pi(MLP(g)) - Pi(tau))^2 with the subgrid dissipation
+ *     Pi(t) = t_ij S_ij, S_ij = (d_j u_i + d_i u_j) / 2; its gradient w.r.t.
+ *     the 5190 parameters (layout W1, b1, W2, b2, W3, b3) into grad (device)
+ *     and the loss into *loss (device); workspace of
  *     gbs_mlp_grad_workspace(batch) bytes.  Deterministic.
  *   gbs_mlp_adam: one Adam step on the FP32 master parameters (same layout)
  *     with moments m, v; writes the BF16 copies W1, W2, W3 of w_bf16. */
@@ -222,7 +225,8 @@ int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld,
                     float* tau, int64_t n, void* stream);
 int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau,
                  int64_t ld, const int64_t* idx, int64_t batch,
-                 void* workspace, float* grad, float* loss, void* stream);
+                 double pi_weight, void* workspace, float* grad, float* loss,
+                 void* stream);
 int gbs_mlp_adam(float* master, float* m, float* v, const float* grad,
                  int64_t step, double lr, double beta1, double beta2,
                  double eps, const gbs_mlp_weights* w_bf16, void* stream);

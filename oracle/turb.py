@@ -10,7 +10,8 @@ Test infrastructure only (see ``oracle/__init__.py``).
   ``g[3*i + j] = d_j u_i`` giving the symmetric stress
   ``tau = (xx, yy, zz, xy, xz, yz)``; its forcing is ``-d_j tau_ij``.
   Forward and backward in float64 numpy, used to check the GPU kernels'
-  outputs and gradients.
+  outputs and gradients.  The training loss may add a term on the
+  pointwise subgrid dissipation ``tau_ij S_ij`` (no reference counterpart).
 """
 
 from math import sqrt
@@ -74,15 +75,21 @@ class MLPClosure:
             self._cache = (x, h1, h2)
         return y * self.out_scale
 
-    def loss_and_grads(self, g, target):
-        """Mean squared error on the scaled outputs and its gradients."""
+    def loss_and_grads(self, g, target, pi_weight=0.0):
+        """Mean squared error on the scaled outputs, plus ``pi_weight`` times
+        the mean squared error of the subgrid dissipation tau_ij S_ij, and
+        the gradients."""
         y = self.forward(g, keep=True) / self.out_scale
         t = target / self.out_scale
         x, h1, h2 = self._cache
         n = g.shape[0]
         d = y - t
-        loss = float((d**2).sum() / (n * 6))
-        dy = 2 * d / (n * 6)
+        # tau_ij S_ij = sum_o sw_o tau_o (off-diagonal terms counted twice)
+        sw = np.stack([g[:, 0], g[:, 4], g[:, 8], g[:, 1] + g[:, 3], g[:, 2] + g[:, 6],
+                       g[:, 5] + g[:, 7]], axis=1)
+        dpi = (sw * (y * self.out_scale - target)).sum(1)
+        loss = float((d**2).sum() / (n * 6) + pi_weight * (dpi**2).sum() / n)
+        dy = 2 * d / (n * 6) + 2 * pi_weight / n * dpi[:, None] * sw * self.out_scale
         gW3 = dy.T @ h2
         gb3 = dy.sum(0)
         dh2 = dy @ self.W3

@@ -32,16 +32,18 @@ def test_forward_matches_oracle(cuda):
     assert np.abs(tau - ref).max() / np.abs(ref).max() < 1e-5
 
 
-def test_gradient_matches_oracle(cuda):
+@pytest.mark.parametrize("pi_weight", [0.0, 0.05])
+def test_gradient_matches_oracle(cuda, pi_weight):
     import torch
     from fluidsim_gb300.closure import ClosureTrainer
     net, G, Tau = _net_and_data(5000, seed=1)
     tr = ClosureTrainer(net, batch=5000)
+    tr.pi_weight = pi_weight
     idx = torch.arange(5000, device="cuda", dtype=torch.int64)
     grad, loss = tr.gradient(G, Tau, idx)
     g64 = G.cpu().numpy().astype(np.float64).T
     t64 = Tau.cpu().numpy().astype(np.float64).T
-    ref_loss, ref = _oracle(net).loss_and_grads(g64, t64)
+    ref_loss, ref = _oracle(net).loss_and_grads(g64, t64, pi_weight=pi_weight)
     flat = np.concatenate([ref[k].ravel() for k in ("W1", "b1", "W2", "b2", "W3", "b3")])
     got = grad.cpu().numpy().astype(np.float64)
     assert abs(loss.item() - ref_loss) < 1e-5 * ref_loss
