@@ -63,6 +63,60 @@ __device__ __forceinline__ bool kept(int p, int n, int kc) {
   return p < kc || p > n - kc;
 }
 
+// exp(-2 pi i r / 16), r = 0..8: the x-pass pre/post-processing twiddle of
+// position jt + r M/8 of a 2M-point real line is tw[jt] times this factor.
+template <typename C>
+__device__ __forceinline__ C w16(int r) {
+  using R = decltype(C::x);
+  constexpr double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173;
+  constexpr double h = 0.70710678118654752440;
+  switch (r) {
+    case 0: return mk<C>(R(1), R(0));
+    case 1: return mk<C>(R(c1), R(-s1));
+    case 2: return mk<C>(R(h), R(-h));
+    case 3: return mk<C>(R(s1), R(-c1));
+    case 4: return mk<C>(R(0), R(-1));
+    case 5: return mk<C>(R(-s1), R(-c1));
+    case 6: return mk<C>(R(-h), R(-h));
+    case 7: return mk<C>(R(-c1), R(-s1));
+    default: return mk<C>(R(-1), R(0));
+  }
+}
+
+// Twiddle of position jt + r M/8 of the 2M-point table twx: FP32 derives it
+// from twx[jt] (one table read per line instead of eight; one rounding more),
+// FP64 reads the table.
+template <typename C>
+__device__ __forceinline__ C twx_at(const C* __restrict__ twx, C t0, int jt, int r, int M8) {
+  if constexpr (sizeof(C) == 8) return r == 0 ? t0 : cmul(t0, w16<C>(r));
+  else return twx[jt + r * M8];
+}
+
+// Stage twiddles w[r] = W^(r k) (conjugated for DIR = +1), r = 1..R-1.  FP32
+// forms the powers of w = W^k by products (one table read instead of R-1,
+// at most three roundings deep), which keeps the twiddle reads from taking
+// the L1 bandwidth the shared-memory exchanges need; FP64 reads the table.
+template <int DIR, int R, typename C>
+__device__ __forceinline__ void stage_twiddles(const C* __restrict__ tw, int k, C (&w)[8]) {
+  if constexpr (sizeof(C) == 8) {
+    const C w1 = twid<DIR>(tw, k);
+    w[1] = w1;
+    if (R > 2) {
+      w[2] = cmul(w1, w1);
+      w[3] = cmul(w[2], w1);
+    }
+    if (R > 4) {
+      w[4] = cmul(w[2], w[2]);
+      w[5] = cmul(w[4], w1);
+      w[6] = cmul(w[4], w[2]);
+      w[7] = cmul(w[4], w[3]);
+    }
+  } else {
+#pragma unroll
+    for (int r = 1; r < R; ++r) w[r] = twid<DIR>(tw, r * k);
+  }
+}
+
 // Stockham FFT of one line whose stage-0 inputs v[r] = x[jt + r N/8] are in
 // registers; `acc(p)` addresses position p of this line in shared memory.
 // Every thread of the CTA must call it (it contains barriers); `active`
@@ -89,10 +143,12 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
       if (s < P::S8) {
         const int bm = jt & (Nsn - 1);
         const int tm = (N / (Nsn * 8)) * tws;
+        C w[8];
+        stage_twiddles<DIR, 8>(tw, bm * tm, w);
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
           C x = acc(jt + r * N8);
-          if (r) x = cmul(x, twid<DIR>(tw, r * bm * tm));
+          if (r) x = cmul(x, w[r]);
           v[r] = x;
         }
         dft8<DIR>(v);
@@ -103,10 +159,12 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
         for (int g = 0; g < 8 / RL; ++g) {
           const int b = jt + g * N8;
           const int bm = b & (Nsn - 1);
+          C w[8];
+          stage_twiddles<DIR, RL>(tw, bm * tm, w);
 #pragma unroll
           for (int r = 0; r < RL; ++r) {
             C x = acc(b + r * (N / RL));
-            if (r) x = cmul(x, twid<DIR>(tw, r * bm * tm));
+            if (r) x = cmul(x, w[r]);
             v[g * RL + r] = x;
           }
           dftR<RL, DIR>(&v[g * RL]);
@@ -208,6 +266,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
   const int64_t row = (int64_t)blockIdx.x * L + l;
   const bool valid = row < nrows;
   const C* rowp = in + row * NKX;
+  const C t0 = twx[jt];
   C v[8];
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
@@ -218,7 +277,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
       C b = cconj(rowp[M - j]);
       if (j == 0) { a.y = 0; b.y = 0; }
       const C s = cadd(a, b), d = csub(a, b);
-      const C wd = cmulc(d, twx[j]);
+      const C wd = cmulc(d, twx_at(twx, t0, jt, r, M8));
       Z = mk<C>(s.x - wd.y, s.y + wd.x);
     }
     v[r] = Z;
@@ -230,91 +289,6 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
   C* xc = reinterpret_cast<C*>(x) + row * M;
 #pragma unroll
   for (int i = 0; i < 8; ++i) xc[jt + P::outm(i) * M8] = v[i];
-}
-
-// ------------------------------------------ pipelined (persistent) column pass
-// Asynchronous copies global -> shared (cp.async, L1-allocating); a copy with
-// src_size 0 writes zeros and reads nothing.
-template <typename C>
-__device__ __forceinline__ void cp_async_elem(C* smem, const C* gmem, bool valid) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  const int sz = valid ? (int)sizeof(C) : 0;
-  if (sizeof(C) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-// Same transform as kf_col, but each CTA walks over tiles (col tile fastest,
-// then outer block, then field) and prefetches the next tile into the other
-// of two staging buffers while it transforms the current one.  A thread
-// stages exactly its own stage-0 inputs (slot r * threads + tid), so it reads
-// them after its own wait_group; the staging buffer then serves as the
-// exchange buffer of run() once every thread has read it.
-template <typename T, int LOGN, int TX, int DIR>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
-kf_colp(const cplx<T>* in, cplx<T>* out, ColArgs a, int ncol_tiles, int nouter, int ntiles,
-        const cplx<T>* __restrict__ tw, T scale) {
-  using C = cplx<T>;
-  using P = Line<LOGN>;
-  constexpr int NT = TX * P::N8;
-  C* const smem0 = reinterpret_cast<C*>(g_smem_fast);
-  auto stage = [&](int k) -> C* { return smem0 + k * (P::N * TX); };
-  const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
-  auto locate = [&](int tile, int64_t& base, bool& valid) {
-    const int ct = tile % ncol_tiles;
-    const int rest = tile / ncol_tiles;
-    const int o = rest % nouter, z = rest / nouter;
-    const int col = ct * TX + c;
-    valid = col < a.ncols;
-    base = z * a.fs + o * a.os + col;
-  };
-  auto issue = [&](int tile, C* stg) {
-    int64_t base;
-    bool valid;
-    locate(tile, base, valid);
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int p = jt + r * P::N8;
-      const bool ok = valid && kept(p, P::N, a.kc_in);
-      cp_async_elem(stg + r * NT + threadIdx.x, ok ? in + base + p * a.es : in, ok);
-    }
-    cp_async_commit();
-  };
-  int tile = blockIdx.x;
-  int b = 0;
-  if (tile < ntiles) issue(tile, stage(0));
-  for (; tile < ntiles; tile += gridDim.x) {
-    const int next = tile + gridDim.x;
-    if (next < ntiles) {
-      issue(next, stage(b ^ 1));
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    C v[8];
-#pragma unroll
-    C* buf = stage(b);
-#pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = buf[r * NT + threadIdx.x];
-    __syncthreads();
-    auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
-    run<DIR, LOGN>(v, jt, true, acc, tw, 1);
-    int64_t base;
-    bool valid;
-    locate(tile, base, valid);
-    if (valid) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int p = jt + P::outm(i) * P::N8;
-        if (kept(p, P::N, a.kc_out)) out[base + p * a.es] = cscale(v[i], scale);
-      }
-    }
-    b ^= 1;
-  }
 }
 
 // ----------------------------------------------------- ns3d geometry
@@ -425,6 +399,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
+  const C t0 = twx[jt];
   {
     const C* rowp = W + f * nK + row * g.nkx;
 #pragma unroll
@@ -436,7 +411,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
         C b = (M - j) < kcx ? cconj(rowp[M - j]) : mk<C>(0, 0);
         if (j == 0) { a.y = 0; b.y = 0; }
         const C s = cadd(a, b), d = csub(a, b);
-        const C wd = cmulc(d, twx[j]);
+        const C wd = cmulc(d, twx_at(twx, t0, jt, r, M8));
         Z = mk<C>(s.x - wd.y, s.y + wd.x);
       }
       v[r] = Z;
@@ -485,7 +460,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
       C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
       const C s = cadd(a, b), d = csub(a, b);
-      const C wd = cmul(twx[k], d);
+      const C wd = cmul(r < 8 ? twx_at(twx, t0, jt, r, M8) : twx[M], d);
       Fo[k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
     }
   }
@@ -617,6 +592,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
+  const C t0 = twx[jt];
   {
     const C* rowp = W + f * nK + row * g.nkx;
 #pragma unroll
@@ -628,7 +604,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
         C b = (M - j) < kcx ? cconj(rowp[M - j]) : mk<C>(0, 0);
         if (j == 0) { a.y = 0; b.y = 0; }
         const C s = cadd(a, b), d = csub(a, b);
-        const C wd = cmulc(d, twx[j]);
+        const C wd = cmulc(d, twx_at(twx, t0, jt, r, M8));
         Z = mk<C>(s.x - wd.y, s.y + wd.x);
       }
       v[r] = Z;

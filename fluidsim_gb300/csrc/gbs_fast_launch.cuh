@@ -40,38 +40,19 @@ static int prep(K kernel, size_t smem) {
       return GBS_EINVAL;                              \
   }
 
-// number of SMs of the current device (cached per device)
-static int sm_count() {
-  static int cache[64] = {0};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-  if (!cache[dev]) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = n > 0 ? n : 152;
-  }
-  return cache[dev];
-}
-
 template <typename T, int LOGN, int DIR>
 static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, int nfields,
                       const void* tw, double scale, cudaStream_t st) {
   using C = cplx<T>;
   constexpr int TX = tx_cols<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX * 2;  // two staging tiles
-  auto kern = kf_colp<T, LOGN, TX, DIR>;
-  int rc = prep(kern, smem);
+  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
   if (rc) return rc;
-  const int nct = ceil_div(a.ncols, TX);
-  const int64_t ntiles = (int64_t)nct * nouter * nfields;
-  int per_sm = 0;
-  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TH, smem));
-  if (per_sm < 1) per_sm = 1;
-  int64_t grid = (int64_t)sm_count() * per_sm;
-  if (grid > ntiles) grid = ntiles;
-  kern<<<(int)grid, TH, smem, st>>>(static_cast<const C*>(in), static_cast<C*>(out), a, nct,
-                                   nouter, (int)ntiles, static_cast<const C*>(tw), T(scale));
+  dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
+  kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
+                                                 static_cast<C*>(out), a,
+                                                 static_cast<const C*>(tw), T(scale));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }

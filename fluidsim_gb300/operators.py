@@ -102,6 +102,41 @@ class _OperBase:
                     arr[..., self._where_dealiased_np.astype(bool)] = 0.0
 
 
+    # ----- spectra (FP64 accumulation on the device) -----
+    # Definitions from the mathematics (fluidfft's own binning is not
+    # available to compare against): an energy array over the half spectrum
+    # (x non-negative) is summed with the Hermitian weights (x modes other
+    # than 0 and nx/2 count twice) and divided by the bin width; a mode goes
+    # to bin round(|k| / dk).
+    def _hermitian_weights(self):
+        nkx = self.nx // 2 + 1
+        w = torch.full((nkx,), 2.0, dtype=torch.float64, device=self.device)
+        w[0] = 1.0
+        if self.nx % 2 == 0:
+            w[-1] = 1.0
+        return w
+
+    def _bin_sum(self, values, index, nbins):
+        out = torch.zeros(nbins, dtype=torch.float64, device=self.device)
+        index = index.clamp(max=nbins - 1).reshape(-1)
+        out.index_add_(0, index, values.reshape(-1))
+        return out
+
+    def create_arrayX_random(self, min_val=None, max_val=None, shape="loc"):
+        """Uniform random real array (``min_val`` 0, ``max_val`` 1 by default)."""
+        lo = 0.0 if min_val is None else float(min_val)
+        hi = 1.0 if max_val is None else float(max_val)
+        return lo + (hi - lo) * torch.rand(self.shapeX, dtype=self.rdtype, device=self.device)
+
+    def create_arrayK_random(self, min_val=None, max_val=None, shape="loc"):
+        """Complex array with uniform random real and imaginary parts."""
+        lo = 0.0 if min_val is None else float(min_val)
+        hi = 1.0 if max_val is None else float(max_val)
+        re = lo + (hi - lo) * torch.rand(self.shapeK, dtype=self.rdtype, device=self.device)
+        im = lo + (hi - lo) * torch.rand(self.shapeK, dtype=self.rdtype, device=self.device)
+        return torch.complex(re, im)
+
+
 class OperatorsPseudoSpectral2D(_OperBase):
     ndim = 2
 
@@ -178,6 +213,30 @@ class OperatorsPseudoSpectral2D(_OperBase):
     def get_XY_loc(self):
         Y, X = torch.meshgrid(self.y, self.x, indexing="ij")
         return X, Y
+
+    def projection_perp(self, fx_fft, fy_fft):
+        """In place: remove the part of (fx, fy) parallel to k (k = 0 kept)."""
+        tmp = (self.KX * fx_fft + self.KY * fy_fft) * self.inv_K_square_nozero
+        fx_fft.sub_(self.KX * tmp)
+        fy_fft.sub_(self.KY * tmp)
+
+    def compute_1dspectra(self, energy_fft):
+        """(E(kx), E(ky)) of an energy array: sums over the other axis,
+        divided by the bin width."""
+        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, :]
+        skx = e.sum(0) / self.deltakx
+        iky = torch.from_numpy(np.abs(_kadim(self.ny))).to(self.device)
+        sky = self._bin_sum(e.sum(1), iky, self.ny // 2 + 1) / self.deltaky
+        return skx, sky
+
+    def compute_2dspectrum(self, energy_fft):
+        """Shell-summed spectrum, bins round(|k| / dk), dk = min(dkx, dky)."""
+        dk = min(self.deltakx, self.deltaky)
+        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, :]
+        kk = torch.sqrt(self.KX.to(torch.float64) ** 2 + self.KY.to(torch.float64) ** 2)
+        idx = torch.floor(kk / dk + 0.5).to(torch.int64)
+        nb = int(max(self.nx, self.ny) // 2 + 1)
+        return self._bin_sum(e, idx, nb) / dk
 
     def produce_str_describing_oper(self):
         return f"{self.nx}x{self.ny}"
@@ -265,6 +324,83 @@ class OperatorsPseudoSpectral3D(_OperBase):
 
     def divfft_from_vecfft(self, vx_fft, vy_fft, vz_fft):
         return 1j * (self.Kx * vx_fft + self.Ky * vy_fft + self.Kz * vz_fft)
+
+    def gradfft_from_fft(self, f_fft):
+        return 1j * self.Kx * f_fft, 1j * self.Ky * f_fft, 1j * self.Kz * f_fft
+
+    def get_XYZ_loc(self):
+        z = torch.arange(self.nz, dtype=torch.float64, device=self.device) * self.deltaz
+        y = torch.arange(self.ny, dtype=torch.float64, device=self.device) * self.deltay
+        x = torch.arange(self.nx, dtype=torch.float64, device=self.device) * self.deltax
+        Z, Y, X = torch.meshgrid(z, y, x, indexing="ij")
+        return X, Y, Z
+
+    @staticmethod
+    def vector_product(ax, ay, az, bx, by, bz):
+        """a x b of physical fields."""
+        return ay * bz - az * by, az * bx - ax * bz, ax * by - ay * bx
+
+    def urudfft_from_vxvyfft(self, vx_fft, vy_fft):
+        """Toroidal (r) and poloidal (d) horizontal velocities,
+        ``operators3d.py:713-730``."""
+        kh2 = self.Kx**2 + self.Ky**2
+        kh2 = torch.where(kh2 == 0, torch.full_like(kh2, 1e-14), kh2)
+        inv = 1.0 / kh2
+        kdotu = self.Kx * vx_fft + self.Ky * vy_fft
+        udx = kdotu * self.Kx * inv
+        udy = kdotu * self.Ky * inv
+        return vx_fft - udx, vy_fft - udy, udx, udy
+
+    def build_invariant_arrayX_from_2d_indices12X(self, arr2d, oper2d=None):
+        """3D array constant along z from a (ny, nx) array."""
+        a = arr2d if isinstance(arr2d, torch.Tensor) else torch.from_numpy(np.asarray(arr2d))
+        return a.to(self.device).unsqueeze(0).expand((self.nz,) + tuple(a.shape)).contiguous()
+
+    def build_invariant_arrayK_from_2d_indices12X(self, arr2d):
+        """Spectral array of a field constant along z: the (ny, nx/2+1)
+        spectrum of the 2D field on the kz = 0 plane (the forward transform
+        is normalised by the number of points, so the plane carries the 2D
+        coefficients unchanged)."""
+        a = arr2d if isinstance(arr2d, torch.Tensor) else torch.from_numpy(np.asarray(arr2d))
+        out = torch.zeros(self.shapeK, dtype=self.cdtype, device=self.device)
+        out[0].copy_(a.to(self.device))
+        return out
+
+    def compute_1dspectra(self, energy_fft):
+        """(E(kx), E(ky), E(kz)) of an energy array: sums over the other
+        axes, |k| binned along y and z, divided by the bin width."""
+        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
+        skx = e.sum((0, 1)) / self.deltakx
+        iky = torch.from_numpy(np.abs(_kadim(self.ny))).to(self.device)
+        ikz = torch.from_numpy(np.abs(_kadim(self.nz))).to(self.device)
+        sky = self._bin_sum(e.sum((0, 2)), iky, self.ny // 2 + 1) / self.deltaky
+        skz = self._bin_sum(e.sum((1, 2)), ikz, self.nz // 2 + 1) / self.deltakz
+        return skx, sky, skz
+
+    def compute_3dspectrum(self, energy_fft):
+        """Shell-summed spectrum, bins round(|k| / dk), dk = min(dkx, dky, dkz)."""
+        dk = min(self.deltakx, self.deltaky, self.deltakz)
+        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
+        k = torch.sqrt(self.Kx.to(torch.float64) ** 2 + self.Ky.to(torch.float64) ** 2
+                       + self.Kz.to(torch.float64) ** 2)
+        idx = torch.floor(k / dk + 0.5).to(torch.int64)
+        nb = int(max(self.nx, self.ny, self.nz) // 2 + 1)
+        return self._bin_sum(e, idx, nb) / dk
+
+    def compute_spectrum_kzkh(self, energy_fft):
+        """2D spectrum over (|kz|, kh), kh = sqrt(kx^2 + ky^2), bins
+        round(|kz| / dkz) and round(kh / dkh), dkh = min(dkx, dky)."""
+        dkh = min(self.deltakx, self.deltaky)
+        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
+        kh = torch.sqrt(self.Kx.to(torch.float64) ** 2 + self.Ky.to(torch.float64) ** 2)
+        ih = torch.floor(kh / dkh + 0.5).to(torch.int64)
+        nh = int(max(self.nx, self.ny) // 2 + 1)
+        ih = ih.clamp(max=nh - 1)
+        iz = torch.from_numpy(np.abs(_kadim(self.nz))).to(self.device)[:, None, None]
+        nz = self.nz // 2 + 1
+        flat = (iz * nh + ih).expand(self.shapeK)
+        out = self._bin_sum(e, flat, nz * nh).reshape(nz, nh)
+        return out / (self.deltakz * dkh)
 
     def project_perpk3d(self, vx_fft, vy_fft, vz_fft):
         tmp = (self.Kx * vx_fft + self.Ky * vy_fft + self.Kz * vz_fft) * self.inv_K_square_nozero

@@ -23,8 +23,8 @@ def test_forcing_injects_the_requested_power(cuda):
 
 def test_pipeline_small_grid(cuda):
     from fluidsim_gb300 import les
-    out = les.pipeline(n_dns=64, n_les=32, nu=5e-3, spinup=100, n_snap=2, snap_every=50,
-                       train_steps=200, les_steps=100)
+    out = les.pipeline(n_dns=64, n_les=32, nu=5e-3, t_coarse=0.3, t_fine=0.1, n_snap=2,
+                       t_between=0.05, train_steps=200, les_steps=100)
     assert out["train"]["rel_mse"] < 1.0
     for name in ("none", "smagorinsky", "learned"):
         assert np.isfinite(out["les"][name]["spectral_error"])
