@@ -32,6 +32,7 @@ EXPORTED = (
     "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
     "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
+    "gbs_ns_is_dealiased",
 )
 
 
@@ -84,6 +85,7 @@ def _declare(lib):
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),
         "gbs_ns_spectrum_size": (ctypes.c_int, [P, I64P]),
         "gbs_ns_spectrum": (ctypes.c_int, [P, P, P, P]),
+        "gbs_ns_is_dealiased": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_int), P]),
         "gbs_ns_timing": (ctypes.c_int, [P, ctypes.c_int]),
         "gbs_ns_timing_report": (ctypes.c_int, [P, DP, I64P, ctypes.c_int, I64P]),
         "gbs_fft_c2r_noalloc": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.c_int,

@@ -150,12 +150,19 @@ class ClosureTrainer:
             ctypes.byref(w), current_stream_handle()), "gbs_mlp_adam")
         return self.loss
 
-    def train(self, G, Tau, steps, log_every=0):
+    def train(self, G, Tau, steps, log_every=0, lr_final=None):
+        """``steps`` Adam steps; with ``lr_final`` the learning rate decays
+        from ``lr`` to ``lr_final`` on a cosine."""
+        from math import cos, pi
         history = []
+        lr0 = self.lr
         for it in range(steps):
+            if lr_final is not None:
+                self.lr = lr_final + 0.5 * (lr0 - lr_final) * (1 + cos(pi * it / max(steps, 1)))
             loss = self.step(G, Tau)
             if log_every and (it % log_every == 0 or it == steps - 1):
                 history.append((it, float(loss.item())))
+        self.lr = lr0
         return history
 
 

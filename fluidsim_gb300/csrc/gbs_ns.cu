@@ -884,6 +884,27 @@ static int64_t spectrum_bins(const Solver* s) {
   return (int64_t)floor(kmax / dk + 0.5) + 1;
 }
 
+// flag = 1 if a removed mode of any field is not +0 (bitwise)
+template <typename T>
+__global__ void k_removed_nonzero(const cplx<T>* __restrict__ S, NSK q, int nvar,
+                                  int* __restrict__ flag) {
+  const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  bool nz = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % q.nkx);
+    const int64_t r = i / q.nkx;
+    const int iy = (int)(r % q.ny), iz = (int)(r / q.ny);
+    const int kz = q.nz > 1 ? kadim(iz, q.nz) : 0;
+    if (!removed(q, ix, kadim(iy, q.ny), kz)) continue;
+    for (int f = 0; f < nvar; ++f) {
+      const cplx<T> v = S[i + f * nK];
+      nz = nz || v.x != T(0) || v.y != T(0) || signbit(v.x) || signbit(v.y);
+    }
+  }
+  if (__syncthreads_or(nz) && threadIdx.x == 0) *flag = 1;
+}
+
 template <typename T>
 __global__ void k_spectrum(const cplx<T>* __restrict__ S, NSK q, int ndim,
                            double dk, int64_t nbins, double* spec) {
@@ -1228,6 +1249,31 @@ int gbs_ns_timing_report(gbs_ns* h, double* ms, int64_t* count, int nkinds,
     if (count) count[k] = s->t_count[k];
   }
   if (launches) *launches = s->launches;
+  return GBS_OK;
+}
+
+int gbs_ns_is_dealiased(gbs_ns* h, const void* S, int* out, void* stream) {
+  gbs::clear_error();
+  if (!h || !S || !out) {
+    gbs::set_error("gbs_ns_is_dealiased: null argument");
+    return GBS_EINVAL;
+  }
+  gbs::Solver* s = &h->s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
+  if (s->p.dtype == GBS_F64)
+    gbs::k_removed_nonzero<double><<<gbs::kRedBlocks * 4, gbs::kRedThreads, 0, st>>>(
+        static_cast<const double2*>(S), s->q, s->nvar, s->dflag);
+  else
+    gbs::k_removed_nonzero<float><<<gbs::kRedBlocks * 4, gbs::kRedThreads, 0, st>>>(
+        static_cast<const float2*>(S), s->q, s->nvar, s->dflag);
+  GBS_CHECK_LAUNCH();
+  ++s->launches;
+  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf + 5, s->dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  int flag;
+  memcpy(&flag, s->hbuf + 5, sizeof(int));
+  *out = flag ? 0 : 1;
   return GBS_OK;
 }
 

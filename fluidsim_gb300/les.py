@@ -201,12 +201,13 @@ def filtered_data(snaps, n_dns, n_les):
         k, np.mean(specs, axis=0)), first
 
 
-def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, seed=0, lambda_pi=1.0):
+def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, lr_final=1e-4, seed=0,
+                  lambda_pi=1.0):
     net = ClosureMLP(seed=seed)
     tr = ClosureTrainer(net, batch=batch, lr=lr, seed=seed, lambda_pi=lambda_pi)
     tr.set_scales(G, Tau)
     t0 = time.perf_counter()
-    hist = tr.train(G, Tau, steps, log_every=max(steps // 10, 1))
+    hist = tr.train(G, Tau, steps, log_every=max(steps // 10, 1), lr_final=lr_final)
     torch.cuda.synchronize()
     return net, {"history": hist, "train_s": time.perf_counter() - t0, "steps": steps,
                  "batch": batch, "samples": int(G.shape[1]), "lambda_pi": lambda_pi}

@@ -177,6 +177,15 @@ class TimeSteppingPseudoSpectral:
         flags = _lib.GBS_STEP_CHECK_NAN if self._nan_check else 0
         if self._dealiased_version is not None and S._version == self._dealiased_version:
             flags |= _lib.GBS_STEP_DEALIASED
+        else:
+            # a state set through torch: prune only if it is exactly zero
+            # outside the 2/3 box (then the pruned step is bit-identical)
+            ok = ctypes.c_int()
+            _lib.check(self.sim._lib.gbs_ns_is_dealiased(
+                self.sim._solver, ctypes.c_void_p(S.data_ptr()), ctypes.byref(ok),
+                current_stream_handle()), "gbs_ns_is_dealiased")
+            if ok.value:
+                flags |= _lib.GBS_STEP_DEALIASED
         rc = self.sim._lib.gbs_ns_step_rk4(
             self.sim._solver, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt), cfl,
             flags, current_stream_handle())

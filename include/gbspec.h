@@ -269,6 +269,14 @@ int gbs_ns_spectrum_size(gbs_ns* solver, int64_t* nk);
 int gbs_ns_spectrum(gbs_ns* solver, const void* state_spect, double* spectrum,
                     void* stream);
 
+/* *out = 1 when every mode that the 2/3 truncation removes is +0 (all bits
+ * zero) in every field of state_spect, else 0; synchronises the stream.  A
+ * step may then be called with GBS_STEP_DEALIASED and gives exactly the
+ * unpruned result (no reference counterpart: the reference has no pruned
+ * passes; the truncation is dealiasing_setofvar, operators3d.py:38-59). */
+int gbs_ns_is_dealiased(gbs_ns* solver, const void* state_spect, int* out,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

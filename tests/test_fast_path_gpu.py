@@ -115,3 +115,54 @@ def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl):
     orc.init_from_rotfft(rot)
     orc.run(it_end=5)
     assert rel(sim.state.state_spect.cpu().numpy(), orc.state_spect) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+def test_pruned_step_is_bit_identical_and_detected(cuda, precision):
+    """gbs_ns_is_dealiased accepts only states that are +0 outside the 2/3
+    box; on such a state the pruned step equals the unpruned one bit for
+    bit."""
+    import ctypes
+    import torch
+    from fluidsim_gb300 import _lib
+    from fluidsim_gb300.fft import current_stream_handle
+    from fluidsim_gb300.init_fields import isotropic_3d
+    from fluidsim_gb300.solvers import SimulNS3D
+    n = 64
+    p = SimulNS3D.create_default_params()
+    p.precision = precision
+    p.oper.nx = p.oper.ny = p.oper.nz = n
+    p.nu_2 = 1e-3
+    sim = SimulNS3D(p)
+    v0 = isotropic_3d(n, n, n, seed=5)
+    sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2])
+    sim.oper.dealiasing(sim.state.state_spect)
+    lib, h = sim._lib, sim._solver
+
+    def is_dealiased(S):
+        ok = ctypes.c_int()
+        _lib.check(lib.gbs_ns_is_dealiased(h, ctypes.c_void_p(S.data_ptr()), ctypes.byref(ok),
+                                           current_stream_handle()))
+        return ok.value
+
+    def step(S, flags):
+        dt = ctypes.c_double(2e-3)
+        _lib.check(lib.gbs_ns_step_rk4(h, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt),
+                                       None, flags, current_stream_handle()))
+
+    S = sim.state.state_spect
+    assert is_dealiased(S) == 1
+    a, b = S.clone(), S.clone()
+    step(a, 0)
+    step(b, _lib.GBS_STEP_DEALIASED)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(a), torch.view_as_real(b))
+    # a removed mode that is not +0 (a value, or -0.0) is detected
+    kc = sim.oper.kcut[2]
+    c = S.clone()
+    c[1, 0, 0, kc] = 1e-30
+    assert is_dealiased(c) == 0
+    c[1, 0, 0, kc] = complex(-0.0, 0.0)
+    assert is_dealiased(c) == 0
+    c[1, 0, 0, kc] = 0
+    assert is_dealiased(c) == 1
