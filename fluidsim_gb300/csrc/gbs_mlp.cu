@@ -22,6 +22,7 @@
 
 #include "gbs_internal.cuh"
 #include "gbs_turb.h"
+#include "gbs_mlp_eval.cuh"
 
 namespace gbs {
 
@@ -34,23 +35,6 @@ constexpr int kRX = 0, kRH1 = kIn, kRH2 = kRH1 + kH, kRZ1 = kRH2 + kH, kRZ2 = kR
               kRDY = kRZ2 + kH;
 constexpr int kChunk = 2048;  // samples per block in the weight-gradient reduction
 constexpr int kTile = 32;
-
-__device__ __forceinline__ void load_weights(float* W1, float* b1, float* W2, float* b2,
-                                             float* W3, float* b3, float* sin, float* sout,
-                                             const MLPWeights& w) {
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) W2[i] = __bfloat162float(w.W2[i]);
-  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) W1[i] = __bfloat162float(w.W1[i]);
-  for (int i = threadIdx.x; i < kOut * kH; i += blockDim.x) W3[i] = __bfloat162float(w.W3[i]);
-  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-    b1[i] = w.b1[i];
-    b2[i] = w.b2[i];
-  }
-  if (threadIdx.x < kOut) {
-    b3[threadIdx.x] = w.b3[threadIdx.x];
-    sout[threadIdx.x] = w.out_scale[threadIdx.x];
-  }
-  if (threadIdx.x < kIn) sin[threadIdx.x] = w.in_scale[threadIdx.x];
-}
 
 // strain-rate component o (xx yy zz xy xz yz) of the gradient g[3 i + j],
 // times the multiplicity of tau_o in tau_ij S_ij (1 on the diagonal, 2 off)
@@ -67,18 +51,18 @@ __global__ void __launch_bounds__(256)
 k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict__ tau,
               int64_t ld, const int64_t* __restrict__ idx, int64_t B, float pi_weight,
               float* __restrict__ ws, float* __restrict__ loss) {
-  __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
-  __shared__ float sin[kIn], sout[kOut];
+  __shared__ MLPShared sm;
   __shared__ float red[8];
-  load_weights(W1, b1, W2, b2, W3, b3, sin, sout, w);
+  mlp_stage(sm, w);
   __syncthreads();
   float lsum = 0.f;
   const float inv = 2.f / (float)(B * kOut);
   const float invB = 1.f / (float)B;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B;
        b += (int64_t)gridDim.x * blockDim.x) {
+    const int o = opaque_zero();  // keeps the weight reads inside the loop
     const int64_t i = idx[b];
-    float x[kIn], sw[kOut];
+    float x[kInPad], sw[kOut];
     {
       float gr[kIn];
 #pragma unroll
@@ -86,64 +70,89 @@ k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict
       strain_weighted(gr, sw);
 #pragma unroll
       for (int c = 0; c < kIn; ++c) {
-        x[c] = gr[c] * sin[c];
+        x[c] = gr[c] * sm.sin[c];
         ws[(kRX + c) * B + b] = x[c];
       }
+#pragma unroll
+      for (int c = kIn; c < kInPad; ++c) x[c] = 0.f;
     }
     float h1[kH];
 #pragma unroll
     for (int j = 0; j < kH; ++j) {
-      float z = b1[j];
+      float z = sm.b1[j + o];
 #pragma unroll
-      for (int c = 0; c < kIn; ++c) z = fmaf(W1[j * kIn + c], x[c], z);
+      for (int q = 0; q < kInPad / 4; ++q) {
+        const float4 wv = sm.W1[j * (kInPad / 4) + q + o];
+        z = fmaf(wv.x, x[4 * q], z);
+        z = fmaf(wv.y, x[4 * q + 1], z);
+        z = fmaf(wv.z, x[4 * q + 2], z);
+        z = fmaf(wv.w, x[4 * q + 3], z);
+      }
       h1[j] = tanhf(z);
       ws[(kRH1 + j) * B + b] = h1[j];
     }
-    float y[kOut];
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) y[o] = b3[o];
-#pragma unroll 4
+    float4 ya = make_float4(sm.b3[0], sm.b3[1], sm.b3[2], sm.b3[3]);
+    float4 yb = make_float4(sm.b3[4], sm.b3[5], 0.f, 0.f);
+#pragma unroll 2
     for (int j = 0; j < kH; ++j) {
-      float z = b2[j];
+      float z = sm.b2[j + o];
 #pragma unroll
-      for (int c = 0; c < kH; ++c) z = fmaf(W2[j * kH + c], h1[c], z);
+      for (int q = 0; q < kH / 4; ++q) {
+        const float4 wv = sm.W2[j * (kH / 4) + q + o];
+        z = fmaf(wv.x, h1[4 * q], z);
+        z = fmaf(wv.y, h1[4 * q + 1], z);
+        z = fmaf(wv.z, h1[4 * q + 2], z);
+        z = fmaf(wv.w, h1[4 * q + 3], z);
+      }
       const float h2 = tanhf(z);
       ws[(kRH2 + j) * B + b] = h2;
-#pragma unroll
-      for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
+      ya = fma4(h2, sm.W3t[2 * j + o], ya);
+      yb = fma4(h2, sm.W3t[2 * j + 1 + o], yb);
     }
+    const float y[kOut] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y};
     float dy[kOut];
     float dpi = 0.f;  // Pi(tau) - Pi(tau_target)
 #pragma unroll
-    for (int o = 0; o < kOut; ++o) {
-      const float t = tau[o * ld + i];
-      const float d = y[o] - t / sout[o];
+    for (int q = 0; q < kOut; ++q) {
+      const float t = tau[q * ld + i];
+      const float d = y[q] - t / sm.sout[q];
       lsum = fmaf(d, d, lsum);
-      dy[o] = inv * d;
-      dpi = fmaf(sw[o], fmaf(y[o], sout[o], -t), dpi);
+      dy[q] = inv * d;
+      dpi = fmaf(sw[q], fmaf(y[q], sm.sout[q], -t), dpi);
     }
     // the loss accumulates per output: the Pi term is folded in with weight
     // kOut so that lsum / (B kOut) is the total loss
     lsum = fmaf(pi_weight * (float)kOut * dpi, dpi, lsum);
     const float cpi = 2.f * pi_weight * invB * dpi;
 #pragma unroll
-    for (int o = 0; o < kOut; ++o) {
-      dy[o] = fmaf(cpi * sw[o], sout[o], dy[o]);
-      ws[(kRDY + o) * B + b] = dy[o];
+    for (int q = 0; q < kOut; ++q) {
+      dy[q] = fmaf(cpi * sw[q], sm.sout[q], dy[q]);
+      ws[(kRDY + q) * B + b] = dy[q];
     }
     // dh1 = W2^T dz2, dz2 = (W3^T dy) * (1 - h2^2); h1 is reused as dh1
 #pragma unroll
     for (int c = 0; c < kH; ++c) h1[c] = 0.f;
-#pragma unroll 4
+#pragma unroll 2
     for (int j = 0; j < kH; ++j) {
+      const float4 wa = sm.W3t[2 * j + o], wb = sm.W3t[2 * j + 1 + o];
       float dh2 = 0.f;
-#pragma unroll
-      for (int o = 0; o < kOut; ++o) dh2 = fmaf(W3[o * kH + j], dy[o], dh2);
+      dh2 = fmaf(wa.x, dy[0], dh2);
+      dh2 = fmaf(wa.y, dy[1], dh2);
+      dh2 = fmaf(wa.z, dy[2], dh2);
+      dh2 = fmaf(wa.w, dy[3], dh2);
+      dh2 = fmaf(wb.x, dy[4], dh2);
+      dh2 = fmaf(wb.y, dy[5], dh2);
       const float h2 = ws[(kRH2 + j) * B + b];
       const float dz2 = dh2 * (1.f - h2 * h2);
       ws[(kRZ2 + j) * B + b] = dz2;
 #pragma unroll
-      for (int c = 0; c < kH; ++c) h1[c] = fmaf(W2[j * kH + c], dz2, h1[c]);
+      for (int q = 0; q < kH / 4; ++q) {
+        const float4 wv = sm.W2[j * (kH / 4) + q + o];
+        h1[4 * q] = fmaf(wv.x, dz2, h1[4 * q]);
+        h1[4 * q + 1] = fmaf(wv.y, dz2, h1[4 * q + 1]);
+        h1[4 * q + 2] = fmaf(wv.z, dz2, h1[4 * q + 2]);
+        h1[4 * q + 3] = fmaf(wv.w, dz2, h1[4 * q + 3]);
+      }
     }
 #pragma unroll
     for (int c = 0; c < kH; ++c) {
@@ -152,7 +161,7 @@ k_mlp_fwd_bwd(MLPWeights w, const float* __restrict__ g, const float* __restrict
     }
   }
   // block reduction of the loss (fixed order inside the block)
-  for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  for (int q = 16; q; q >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, q);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lsum;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -242,42 +251,21 @@ __global__ void k_adam(float* __restrict__ master, float* __restrict__ m, float*
   else if (p >= kOffW3 && p < kOffB3) W3[p - kOffW3] = __float2bfloat16(w);
 }
 
-// inference on SoA fields (float)
-template <typename T>
+// inference on SoA fields (float), gbs_mlp_eval.cuh
 __global__ void __launch_bounds__(256)
-k_mlp_forward(MLPWeights w, const T* __restrict__ g, int64_t ld, T* __restrict__ tau,
+k_mlp_forward(MLPWeights w, const float* __restrict__ g, int64_t ld, float* __restrict__ tau,
               int64_t n) {
-  __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
-  __shared__ float sin[kIn], sout[kOut];
-  load_weights(W1, b1, W2, b2, W3, b3, sin, sout, w);
+  __shared__ MLPShared sm;
+  mlp_stage(sm, w);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float x[kIn];
+    float x[kIn], y[kOut];
 #pragma unroll
-    for (int c = 0; c < kIn; ++c) x[c] = (float)g[c * ld + i] * sin[c];
-    float h1[kH];
+    for (int c = 0; c < kIn; ++c) x[c] = g[c * ld + i];
+    mlp_eval(sm, x, y);
 #pragma unroll
-    for (int j = 0; j < kH; ++j) {
-      float z = b1[j];
-#pragma unroll
-      for (int c = 0; c < kIn; ++c) z = fmaf(W1[j * kIn + c], x[c], z);
-      h1[j] = tanhf(z);
-    }
-    float y[kOut];
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) y[o] = b3[o];
-#pragma unroll 4
-    for (int j = 0; j < kH; ++j) {
-      float z = b2[j];
-#pragma unroll
-      for (int c = 0; c < kH; ++c) z = fmaf(W2[j * kH + c], h1[c], z);
-      const float h2 = tanhf(z);
-#pragma unroll
-      for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
-    }
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) tau[o * ld + i] = T(y[o] * sout[o]);
+    for (int o = 0; o < kOut; ++o) tau[o * ld + i] = y[o];
   }
 }
 
@@ -314,7 +302,7 @@ int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float*
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int64_t nb = (n + 255) / 256;
   if (nb > 152 * 16) nb = 152 * 16;
-  gbs::k_mlp_forward<float><<<(int)nb, 256, 0, st>>>(gbs::to_w(w), g, ld, tau, n);
+  gbs::k_mlp_forward<<<(int)nb, 256, 0, st>>>(gbs::to_w(w), g, ld, tau, n);
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }

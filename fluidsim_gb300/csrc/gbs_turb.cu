@@ -18,6 +18,7 @@
 
 #include "gbs_internal.cuh"
 #include "gbs_turb.h"
+#include "gbs_mlp_eval.cuh"
 
 namespace gbs {
 
@@ -76,52 +77,22 @@ __global__ void k_smagorinsky(const T* __restrict__ g, T* __restrict__ tau, int6
 }
 
 // Pointwise MLP 9 -> 64 -> 64 -> 6 (tanh), BF16 weights staged in shared
-// memory as float, FP32 accumulation.  One point per thread.
+// memory as float, FP32 accumulation (gbs_mlp_eval.cuh).  One point per
+// thread.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mlp_closure(const T* __restrict__ g, T* __restrict__ tau, int64_t n, MLPWeights w) {
-  __shared__ float W1[kH * kIn], b1[kH], W2[kH * kH], b2[kH], W3[kOut * kH], b3[kOut];
-  __shared__ float sin[kIn], sout[kOut];
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) W2[i] = __bfloat162float(w.W2[i]);
-  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) W1[i] = __bfloat162float(w.W1[i]);
-  for (int i = threadIdx.x; i < kOut * kH; i += blockDim.x) W3[i] = __bfloat162float(w.W3[i]);
-  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-    b1[i] = w.b1[i];
-    b2[i] = w.b2[i];
-  }
-  if (threadIdx.x < kOut) {
-    b3[threadIdx.x] = w.b3[threadIdx.x];
-    sout[threadIdx.x] = w.out_scale[threadIdx.x];
-  }
-  if (threadIdx.x < kIn) sin[threadIdx.x] = w.in_scale[threadIdx.x];
+  __shared__ MLPShared sm;
+  mlp_stage(sm, w);
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float x[kIn];
+    float x[kIn], y[kOut];
 #pragma unroll
-    for (int c = 0; c < kIn; ++c) x[c] = (float)g[i + c * n] * sin[c];
-    float h1[kH];
+    for (int c = 0; c < kIn; ++c) x[c] = (float)g[i + c * n];
+    mlp_eval(sm, x, y);
 #pragma unroll
-    for (int j = 0; j < kH; ++j) {
-      float z = b1[j];
-#pragma unroll
-      for (int c = 0; c < kIn; ++c) z = fmaf(W1[j * kIn + c], x[c], z);
-      h1[j] = tanhf(z);
-    }
-    float y[kOut];
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) y[o] = b3[o];
-#pragma unroll 4
-    for (int j = 0; j < kH; ++j) {
-      float z = b2[j];
-#pragma unroll
-      for (int c = 0; c < kH; ++c) z = fmaf(W2[j * kH + c], h1[c], z);
-      const float h2 = tanhf(z);
-#pragma unroll
-      for (int o = 0; o < kOut; ++o) y[o] = fmaf(W3[o * kH + j], h2, y[o]);
-    }
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) tau[i + o * n] = T(y[o] * sout[o]);
+    for (int o = 0; o < kOut; ++o) tau[i + o * n] = T(y[o]);
   }
 }
 
