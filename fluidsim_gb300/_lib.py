@@ -32,8 +32,9 @@ EXPORTED = (
     "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
     "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
-    "gbs_ns_is_dealiased",
+    "gbs_ns_is_dealiased", "gbs_ns_step",
 )
+SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3}
 
 
 class NSParams(ctypes.Structure):
@@ -80,6 +81,7 @@ def _declare(lib):
         "gbs_ns_destroy": (ctypes.c_int, [P]),
         "gbs_ns_tendencies": (ctypes.c_int, [P, P, P, P]),
         "gbs_ns_step_rk4": (ctypes.c_int, [P, P, DP, DP, ctypes.c_int, P]),
+        "gbs_ns_step": (ctypes.c_int, [P, ctypes.c_int, P, DP, DP, ctypes.c_int, P]),
         "gbs_ns_max_velocity": (ctypes.c_int, [P, P, DP, P]),
         "gbs_cfl_update": (ctypes.c_double, [ctypes.c_double] * 4),
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),

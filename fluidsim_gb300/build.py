@@ -35,7 +35,8 @@ def _needs_rebuild(obj, src):
     stamp = obj.with_suffix(".flags")
     if not stamp.exists() or stamp.read_text() != os.environ.get("GBS_NVCC_FLAGS", ""):
         return True
-    deps = [src] + list(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "gbspec.h"]
+    deps = ([src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+            + [HERE.parent / "include" / "gbspec.h"])
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps)
 
 

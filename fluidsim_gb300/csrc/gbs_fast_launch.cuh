@@ -7,8 +7,20 @@
 namespace gbs {
 namespace fast {
 
-// columns per CTA for the strided passes: 64 B segments in FP32 and FP64
-template <typename T> constexpr int tx_cols() { return sizeof(T) == 4 ? 8 : 4; }
+// columns per CTA for the strided passes: 64 B segments in FP32 and FP64;
+// FP32 widths per pass are compile-time knobs (A/B at 512^3)
+#ifndef GBS_TX_COL
+#define GBS_TX_COL 8
+#endif
+#ifndef GBS_TX_INVZ
+#define GBS_TX_INVZ 8
+#endif
+#ifndef GBS_TX_FWDZ
+#define GBS_TX_FWDZ 8
+#endif
+template <typename T> constexpr int tx_cols() { return sizeof(T) == 4 ? GBS_TX_COL : 4; }
+template <typename T> constexpr int tx_invz() { return sizeof(T) == 4 ? GBS_TX_INVZ : 4; }
+template <typename T> constexpr int tx_fwdz() { return sizeof(T) == 4 ? GBS_TX_FWDZ : 4; }
 // rows per CTA for the x passes
 template <typename T, int LOGM, int NF> constexpr int rows_x() {
   constexpr int M8 = (1 << LOGM) / 8;
@@ -116,7 +128,7 @@ int c2r_rows(int nx, const void* k, void* x, int64_t nrows, const void* twx, cud
 template <typename T, int LOGN>
 static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T>();
+  constexpr int TX = tx_invz<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf3_inv_z<T, LOGN, TX>, smem);
@@ -162,7 +174,7 @@ template <typename T, int LOGN>
 static int C3_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
                      cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T>();
+  constexpr int TX = tx_fwdz<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)3 * (1 << LOGN) * TX;
   int rc = prep(kf3_fwd_z<T, LOGN, TX>, smem);

@@ -223,47 +223,7 @@ k3_fwd_z_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
 #pragma unroll
       for (int f = 0; f < 3; ++f) N[f] = cadd(N[f], static_cast<const C*>(a.add)[i + f * nK]);
     }
-    // project_perpk3d: N -= k (k.N)/|k|^2 ; k = 0 untouched
-    if (!k0) {
-      const T inv = T(1) / k2;
-      C t = mk<C>((kx * N[0].x + ky * N[1].x + kz * N[2].x) * inv,
-                  (kx * N[0].y + ky * N[1].y + kz * N[2].y) * inv);
-      N[0] = csub(N[0], cscale(t, kx));
-      N[1] = csub(N[1], cscale(t, ky));
-      N[2] = csub(N[2], cscale(t, kz));
-    }
-    if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
-    if (mode == kTend) {
-      C* o = static_cast<C*>(a.tend);
-#pragma unroll
-      for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
-    } else if (mode == kRK3) {
-      const C* tmp = static_cast<const C*>(a.tmp);
-      const T c6 = T(a.dt) / T(6);
-      C Sn[3];
-#pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        C t = tmp[i + f * nK];
-        Sn[f] = mk<C>(t.x + c6 * N[f].x, t.y + c6 * N[f].y);
-      }
-      if (!k0) {
-        const T inv = T(1) / k2;
-        C t = mk<C>((kx * Sn[0].x + ky * Sn[1].x + kz * Sn[2].x) * inv,
-                    (kx * Sn[0].y + ky * Sn[1].y + kz * Sn[2].y) * inv);
-        Sn[0] = csub(Sn[0], cscale(t, kx));
-        Sn[1] = csub(Sn[1], cscale(t, ky));
-        Sn[2] = csub(Sn[2], cscale(t, kz));
-      }
-      if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
-      C* So = static_cast<C*>(a.Sout);
-#pragma unroll
-      for (int f = 0; f < 3; ++f) So[i + f * nK] = Sn[f];
-      if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
-    } else {
-      const T sig = freq_lin<T>(phys(q), k2, k0);
-#pragma unroll
-      for (int f = 0; f < 3; ++f) rk_update<C, T>(mode, a, i + f * nK, N[f], sig);
-    }
+    stage_epilogue3<C, T>(mode, a, i, nK, N, kx, ky, kz, k2, k0, rm, phys(q));
   }
 }
 
@@ -385,23 +345,10 @@ k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
     const int64_t i = (int64_t)iy * q.nkx + ix;
     const int kyi = kadim(iy, q.ny);
     const bool rm = removed(q, ix, kyi, 0);
-    C N = cscale(buf[iy * LP + c], inv_n);
-    if (rm) N = mk<C>(0, 0);
-    if (mode == kTend) {
-      static_cast<C*>(a.tend)[i] = N;
-    } else if (mode == kRK3) {
-      const C t = static_cast<const C*>(a.tmp)[i];
-      const T c6 = T(a.dt) / T(6);
-      C Sn = mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
-      if (rm) Sn = mk<C>(0, 0);
-      static_cast<C*>(a.Sout)[i] = Sn;
-      if (isnan(Sn.x) || isnan(Sn.y)) atomicOr(a.nan_flag, 1);
-    } else {
-      const T kx = T(q.dkx * ix), ky = T(q.dky * kyi);
-      const T k2 = kx * kx + ky * ky;
-      const T sig = freq_lin<T>(phys(q), k2, ix == 0 && kyi == 0);
-      rk_update<C, T>(mode, a, i, N, sig);
-    }
+    const C N = cscale(buf[iy * LP + c], inv_n);
+    const T kx = T(q.dkx * ix), ky = T(q.dky * kyi);
+    stage_epilogue1<C, T>(mode, a, i, N, kx * kx + ky * ky, ix == 0 && kyi == 0, rm,
+                          phys(q));
   }
 }
 
@@ -723,11 +670,44 @@ static double cfl_tmp(const Solver* s, const double* m) {
   return t;
 }
 
+// The stages of one time step of each scheme: the evaluation input (S or
+// the intermediate state written by the previous stage) and the epilogue
+// mode.  pseudo_spect.py: RK4 798-984, Euler 245-280, RK2 469-517,
+// RK2_trapezoid 519-569.
+struct Stage {
+  int input;  // 0: S, 1: tmp, 2: tmp1
+  int mode;
+};
+static int scheme_stages(int scheme, Stage* st) {
+  switch (scheme) {
+    case GBS_SCHEME_RK4:
+      st[0] = {0, kRK0}; st[1] = {2, kRK1}; st[2] = {2, kRK2}; st[3] = {2, kRK3};
+      return 4;
+    case GBS_SCHEME_EULER:
+      st[0] = {0, kEuler};
+      return 1;
+    case GBS_SCHEME_RK2:
+      st[0] = {0, kR2a}; st[1] = {1, kR2b};
+      return 2;
+    case GBS_SCHEME_RK2_TRAPEZOID:
+      st[0] = {0, kHeunA}; st[1] = {1, kHeunB};
+      return 2;
+    default:
+      return 0;
+  }
+}
+
 template <typename T>
-static int step(Solver* s, void* S, double* dt, const double* cfl, int flags,
+static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, int flags,
                 cudaStream_t st) {
   const int check_nan = flags & GBS_STEP_CHECK_NAN;
   const bool pr = (flags & GBS_STEP_DEALIASED) != 0;
+  Stage stages[4];
+  const int nst = scheme_stages(scheme, stages);
+  if (nst == 0) {
+    set_error("unknown time scheme");
+    return GBS_EINVAL;
+  }
   RKArgs a{};
   a.S = S;
   a.Sout = S;
@@ -737,23 +717,19 @@ static int step(Solver* s, void* S, double* dt, const double* cfl, int flags,
   int rc;
   if (cfl) GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
   if (check_nan) GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
-  rc = eval<T>(s, S, kRK0, a, cfl != nullptr, st, pr);
-  if (rc) return rc;
-  if (cfl) {
-    GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
-                                 cudaMemcpyDeviceToHost, st));
-    GBS_CUDA_TRY(cudaStreamSynchronize(st));
-    *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
-  }
-  a.dt = *dt;
-  rc = turb_stage<T>(s, S, a, st);
-  if (rc) return rc;
-  rc = finish<T>(s, kRK0, a, st, pr);
-  if (rc) return rc;
-  for (int m = kRK1; m <= kRK3; ++m) {
-    rc = eval<T>(s, s->tmp1, m, a, false, st, pr);
+  for (int k = 0; k < nst; ++k) {
+    const void* in = stages[k].input == 0 ? S : (stages[k].input == 1 ? s->tmp : s->tmp1);
+    const int m = stages[k].mode;
+    rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr);
     if (rc) return rc;
-    rc = turb_stage<T>(s, s->tmp1, a, st);
+    if (k == 0 && cfl) {
+      GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st));
+      GBS_CUDA_TRY(cudaStreamSynchronize(st));
+      *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
+    }
+    a.dt = *dt;
+    rc = turb_stage<T>(s, in, a, st);
     if (rc) return rc;
     rc = finish<T>(s, m, a, st, pr);
     if (rc) return rc;
@@ -1108,20 +1084,26 @@ int gbs_ns_tendencies(gbs_ns* h, const void* S, void* tend, void* stream) {
   return gbs::tendencies<float>(&h->s, S, tend, st);
 }
 
-int gbs_ns_step_rk4(gbs_ns* h, void* S, double* dt, const double* cfl,
-                    int flags, void* stream) {
+int gbs_ns_step(gbs_ns* h, int scheme, void* S, double* dt, const double* cfl, int flags,
+                void* stream) {
   gbs::clear_error();
-  if (!h || !S || !dt || !(*dt > 0)) {
-    gbs::set_error("gbs_ns_step_rk4: invalid argument");
+  if (!h || !S || !dt || !(*dt > 0) || scheme < GBS_SCHEME_RK4 ||
+      scheme > GBS_SCHEME_RK2_TRAPEZOID) {
+    gbs::set_error("gbs_ns_step: invalid argument");
     return GBS_EINVAL;
   }
   if (cfl && (!(cfl[0] > 0) || !(cfl[1] > 0))) {
-    gbs::set_error("gbs_ns_step_rk4: invalid CFL parameters");
+    gbs::set_error("gbs_ns_step: invalid CFL parameters");
     return GBS_EINVAL;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (h->s.p.dtype == GBS_F64) return gbs::step<double>(&h->s, S, dt, cfl, flags, st);
-  return gbs::step<float>(&h->s, S, dt, cfl, flags, st);
+  if (h->s.p.dtype == GBS_F64) return gbs::step<double>(&h->s, scheme, S, dt, cfl, flags, st);
+  return gbs::step<float>(&h->s, scheme, S, dt, cfl, flags, st);
+}
+
+int gbs_ns_step_rk4(gbs_ns* h, void* S, double* dt, const double* cfl,
+                    int flags, void* stream) {
+  return gbs_ns_step(h, GBS_SCHEME_RK4, S, dt, cfl, flags, stream);
 }
 
 int gbs_ns_max_velocity(gbs_ns* h, const void* S, double* out, void* stream) {

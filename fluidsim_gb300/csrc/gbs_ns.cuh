@@ -8,12 +8,22 @@
 
 namespace gbs {
 
-// RK4 stage selector for the last pass of a tendency evaluation.
-enum Mode { kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4 };
+// Stage selector for the last pass of a tendency evaluation: the plain
+// tendency, the four RK4 stages, forward Euler, the two RK2 stages and the
+// two RK2_trapezoid (Heun) stages of TimeSteppingPseudoSpectral.  Final
+// stages write the new state (projected, dealiased, NaN-checked).
+enum Mode {
+  kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4,
+  kEuler = 5, kR2a = 6, kR2b = 7, kHeunA = 8, kHeunB = 9
+};
+
+__device__ __forceinline__ bool final_stage(int mode) {
+  return mode == kRK3 || mode == kEuler || mode == kR2b || mode == kHeunB;
+}
 
 struct RKArgs {
-  const void* S;  // state (read) for kRK0..kRK2
-  void* Sout;     // state (write) for kRK3
+  const void* S;  // state (read) for the stages that use S_0
+  void* Sout;     // state (write) for the final stages
   void* tmp;      // _state_spect_tmp
   void* tmp1;     // _state_spect_tmp1
   void* tend;     // output for kTend
@@ -48,8 +58,37 @@ __device__ __forceinline__ T freq_lin(const Phys& q, T k2, bool k0) {
 __device__ __forceinline__ double dexp(double x) { return exp(x); }
 __device__ __forceinline__ float dexp(float x) { return expf(x); }
 
-// RK4 stage update at one mode, pseudo_spect.py:898-984 (same evaluation
-// order as the numpy expressions there).
+// New state of a final stage at one mode, before projection and
+// dealiasing (same evaluation order as the numpy expressions):
+//   kRK3   tmp + dt/6 N3                         pseudo_spect.py:984
+//   kEuler (S + dt N) E                          pseudo_spect.py:51-60,279
+//   kR2b   S E + dt E2 N                         pseudo_spect.py:63-67,517
+//   kHeunB tmp1 + dt/2 N, tmp1 = (S + dt/2 N0) E pseudo_spect.py:567-569
+template <typename C, typename T>
+__device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C N, T sigma) {
+  const T dt = T(a.dt);
+  if (mode == kRK3) {
+    const C t = static_cast<const C*>(a.tmp)[i];
+    const T c6 = dt / T(6);
+    return mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
+  }
+  if (mode == kHeunB) {
+    const C t = static_cast<const C*>(a.tmp1)[i];
+    const T c2 = dt / T(2);
+    return mk<C>(t.x + c2 * N.x, t.y + c2 * N.y);
+  }
+  const C S = static_cast<const C*>(a.S)[i];
+  const T E = dexp(-dt * sigma);
+  if (mode == kEuler) return cscale(mk<C>(S.x + dt * N.x, S.y + dt * N.y), E);
+  // kR2b
+  const T E2 = dexp(-dt / T(2) * sigma);
+  const T c1 = dt * E2;
+  return mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+}
+
+// Intermediate stage update at one mode (RK4: pseudo_spect.py:898-984;
+// RK2 first stage: 505-512; RK2_trapezoid first stage: 559-567), same
+// evaluation order as the numpy expressions there.
 template <typename C, typename T>
 __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
                                          C N, T sigma) {
@@ -76,6 +115,17 @@ __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
     C t = tmp[i];
     tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
     tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  } else if (mode == kR2a) {
+    const C S = static_cast<const C*>(a.S)[i];
+    const T E2 = dexp(-dt / T(2) * sigma);
+    const T c2 = dt / T(2);
+    tmp[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
+  } else if (mode == kHeunA) {
+    const C S = static_cast<const C*>(a.S)[i];
+    const T E = dexp(-dt * sigma);
+    const T c2 = dt / T(2);
+    tmp[i] = cscale(mk<C>(S.x + dt * N.x, S.y + dt * N.y), E);
+    tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E);
   }
 }
 
@@ -105,15 +155,11 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
     C* o = static_cast<C*>(a.tend);
 #pragma unroll
     for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
-  } else if (mode == kRK3) {
-    const C* tmp = static_cast<const C*>(a.tmp);
-    const T c6 = T(a.dt) / T(6);
+  } else if (final_stage(mode)) {
+    const T sig = (mode == kEuler || mode == kR2b) ? freq_lin<T>(q, k2, k0) : T(0);
     C Sn[3];
 #pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      C t = tmp[i + f * nK];
-      Sn[f] = mk<C>(t.x + c6 * N[f].x, t.y + c6 * N[f].y);
-    }
+    for (int f = 0; f < 3; ++f) Sn[f] = final_value<C, T>(mode, a, i + f * nK, N[f], sig);
     project3(Sn, kx, ky, kz, k2, k0);
     if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
     C* So = static_cast<C*>(a.Sout);
@@ -135,10 +181,9 @@ __device__ __forceinline__ void stage_epilogue1(int mode, const RKArgs& a, int64
   if (rm) N = mk<C>(0, 0);
   if (mode == kTend) {
     static_cast<C*>(a.tend)[i] = N;
-  } else if (mode == kRK3) {
-    const C t = static_cast<const C*>(a.tmp)[i];
-    const T c6 = T(a.dt) / T(6);
-    C Sn = mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
+  } else if (final_stage(mode)) {
+    const T sig = (mode == kEuler || mode == kR2b) ? freq_lin<T>(q, k2, k0) : T(0);
+    C Sn = final_value<C, T>(mode, a, i, N, sig);
     if (rm) Sn = mk<C>(0, 0);
     static_cast<C*>(a.Sout)[i] = Sn;
     if (isnan(Sn.x) || isnan(Sn.y)) atomicOr(a.nan_flag, 1);

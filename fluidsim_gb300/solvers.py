@@ -8,9 +8,10 @@ with the spatial means), so solver scripts written for
 
 * ``fluidsim/solvers/ns2d/solver.py:111-194`` / ``ns3d/solver.py:180-263``
   -> ``Simul.tendencies_nonlin`` (fused kernels, ``gbs_ns_tendencies``);
-* ``fluidsim/base/time_stepping/pseudo_spect.py:798-984`` (RK4 with exact
-  integrating factor) + ``one_time_step_computation`` (236-243, ns3d
-  ``time_stepping.py:8-20``) -> ``gbs_ns_step_rk4``;
+* ``fluidsim/base/time_stepping/pseudo_spect.py`` time schemes with exact
+  integrating factor (RK4 798-984, Euler 245-280, RK2 469-517,
+  RK2_trapezoid 519-569) + ``one_time_step_computation`` (236-243, ns3d
+  ``time_stepping.py:8-20``) -> ``gbs_ns_step``;
 * ``fluidsim/base/time_stepping/base.py:182-354`` (loop, CFL with the 2 %
   hysteresis, ``max_elapsed``, SIGUSR2 stop) -> ``TimeSteppingPseudoSpectral``;
 * spatial means / spectra (FP64 device reductions).
@@ -86,7 +87,8 @@ class StatePseudoSpectral:
 
 
 class TimeSteppingPseudoSpectral:
-    """RK4 pseudo-spectral time stepping with the reference loop semantics."""
+    """Pseudo-spectral time stepping (RK4, RK2, RK2_trapezoid, Euler) with the
+    reference loop semantics."""
 
     @staticmethod
     def _complete_params_with_default(params):
@@ -104,11 +106,17 @@ class TimeSteppingPseudoSpectral:
         self.t = 0.0
         self._has_to_stop = False
         self._stop_signal_received = False
-        if pts.type_time_scheme != "RK4":
+        if pts.type_time_scheme not in _lib.SCHEMES:
             raise NotImplementedError(
-                f"type_time_scheme {pts.type_time_scheme!r}: only RK4 runs on GB300")
+                f"type_time_scheme {pts.type_time_scheme!r}: GB300 runs "
+                + ", ".join(_lib.SCHEMES))
+        self._scheme = _lib.SCHEMES[pts.type_time_scheme]
         if pts.USE_CFL:
-            self.CFL = pts.cfl_coef if pts.cfl_coef is not None else 1.0
+            # base.py:249-260: default coefficient 0.4 for RK2*/Euler*, 1 for RK4
+            if pts.cfl_coef is not None:
+                self.CFL = pts.cfl_coef
+            else:
+                self.CFL = 1.0 if pts.type_time_scheme.startswith("RK4") else 0.4
         self.deltat = pts.deltat0
         self.deltat_max = pts.deltat_max
         self._nan_check = True
@@ -167,7 +175,8 @@ class TimeSteppingPseudoSpectral:
         self.it += 1
 
     def one_time_step_computation(self):
-        """RK4 + projection (ns3d) + dealiasing + NaN check, one library call."""
+        """One step of the scheme + projection (ns3d) + dealiasing + NaN
+        check, one library call."""
         pts = self.params.time_stepping
         dt = ctypes.c_double(self.deltat)
         cfl = (ctypes.c_double * 2)(self.CFL, self.deltat_max) if pts.USE_CFL else None
@@ -186,9 +195,9 @@ class TimeSteppingPseudoSpectral:
                 current_stream_handle()), "gbs_ns_is_dealiased")
             if ok.value:
                 flags |= _lib.GBS_STEP_DEALIASED
-        rc = self.sim._lib.gbs_ns_step_rk4(
-            self.sim._solver, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt), cfl,
-            flags, current_stream_handle())
+        rc = self.sim._lib.gbs_ns_step(
+            self.sim._solver, self._scheme, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt),
+            cfl, flags, current_stream_handle())
         self.deltat = dt.value
         self._dealiased_version = S._version
         self.sim.state._phys = None

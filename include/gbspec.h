@@ -108,7 +108,7 @@ int gbs_ns_destroy(gbs_ns* solver);
 int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
                       void* stream);
 
-/* flags of gbs_ns_step_rk4 */
+/* flags of gbs_ns_step / gbs_ns_step_rk4 */
 #define GBS_STEP_CHECK_NAN 1 /* check state_spect[0] for NaN (synchronises)  */
 #define GBS_STEP_DEALIASED 2 /* state_spect is zero at every mode removed by
                                 the truncation (true after any completed
@@ -129,6 +129,18 @@ int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
  * result is the same, the transforms skip the modes the 2/3 rule zeroes. */
 int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
                     const double* cfl, int flags, void* stream);
+
+/* Time schemes of TimeSteppingPseudoSpectral (params.time_stepping
+ * .type_time_scheme), all with the exact integrating factor. */
+#define GBS_SCHEME_RK4 0            /* _time_step_RK4, pseudo_spect.py:798-984 */
+#define GBS_SCHEME_EULER 1          /* _time_step_Euler, 245-280             */
+#define GBS_SCHEME_RK2 2            /* _time_step_RK2, 469-517               */
+#define GBS_SCHEME_RK2_TRAPEZOID 3  /* _time_step_RK2_trapezoid, 519-569     */
+
+/* One step of `scheme`, otherwise as gbs_ns_step_rk4 (same flags, CFL rule,
+ * projection, dealiasing and NaN check). */
+int gbs_ns_step(gbs_ns* solver, int scheme, void* state_spect, double* dt,
+                const double* cfl, int flags, void* stream);
 
 /* Turbulence model added to the ns3d tendencies before projection and
  * dealiasing, in every stage (fluidsim/solvers/ns3d/solver.py:246-249,

@@ -9,7 +9,7 @@ The following reference files are executed unmodified, loaded with
 bypassed because it needs fluiddyn/h5py/matplotlib, which are absent):
 
 * ``fluidsim/base/time_stepping/base.py``          (loop, CFL, hysteresis)
-* ``fluidsim/base/time_stepping/pseudo_spect.py``  (ExactLinearCoefs, RK4)
+* ``fluidsim/base/time_stepping/pseudo_spect.py``  (ExactLinearCoefs, RK4, RK2, RK2_trapezoid, Euler)
 * ``fluidsim/base/solvers/pseudo_spect.py``        (compute_freq_diss)
 * ``fluidsim/base/state.py``                       (StatePseudoSpectral)
 * ``fluidsim/base/setofvariables.py``
@@ -244,13 +244,13 @@ def load_reference(root):
 
 
 def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
-            extra):
+            extra, type_time_scheme="RK4"):
     p = _Container(nu_2=nu_2, nu_4=nu_4, nu_8=nu_8, nu_m4=nu_m4)
     p.__dict__.update(extra)
     p.forcing = _Container(enable=False)
     p.time_stepping = _Container(
         USE_T_END=False, t_end=10.0, it_end=10, USE_CFL=USE_CFL,
-        type_time_scheme="RK4", deltat0=deltat0, deltat_max=deltat_max,
+        type_time_scheme=type_time_scheme, deltat0=deltat0, deltat_max=deltat_max,
         cfl_coef=cfl_coef, max_elapsed=None,
     )
     return p
@@ -258,12 +258,12 @@ def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
 
 def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, beta=0.0, USE_CFL=False, deltat0=0.2,
-              deltat_max=0.2, cfl_coef=None):
-    """A reference ns2d ``Simul`` (RK4) wired around ``oper``."""
+              deltat_max=0.2, cfl_coef=None, type_time_scheme="RK4"):
+    """A reference ns2d ``Simul`` wired around ``oper``."""
     Simul = mods["ns2d_solver"].Simul
     sim = object.__new__(Simul)
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
-                         deltat_max, cfl_coef, {"beta": beta})
+                         deltat_max, cfl_coef, {"beta": beta}, type_time_scheme)
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
     mods["ns2d_state"].StateNS2D._complete_info_solver(info.solver)
     sim.info = info
@@ -279,13 +279,14 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
 
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
-              cfl_coef=None, smagorinsky_C=None):
-    """A reference ns3d ``Simul`` (RK4) wired around ``oper``."""
+              cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4"):
+    """A reference ns3d ``Simul`` wired around ``oper``."""
     Simul = mods["ns3d_solver"].Simul
     sim = object.__new__(Simul)
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
                          deltat_max, cfl_coef,
-                         {"f": f, "no_vz_kz0": False, "projection": None})
+                         {"f": f, "no_vz_kz0": False, "projection": None},
+                         type_time_scheme)
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
     mods["ns3d_state"].StateNS3D._complete_info_solver(info.solver)
     sim.info = info

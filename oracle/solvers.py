@@ -43,14 +43,24 @@ class _SolverBase:
     ``fluidsim/base/time_stepping/base.py:248-354``; loop 182-244.
     """
 
+    SCHEMES = ("RK4", "RK2", "Euler", "RK2_trapezoid")
+
     def __init__(self, oper, nu_2=0.0, nu_4=0.0, nu_8=0.0, nu_m4=0.0,
-                 deltat0=0.2, deltat_max=0.2, USE_CFL=False, cfl_coef=None):
+                 deltat0=0.2, deltat_max=0.2, USE_CFL=False, cfl_coef=None,
+                 type_time_scheme="RK4"):
+        if type_time_scheme not in self.SCHEMES:
+            raise ValueError(f"time scheme {type_time_scheme!r} not in the oracle")
+        self.type_time_scheme = type_time_scheme
         self.oper = oper
         self.nu_2, self.nu_4, self.nu_8, self.nu_m4 = nu_2, nu_4, nu_8, nu_m4
         f_d, f_d_hypo = compute_freq_diss(oper, nu_2, nu_4, nu_8, nu_m4)
         self.freq_lin = f_d + f_d_hypo
         self.USE_CFL = USE_CFL
-        self.CFL = cfl_coef if cfl_coef is not None else 1.0
+        # base.py:249-260: default coefficient 0.4 for RK2*/Euler*, 1 for RK4
+        if cfl_coef is not None:
+            self.CFL = cfl_coef
+        else:
+            self.CFL = 1.0 if type_time_scheme.startswith("RK4") else 0.4
         self.deltat = deltat0
         self.deltat_max = deltat_max
         self.dt_old = None
@@ -95,6 +105,39 @@ class _SolverBase:
         tmp1 = S * diss + dt * diss2 * N2
         N3 = self.tendencies_nonlin(tmp1)
         S[:] = tmp + dt / 6 * N3
+
+    def time_step_Euler(self):
+        """``pseudo_spect.py:245-280`` (``step_Euler_inplace``, 51-60)."""
+        dt = self.deltat
+        diss = self._coefs()[0]
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        S[:] = (S + dt * N0) * diss
+
+    def time_step_RK2(self):
+        """``pseudo_spect.py:469-517`` (``step_Euler`` 51-56, ``step_like_RK2``
+        63-67)."""
+        dt = self.deltat
+        diss, diss2 = self._coefs()
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        S12 = (S + dt / 2 * N0) * diss2
+        N12 = self.tendencies_nonlin(S12)
+        S[:] = S * diss + dt * diss2 * N12
+
+    def time_step_RK2_trapezoid(self):
+        """``pseudo_spect.py:519-569``."""
+        dt = self.deltat
+        diss = self._coefs()[0]
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        S1 = (S + dt * N0) * diss
+        N1 = self.tendencies_nonlin(S1)
+        S[:] = (S + dt / 2 * N0) * diss + dt / 2 * N1
+
+    def time_step(self):
+        """``_init_time_scheme`` dispatch, ``pseudo_spect.py:191-231``."""
+        getattr(self, "time_step_" + self.type_time_scheme)()
 
     def one_time_step(self):
         """``base.py:208-244`` without outputs, forcing or signals."""
@@ -164,7 +207,7 @@ class NS2DOracle(_SolverBase):
 
     def one_time_step_computation(self):
         """``pseudo_spect.py:236-243``."""
-        self.time_step_RK4()
+        self.time_step()
         self.oper.dealiasing(self.state_spect[0])
         self.statephys_from_statespect()
         if np.isnan(np.sum(self.state_spect[0])):
@@ -266,7 +309,7 @@ class NS3DOracle(_SolverBase):
 
     def one_time_step_computation(self):
         """``ns3d/time_stepping.py:8-20``."""
-        self.time_step_RK4()
+        self.time_step()
         self.project_state_spect(self.state_spect)
         self.oper.dealiasing(self.state_spect)
         self.statephys_from_statespect()

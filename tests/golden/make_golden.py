@@ -39,6 +39,12 @@ CASES_2D = [
     dict(name="ns2d_256_c1", nx=256, ny=256, Lx=2 * pi, Ly=2 * pi, nu_2=1e-4,
          USE_CFL=False, deltat0=1e-3, init=dict(kmin=4.0, kmax=8.0, seed=2024),
          steps=10),
+    dict(name="ns2d_32_euler", nx=32, ny=32, Lx=6.0, Ly=6.0, nu_2=1e-3,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="Euler", init=dict(kmin=2.0, kmax=6.0, seed=5), steps=10),
+    dict(name="ns2d_40x32_rk2", nx=40, ny=32, Lx=2 * pi, Ly=2 * pi * 32 / 40,
+         nu_2=1e-3, beta=0.5, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2", init=dict(kmin=2.0, kmax=8.0, seed=7), steps=10),
 ]
 
 CASES_3D = [
@@ -52,7 +58,18 @@ CASES_3D = [
     dict(name="ns3d_smag_20x24x16", nx=20, ny=24, nz=16, nu_2=1e-3,
          smagorinsky_C=0.18, USE_CFL=True, deltat0=0.2, deltat_max=0.2,
          cfl_coef=0.5, init="iso", seed=6, steps=10),
+    dict(name="ns3d_rk2_20x15x10", nx=20, ny=15, nz=10, Lx=6.0, Ly=4.5, Lz=3.0,
+         nu_2=1e-2, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2", init="iso", seed=8, steps=10),
+    dict(name="ns3d_heun_24x16x32_f", nx=24, ny=16, nz=32, nu_2=5e-3, f=1.0,
+         USE_CFL=False, deltat0=5e-3, type_time_scheme="RK2_trapezoid", init="iso",
+         seed=9, steps=10),
+    dict(name="ns3d_euler_tgv_32", nx=32, ny=32, nz=32, nu_2=1 / 1600, USE_CFL=True,
+         deltat0=0.2, deltat_max=0.2, cfl_coef=None, type_time_scheme="Euler",
+         init="tgv", steps=10),
 ]
+
+SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3}
 
 
 def _kw(case, keys):
@@ -64,7 +81,7 @@ def run_2d(mods, case):
     rot0 = noise_rot_2d(case["nx"], case["ny"], case["Lx"], case["Ly"],
                         **case["init"])
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
-                    "deltat_max", "cfl_coef"])
+                    "deltat_max", "cfl_coef", "type_time_scheme"])
     sim = refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0), **kw)
     sim.state.init_from_rotfft(rot0.copy())
     S_init = np.array(sim.state.state_spect)
@@ -100,7 +117,7 @@ def run_3d(mods, case):
     else:
         v0 = isotropic_3d(nx, ny, nz, *L, seed=case["seed"])
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
-                    "deltat_max", "cfl_coef"])
+                    "deltat_max", "cfl_coef", "type_time_scheme"])
     sim = refshim.make_ns3d(mods, oper, f=case.get("f"),
                             smagorinsky_C=case.get("smagorinsky_C"), **kw)
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
@@ -139,19 +156,26 @@ def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
             "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
             "smagorinsky_C"]
-    return {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
-                                   dtype=np.float64)
-            for k in keys if k in case}
+    out = {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
+                                  dtype=np.float64)
+           for k in keys if k in case}
+    out["p_scheme"] = np.asarray(SCHEME_CODES[case.get("type_time_scheme", "RK4")],
+                                 dtype=np.float64)
+    return out
 
 
-def main(ref_root):
+def main(ref_root, only=None):
     mods = refshim.load_reference(ref_root)
     for case in CASES_2D:
+        if only and case["name"] not in only:
+            continue
         out = run_2d(mods, case)
         np.savez_compressed(HERE / f"{case['name']}.npz", **_params_array(case),
                             **{k: np.asarray(v) for k, v in out.items()})
         print(case["name"], "ok", out["dts"][-1], out["E"][-1])
     for case in CASES_3D:
+        if only and case["name"] not in only:
+            continue
         out = run_3d(mods, case)
         np.savez_compressed(HERE / f"{case['name']}.npz", **_params_array(case),
                             **{k: np.asarray(v) for k, v in out.items()})
@@ -159,4 +183,4 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])

@@ -5,8 +5,10 @@ from pathlib import Path
 import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES_2D = ["ns2d_32_cfl", "ns2d_48x40_beta", "ns2d_256_c1"]
-CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20x24x16"]
+CASES_2D = ["ns2d_32_cfl", "ns2d_48x40_beta", "ns2d_256_c1", "ns2d_32_euler", "ns2d_40x32_rk2"]
+CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20x24x16",
+            "ns3d_rk2_20x15x10", "ns3d_heun_24x16x32_f", "ns3d_euler_tgv_32"]
+SCHEME_NAMES = {0: "RK4", 1: "Euler", 2: "RK2", 3: "RK2_trapezoid"}
 
 
 def load(name):
@@ -18,8 +20,13 @@ def load(name):
     return d, p
 
 
+def scheme(p):
+    """type_time_scheme of a fixture (RK4 when it records none)."""
+    return SCHEME_NAMES[int(p["scheme"])] if p.get("scheme") is not None else "RK4"
+
+
 def solver_kwargs(p):
-    kw = {}
+    kw = {"type_time_scheme": scheme(p)}
     for k in ("nu_2", "nu_4", "nu_8", "nu_m4", "deltat0", "deltat_max", "cfl_coef"):
         if p.get(k) is not None:
             kw[k] = p[k]

@@ -37,6 +37,7 @@ def run_3d(shape, precision, steps, **kw):
     ts.USE_CFL = kw.get("USE_CFL", False)
     ts.cfl_coef = kw.get("cfl_coef")
     ts.deltat0 = kw.get("dt", 5e-3)
+    ts.type_time_scheme = kw.get("type_time_scheme", "RK4")
     ts.USE_T_END = False
     ts.it_end = steps
     sim = SimulNS3D(p)
@@ -45,7 +46,8 @@ def run_3d(shape, precision, steps, **kw):
     sim.time_stepping.start()
     orc = NS3DOracle(OperNumpy3D(nx, ny, nz, *L), f=kw.get("f"), nu_2=p.nu_2,
                      nu_4=p.nu_4, nu_m4=p.nu_m4, USE_CFL=ts.USE_CFL,
-                     cfl_coef=ts.cfl_coef, deltat0=ts.deltat0)
+                     cfl_coef=ts.cfl_coef, deltat0=ts.deltat0,
+                     type_time_scheme=ts.type_time_scheme)
     orc.state_spect[:] = v0
     orc.statephys_from_statespect()
     orc.run(it_end=steps)
@@ -56,6 +58,9 @@ def run_3d(shape, precision, steps, **kw):
     ((64, 64, 64), {}),
     ((32, 64, 128), {"USE_CFL": True, "cfl_coef": 0.5, "f": 0.7}),
     ((64, 32, 64), {"nu_4": 1e-6, "nu_m4": 1e-3}),
+    ((32, 64, 64), {"type_time_scheme": "RK2", "USE_CFL": True}),
+    ((64, 64, 32), {"type_time_scheme": "RK2_trapezoid", "f": 0.3}),
+    ((32, 32, 64), {"type_time_scheme": "Euler", "dt": 2e-3}),
 ])
 def test_ns3d_fast_fp64_matches_oracle(cuda, shape, kw):
     sim, orc = run_3d(shape, "float64", 4, **kw)

@@ -6,7 +6,7 @@ the first tendency); FP32: relative L2 <= 1e-5 after 10 steps.
 import numpy as np
 import pytest
 
-from golden_cases import CASES_2D, CASES_3D, lengths, load
+from golden_cases import CASES_2D, CASES_3D, lengths, load, scheme
 
 pytestmark = pytest.mark.gpu
 
@@ -44,6 +44,7 @@ def make_sim(name, precision="float64"):
     if p.get("deltat_max") is not None:
         ts.deltat_max = p["deltat_max"]
     ts.cfl_coef = p.get("cfl_coef")
+    ts.type_time_scheme = scheme(p)
     ts.USE_T_END = False
     ts.it_end = int(p["steps"])
     sim = Simul(params)
@@ -60,7 +61,7 @@ def rel_l2_per_var(a, b):
 def test_tendencies_fp64(cuda, name):
     sim, d, _ = make_sim(name)
     tend = sim.tendencies_nonlin(sim.state.state_spect).cpu().numpy()
-    if name == "ns3d_tgv_32":  # round-off-only tendency: absolute check
+    if "tgv" in name:  # round-off-only tendency: absolute check
         assert np.abs(tend - d["tend0"]).max() < 1e-14
     else:
         assert rel_l2_per_var(tend, d["tend0"]) < TOL_F64
@@ -83,7 +84,8 @@ def test_ten_steps_fp64(cuda, name):
     assert rel_l2_per_var(phys, d["phys_end"]) < TOL_F64
 
 
-@pytest.mark.parametrize("name", ["ns2d_256_c1", "ns3d_iso_24x16x32_f", "ns3d_tgv_32"])
+@pytest.mark.parametrize("name", ["ns2d_256_c1", "ns3d_iso_24x16x32_f", "ns3d_tgv_32",
+                                  "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()

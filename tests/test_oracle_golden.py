@@ -1,7 +1,7 @@
 """The oracle restatement reproduces the fixtures made by the reference code.
 
-Fixtures (``tests/golden/*.npz``) come from the reference's own RK4 / CFL /
-tendency code (``oracle/refshim.py``, see ``golden/make_golden.py``).
+Fixtures (``tests/golden/*.npz``) come from the reference's own time-scheme
+(RK4, RK2, RK2_trapezoid, Euler) / CFL / tendency code (``oracle/refshim.py``, see ``golden/make_golden.py``).
 """
 import numpy as np
 import pytest
@@ -58,7 +58,7 @@ def test_oracle_steps_match_reference(name):
 @pytest.mark.parametrize("name", CASES_2D + CASES_3D)
 def test_reference_tendency_conserves_energy(name):
     """``ns2d/test_solver.py:49-69`` and ``ns3d/test_solver.py:73-96``."""
-    if name == "ns3d_tgv_32":
+    if "tgv" in name:
         pytest.skip("Taylor-Green at t=0: the tendency is round-off only")
     if "smag" in name:
         pytest.skip("with a turbulence model the tendency dissipates energy")
