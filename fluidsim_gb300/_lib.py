@@ -34,7 +34,8 @@ EXPORTED = (
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
     "gbs_ns_is_dealiased", "gbs_ns_step",
 )
-SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3}
+SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
+           "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
 
 
 class NSParams(ctypes.Structure):

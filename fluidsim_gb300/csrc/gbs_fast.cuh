@@ -301,6 +301,8 @@ struct Geo {
   double dkx, dky, dkz;
   double nu2, nu4, nu8, num4, beta, f, inv_n, k2_hypo0;
   int has_f;
+  int phase;             // multiply the input state by exp(i phi)
+  double dx, dy, dz;     // grid spacings (phase factor)
 };
 
 // Per-run parameters of a batched ensemble (null pointers: single run).
@@ -362,8 +364,11 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           else { a = S[i + nK]; b = S[i]; ka = kx; kb = ky; }
           const C d = mk<C>(ka * a.x - kb * b.x, ka * a.y - kb * b.y);
           x = mk<C>(-d.y, d.x);
-          if (f == 5 && g.has_f && ix == 0 && iy == 0 && p == 0) x.x += T(g.f);
         }
+        if (g.phase)
+          x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
+                                         T(g.dkz * kadim(p, P::N))));
+        if (f == 5 && g.has_f && ix == 0 && iy == 0 && p == 0) x.x += T(g.f);
       }
       v[r] = x;
     }
@@ -546,9 +551,10 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
       const int p = jt + r * P::N8;
       C x = mk<C>(0, 0);
       if (valid && (!g.pr || kept(p, P::N, g.kcy))) {
-        const C w = S[(int64_t)p * g.nkx + ix];
+        C w = S[(int64_t)p * g.nkx + ix];
         const int kyi = kadim(p, P::N);
         const T ky = T(g.dky * kyi);
+        if (g.phase) w = cmul(w, phase_factor<C, T>(T(g.dx), T(g.dy), T(0), kx, ky, T(0)));
         T cc;
         if (f == 0 || f == 1) {
           const T k2 = kx * kx + ky * ky;
@@ -701,7 +707,7 @@ kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
     if (g.pr && rm) continue;
     const T ky = T(g.dky * kyi);
     stage_epilogue1<C, T>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
-                          kx * kx + ky * ky, ix == 0 && kyi == 0, rm, q);
+                          kx, ky, ix == 0 && kyi == 0, rm, q);
   }
 }
 

@@ -43,6 +43,8 @@ struct NSK {
   double inv_n;
   double k2_hypo0;  // K2 at (iz, iy, ix) = (0, 0, 1): f_d_hypo[0,..,0] source
   int TX, L, LP;
+  int phase;          // multiply the input state by exp(i phi)
+  double dx, dy, dz;  // grid spacings (phase factor)
 };
 
 __device__ __forceinline__ bool removed(const NSK& q, int ix, int ky, int kz) {
@@ -103,8 +105,14 @@ k3_inv_z_curl(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
     for (int f = 0; f < 6; ++f) v[f] = mk<C>(0, 0);
     if (ix < q.nkx) {
       const int64_t i = iz * plane + (int64_t)iy * q.nkx + ix;
-      const C vx = S[i], vy = S[i + nK], vz = S[i + 2 * nK];
+      C vx = S[i], vy = S[i + nK], vz = S[i + 2 * nK];
       const T kx = T(q.dkx * ix), kz = T(q.dkz * kadim(iz, q.nz));
+      if (q.phase) {
+        const C e = phase_factor<C, T>(T(q.dx), T(q.dy), T(q.dz), kx, ky, kz);
+        vx = cmul(vx, e);
+        vy = cmul(vy, e);
+        vz = cmul(vz, e);
+      }
       v[0] = vx;
       v[1] = vy;
       v[2] = vz;
@@ -245,8 +253,9 @@ k2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
 #pragma unroll
     for (int f = 0; f < 4; ++f) v[f] = mk<C>(0, 0);
     if (ix < q.nkx) {
-      const C w = S[(int64_t)iy * q.nkx + ix];
+      C w = S[(int64_t)iy * q.nkx + ix];
       const T kx = T(q.dkx * ix), ky = T(q.dky * kadim(iy, q.ny));
+      if (q.phase) w = cmul(w, phase_factor<C, T>(T(q.dx), T(q.dy), T(0), kx, ky, T(0)));
       const T k2 = kx * kx + ky * ky;
       const T inv = (ix == 0 && kadim(iy, q.ny) == 0) ? T(0) : T(1) / k2;
       const T cx = ky * inv, cy = -(kx * inv);
@@ -347,8 +356,7 @@ k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
     const bool rm = removed(q, ix, kyi, 0);
     const C N = cscale(buf[iy * LP + c], inv_n);
     const T kx = T(q.dkx * ix), ky = T(q.dky * kyi);
-    stage_epilogue1<C, T>(mode, a, i, N, kx * kx + ky * ky, ix == 0 && kyi == 0, rm,
-                          phys(q));
+    stage_epilogue1<C, T>(mode, a, i, N, kx, ky, ix == 0 && kyi == 0, rm, phys(q));
   }
 }
 
@@ -367,6 +375,7 @@ struct Solver {
   void* F;
   void* tmp;
   void* tmp1;
+  void* tmp2;                // RK2_phaseshift_exact only (allocated at first use)
   unsigned long long* dmax;  // 3 maxima (double bits)
   int* dflag;
   double* dred;              // reduction partials
@@ -483,9 +492,13 @@ static int setup_shapes(Solver* s) {
 }
 
 // One tendency evaluation from `in`; kernel C runs `mode`.
-static fast::Geo geo_for(const Solver* s, bool pruned) {
+static fast::Geo geo_for(const Solver* s, bool pruned, bool phase = false) {
   fast::Geo g = s->geo;
   g.pr = pruned ? 1 : 0;
+  g.phase = phase ? 1 : 0;
+  g.dx = s->p.Lx / s->p.nx;
+  g.dy = s->p.Ly / s->p.ny;
+  g.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
   g.ncx = pruned ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
   const int nkeep = 2 * g.kcy - 1;
   g.nky_keep = (pruned && nkeep < g.ny) ? nkeep : g.ny;
@@ -494,8 +507,9 @@ static fast::Geo geo_for(const Solver* s, bool pruned) {
 
 // compile-time-size path: same passes as the generic one, optionally pruned
 template <typename T>
-static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, cudaStream_t st) {
-  const fast::Geo g = geo_for(s, pruned);
+static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, bool phase,
+                     cudaStream_t st) {
+  const fast::Geo g = geo_for(s, pruned, phase);
   unsigned long long* vmax = want_max ? s->dmax : nullptr;
   int rc;
   const int kcy_in = pruned ? g.kcy : g.ny + 1;
@@ -549,10 +563,14 @@ static int finish_fast(Solver* s, int mode, const RKArgs& a, bool pruned, cudaSt
 
 template <typename T>
 static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
-                bool want_max, cudaStream_t st, bool pruned = false) {
-  if (s->use_fast) return eval_fast<T>(s, in, pruned, want_max, st);
+                bool want_max, cudaStream_t st, bool pruned = false, bool phase = false) {
+  if (s->use_fast) return eval_fast<T>(s, in, pruned, want_max, phase, st);
   using C = cplx<T>;
   NSK q = s->q;
+  q.phase = phase ? 1 : 0;
+  q.dx = s->p.Lx / s->p.nx;
+  q.dy = s->p.Ly / s->p.ny;
+  q.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
   const C* twx = static_cast<const C*>(s->tw[0]);
   const C* twy = static_cast<const C*>(s->tw[1]);
   const C* twz = static_cast<const C*>(s->tw[2]);
@@ -674,24 +692,38 @@ static double cfl_tmp(const Solver* s, const double* m) {
 // the intermediate state written by the previous stage) and the epilogue
 // mode.  pseudo_spect.py: RK4 798-984, Euler 245-280, RK2 469-517,
 // RK2_trapezoid 519-569.
+// The phase-shift schemes evaluate some tendencies on exp(i phi) X and
+// divide them by exp(i phi) (Euler_phaseshift 374-419, RK2_phaseshift
+// 571-639, RK2_phaseshift_exact 712-796).
 struct Stage {
   int input;  // 0: S, 1: tmp, 2: tmp1
   int mode;
+  int phase;  // shifted evaluation
 };
 static int scheme_stages(int scheme, Stage* st) {
   switch (scheme) {
     case GBS_SCHEME_RK4:
-      st[0] = {0, kRK0}; st[1] = {2, kRK1}; st[2] = {2, kRK2}; st[3] = {2, kRK3};
+      st[0] = {0, kRK0, 0}; st[1] = {2, kRK1, 0}; st[2] = {2, kRK2, 0}; st[3] = {2, kRK3, 0};
       return 4;
     case GBS_SCHEME_EULER:
-      st[0] = {0, kEuler};
+      st[0] = {0, kEuler, 0};
       return 1;
     case GBS_SCHEME_RK2:
-      st[0] = {0, kR2a}; st[1] = {1, kR2b};
+      st[0] = {0, kR2a, 0}; st[1] = {1, kR2b, 0};
       return 2;
     case GBS_SCHEME_RK2_TRAPEZOID:
-      st[0] = {0, kHeunA}; st[1] = {1, kHeunB};
+      st[0] = {0, kHeunA, 0}; st[1] = {1, kHeunB, 0};
       return 2;
+    case GBS_SCHEME_EULER_PHASESHIFT:
+      st[0] = {0, kStoreTmp, 0}; st[1] = {0, kEulerPS, 1};
+      return 2;
+    case GBS_SCHEME_RK2_PHASESHIFT:
+      st[0] = {0, kPS2a, 0}; st[1] = {1, kPS2b, 1};
+      return 2;
+    case GBS_SCHEME_RK2_PHASESHIFT_EXACT:
+      st[0] = {0, kStoreTmp1, 0}; st[1] = {0, kPSXb, 1};
+      st[2] = {1, kStoreTmp2, 0}; st[3] = {1, kPSXd, 1};
+      return 4;
     default:
       return 0;
   }
@@ -708,19 +740,40 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     set_error("unknown time scheme");
     return GBS_EINVAL;
   }
+  bool shifted = false;
+  for (int k = 0; k < nst; ++k) shifted = shifted || stages[k].phase;
+  if (shifted && s->turb.type != 0) {
+    set_error("phase-shift schemes with a turbulence model are not implemented");
+    return GBS_EINVAL;
+  }
+  if (scheme == GBS_SCHEME_RK2_PHASESHIFT_EXACT && !s->tmp2) {
+    // the one scheme with a third intermediate state: allocated at its first step
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    if (cudaMalloc(&s->tmp2, s->csize * s->nvar * s->nK) != cudaSuccess) {
+      s->tmp2 = nullptr;
+      set_error("out of device memory");
+      return GBS_ENOMEM;
+    }
+    GBS_CUDA_TRY(cudaMemsetAsync(s->tmp2, 0, s->csize * s->nvar * s->nK, st));
+  }
   RKArgs a{};
   a.S = S;
   a.Sout = S;
   a.tmp = s->tmp;
   a.tmp1 = s->tmp1;
+  a.tmp2 = s->tmp2;
   a.nan_flag = s->dflag;
+  a.dx = s->p.Lx / s->p.nx;
+  a.dy = s->p.Ly / s->p.ny;
+  a.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
   int rc;
   if (cfl) GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
   if (check_nan) GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
   for (int k = 0; k < nst; ++k) {
     const void* in = stages[k].input == 0 ? S : (stages[k].input == 1 ? s->tmp : s->tmp1);
     const int m = stages[k].mode;
-    rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr);
+    a.phase = stages[k].phase;
+    rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr, stages[k].phase != 0);
     if (rc) return rc;
     if (k == 0 && cfl) {
       GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
@@ -939,7 +992,7 @@ static void free_solver(Solver* s) {
   }
   for (void* t : s->tw)
     if (t) cudaFree(t);
-  void* ptrs[] = {s->W, s->F, s->tmp, s->tmp1, s->dmax, s->dflag, s->dred};
+  void* ptrs[] = {s->W, s->F, s->tmp, s->tmp1, s->tmp2, s->dmax, s->dflag, s->dred};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->hbuf) cudaFreeHost(s->hbuf);
@@ -1088,7 +1141,7 @@ int gbs_ns_step(gbs_ns* h, int scheme, void* S, double* dt, const double* cfl, i
                 void* stream) {
   gbs::clear_error();
   if (!h || !S || !dt || !(*dt > 0) || scheme < GBS_SCHEME_RK4 ||
-      scheme > GBS_SCHEME_RK2_TRAPEZOID) {
+      scheme > GBS_SCHEME_RK2_PHASESHIFT_EXACT) {
     gbs::set_error("gbs_ns_step: invalid argument");
     return GBS_EINVAL;
   }

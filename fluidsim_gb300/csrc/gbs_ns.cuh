@@ -14,11 +14,36 @@ namespace gbs {
 // stages write the new state (projected, dealiased, NaN-checked).
 enum Mode {
   kTend = 0, kRK0 = 1, kRK1 = 2, kRK2 = 3, kRK3 = 4,
-  kEuler = 5, kR2a = 6, kR2b = 7, kHeunA = 8, kHeunB = 9
+  kEuler = 5, kR2a = 6, kR2b = 7, kHeunA = 8, kHeunB = 9,
+  // phase-shift schemes (the shifted evaluations divide their tendency by
+  // the phase factor before the stage formula)
+  kStoreTmp = 10,   // tmp  = N
+  kStoreTmp1 = 11,  // tmp1 = N
+  kStoreTmp2 = 12,  // tmp2 = N
+  kEulerPS = 13,    // S <- (S + dt (tmp + N~)/2) E
+  kPS2a = 14,       // tmp = (S + dt N) E, tmp1 = N
+  kPS2b = 15,       // S <- S E + dt E2 (tmp1 + N~)/2
+  kPSXb = 16,       // tmp1 = Nd0 = (tmp1 + N~)/2, tmp = (S + dt Nd0) E
+  kPSXd = 17        // S <- S E + dt E2 (tmp1 + (tmp2 + N~)/2)/2
 };
 
 __device__ __forceinline__ bool final_stage(int mode) {
-  return mode == kRK3 || mode == kEuler || mode == kR2b || mode == kHeunB;
+  return mode == kRK3 || mode == kEuler || mode == kR2b || mode == kHeunB ||
+         mode == kEulerPS || mode == kPS2b || mode == kPSXd;
+}
+
+// Phase factor exp(i phi), phi = (dx kx + dy ky + dz kz) / 2 of the
+// phase-shift schemes (pseudo_spect.py:282-300), computed in the working
+// precision from the wavenumbers of the mode.
+__device__ __forceinline__ void tsincos(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void tsincos(double x, double* s, double* c) { sincos(x, s, c); }
+
+template <typename C, typename T>
+__device__ __forceinline__ C phase_factor(T dx, T dy, T dz, T kx, T ky, T kz) {
+  const T phi = T(0.5) * (dx * kx + dy * ky + dz * kz);
+  T sn, cs;
+  tsincos(phi, &sn, &cs);
+  return mk<C>(cs, sn);
 }
 
 struct RKArgs {
@@ -31,6 +56,9 @@ struct RKArgs {
   int* nan_flag;
   const void* add;  // optional forcing (nvar spectral fields) added to the
                     // tendency before projection and dealiasing
+  void* tmp2;       // third buffer of RK2_phaseshift_exact
+  int phase;        // divide the tendency by exp(i phi) (shifted evaluation)
+  double dx, dy, dz;  // grid spacings (phase factor)
 };
 
 // Viscosities for sigma(k) = f_d + f_d_hypo.
@@ -80,10 +108,21 @@ __device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C
   const C S = static_cast<const C*>(a.S)[i];
   const T E = dexp(-dt * sigma);
   if (mode == kEuler) return cscale(mk<C>(S.x + dt * N.x, S.y + dt * N.y), E);
-  // kR2b
+  if (mode == kEulerPS) {  // pseudo_spect.py:409-419
+    const C t = static_cast<const C*>(a.tmp)[i];
+    const C Nd = cscale(cadd(t, N), T(0.5));
+    return cscale(mk<C>(S.x + dt * Nd.x, S.y + dt * Nd.y), E);
+  }
+  C Nd = N;  // kR2b
+  if (mode == kPS2b) {  // pseudo_spect.py:624-639
+    Nd = cscale(cadd(static_cast<const C*>(a.tmp1)[i], N), T(0.5));
+  } else if (mode == kPSXd) {  // pseudo_spect.py:784-796
+    const C n1 = cscale(cadd(static_cast<const C*>(a.tmp2)[i], N), T(0.5));
+    Nd = cscale(cadd(static_cast<const C*>(a.tmp1)[i], n1), T(0.5));
+  }
   const T E2 = dexp(-dt / T(2) * sigma);
   const T c1 = dt * E2;
-  return mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  return mk<C>(S.x * E + c1 * Nd.x, S.y * E + c1 * Nd.y);
 }
 
 // Intermediate stage update at one mode (RK4: pseudo_spect.py:898-984;
@@ -126,7 +165,32 @@ __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
     const T c2 = dt / T(2);
     tmp[i] = cscale(mk<C>(S.x + dt * N.x, S.y + dt * N.y), E);
     tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E);
+  } else if (mode == kStoreTmp) {
+    tmp[i] = N;
+  } else if (mode == kStoreTmp1) {
+    tmp1[i] = N;
+  } else if (mode == kStoreTmp2) {
+    static_cast<C*>(a.tmp2)[i] = N;
+  } else if (mode == kPS2a) {  // pseudo_spect.py:617-620
+    const C S = static_cast<const C*>(a.S)[i];
+    const T E = dexp(-dt * sigma);
+    tmp[i] = cscale(mk<C>(S.x + dt * N.x, S.y + dt * N.y), E);
+    tmp1[i] = N;
+  } else if (mode == kPSXb) {  // pseudo_spect.py:759-767
+    const C S = static_cast<const C*>(a.S)[i];
+    const T E = dexp(-dt * sigma);
+    const C Nd0 = cscale(cadd(tmp1[i], N), T(0.5));
+    tmp1[i] = Nd0;
+    tmp[i] = cscale(mk<C>(S.x + dt * Nd0.x, S.y + dt * Nd0.y), E);
   }
+}
+
+// N / exp(i phi) for the shifted evaluations (|exp(i phi)| = 1: times the
+// conjugate)
+template <typename C, typename T>
+__device__ __forceinline__ C unshift(const RKArgs& a, C N, T kx, T ky, T kz) {
+  const C e = phase_factor<C, T>(T(a.dx), T(a.dy), T(a.dz), kx, ky, kz);
+  return cmulc(N, e);
 }
 
 // project_perpk3d: v -= k (k.v)/|k|^2; the k = 0 mode is left unchanged
@@ -151,12 +215,16 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
                                                 const Phys& q) {
   project3(N, kx, ky, kz, k2, k0);
   if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
+  if (a.phase) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) N[f] = unshift<C, T>(a, N[f], kx, ky, kz);
+  }
   if (mode == kTend) {
     C* o = static_cast<C*>(a.tend);
 #pragma unroll
     for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
   } else if (final_stage(mode)) {
-    const T sig = (mode == kEuler || mode == kR2b) ? freq_lin<T>(q, k2, k0) : T(0);
+    const T sig = (mode == kRK3 || mode == kHeunB) ? T(0) : freq_lin<T>(q, k2, k0);
     C Sn[3];
 #pragma unroll
     for (int f = 0; f < 3; ++f) Sn[f] = final_value<C, T>(mode, a, i + f * nK, N[f], sig);
@@ -176,13 +244,15 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
 // ns2d epilogue at one mode (no projection).
 template <typename C, typename T>
 __device__ __forceinline__ void stage_epilogue1(int mode, const RKArgs& a, int64_t i,
-                                                C N, T k2, bool k0, bool rm,
+                                                C N, T kx, T ky, bool k0, bool rm,
                                                 const Phys& q) {
+  const T k2 = kx * kx + ky * ky;
   if (rm) N = mk<C>(0, 0);
+  if (a.phase) N = unshift<C, T>(a, N, kx, ky, T(0));
   if (mode == kTend) {
     static_cast<C*>(a.tend)[i] = N;
   } else if (final_stage(mode)) {
-    const T sig = (mode == kEuler || mode == kR2b) ? freq_lin<T>(q, k2, k0) : T(0);
+    const T sig = (mode == kRK3 || mode == kHeunB) ? T(0) : freq_lin<T>(q, k2, k0);
     C Sn = final_value<C, T>(mode, a, i, N, sig);
     if (rm) Sn = mk<C>(0, 0);
     static_cast<C*>(a.Sout)[i] = Sn;

@@ -136,9 +136,16 @@ int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
 #define GBS_SCHEME_EULER 1          /* _time_step_Euler, 245-280             */
 #define GBS_SCHEME_RK2 2            /* _time_step_RK2, 469-517               */
 #define GBS_SCHEME_RK2_TRAPEZOID 3  /* _time_step_RK2_trapezoid, 519-569     */
+#define GBS_SCHEME_EULER_PHASESHIFT 4      /* _time_step_Euler_phaseshift, 374-419 */
+#define GBS_SCHEME_RK2_PHASESHIFT 5        /* _time_step_RK2_phaseshift, 571-639   */
+#define GBS_SCHEME_RK2_PHASESHIFT_EXACT 6  /* _time_step_RK2_phaseshift_exact,
+                                              712-796 (allocates one more state
+                                              buffer at its first step)          */
 
 /* One step of `scheme`, otherwise as gbs_ns_step_rk4 (same flags, CFL rule,
- * projection, dealiasing and NaN check). */
+ * projection, dealiasing and NaN check).  The phase-shift schemes use the
+ * phase exp(i (dx kx + dy ky + dz kz) / 2) (pseudo_spect.py:282-300) and are
+ * rejected with GBS_EINVAL when a turbulence model is set. */
 int gbs_ns_step(gbs_ns* solver, int scheme, void* state_spect, double* dt,
                 const double* cfl, int flags, void* stream);
 

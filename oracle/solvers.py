@@ -43,7 +43,8 @@ class _SolverBase:
     ``fluidsim/base/time_stepping/base.py:248-354``; loop 182-244.
     """
 
-    SCHEMES = ("RK4", "RK2", "Euler", "RK2_trapezoid")
+    SCHEMES = ("RK4", "RK2", "Euler", "RK2_trapezoid", "Euler_phaseshift",
+               "RK2_phaseshift", "RK2_phaseshift_exact")
 
     def __init__(self, oper, nu_2=0.0, nu_4=0.0, nu_8=0.0, nu_m4=0.0,
                  deltat0=0.2, deltat_max=0.2, USE_CFL=False, cfl_coef=None,
@@ -134,6 +135,54 @@ class _SolverBase:
         S1 = (S + dt * N0) * diss
         N1 = self.tendencies_nonlin(S1)
         S[:] = (S + dt / 2 * N0) * diss + dt / 2 * N1
+
+    def _phaseshift(self):
+        """exp(i phi), phi = (dx kx + dy ky (+ dz kz)) / 2,
+        ``pseudo_spect.py:282-300``."""
+        o = self.oper
+        if len(o.axes) == 3:
+            phase = 0.5 * (o.deltax * o.Kx + o.deltay * o.Ky + o.deltaz * o.Kz)
+        else:
+            phase = 0.5 * (o.deltax * o.KX + o.deltay * o.KY)
+        return np.exp(1j * phase)
+
+    def time_step_Euler_phaseshift(self):
+        """``pseudo_spect.py:374-419``."""
+        dt = self.deltat
+        diss = self._coefs()[0]
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        ph = self._phaseshift()
+        Ns = self.tendencies_nonlin(ph * S) / ph
+        Nd = 0.5 * (N0 + Ns)
+        S[:] = (S + dt * Nd) * diss
+
+    def time_step_RK2_phaseshift(self):
+        """``pseudo_spect.py:571-639``."""
+        dt = self.deltat
+        diss, diss2 = self._coefs()
+        S = self.state_spect
+        N0 = self.tendencies_nonlin()
+        S1 = (S + dt * N0) * diss
+        ph = self._phaseshift()
+        N1s = self.tendencies_nonlin(ph * S1)
+        Nd = 0.5 * (N0 + N1s / ph)
+        S[:] = S * diss + dt * diss2 * Nd
+
+    def time_step_RK2_phaseshift_exact(self):
+        """``pseudo_spect.py:712-796``."""
+        dt = self.deltat
+        diss, diss2 = self._coefs()
+        ph = self._phaseshift()
+        S = self.state_spect
+        N0 = self.tendencies_nonlin(S)
+        N0s = self.tendencies_nonlin(ph * S)
+        Nd0 = 0.5 * (N0 + N0s / ph)
+        S1 = (S + dt * Nd0) * diss
+        N1 = self.tendencies_nonlin(S1)
+        N1s = self.tendencies_nonlin(ph * S1)
+        Nd = 0.5 * (Nd0 + 0.5 * (N1 + N1s / ph))
+        S[:] = S * diss + dt * diss2 * Nd
 
     def time_step(self):
         """``_init_time_scheme`` dispatch, ``pseudo_spect.py:191-231``."""

@@ -80,6 +80,7 @@ class OperNumpy3D:
     def __init__(self, nx, ny, nz, Lx=2 * pi, Ly=2 * pi, Lz=2 * pi,
                  coef_dealiasing=2.0 / 3, truncation_shape="cubic"):
         self.nx, self.ny, self.nz = nx, ny, nz
+        self.axes = ("z", "y", "x")
         self.Lx, self.Ly, self.Lz = float(Lx), float(Ly), float(Lz)
         self.coef_dealiasing = coef_dealiasing
         self.deltax = self.Lx / nx
@@ -252,6 +253,7 @@ class OperNumpy2D:
     def __init__(self, nx, ny, Lx=2 * pi, Ly=2 * pi, coef_dealiasing=2.0 / 3,
                  truncation_shape="cubic"):
         self.nx, self.ny = nx, ny
+        self.axes = ("y", "x")
         self.Lx, self.Ly = float(Lx), float(Ly)
         self.coef_dealiasing = coef_dealiasing
         self.deltax = self.Lx / nx

@@ -45,6 +45,13 @@ CASES_2D = [
     dict(name="ns2d_40x32_rk2", nx=40, ny=32, Lx=2 * pi, Ly=2 * pi * 32 / 40,
          nu_2=1e-3, beta=0.5, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
          type_time_scheme="RK2", init=dict(kmin=2.0, kmax=8.0, seed=7), steps=10),
+    dict(name="ns2d_32_rk2ps", nx=32, ny=32, Lx=6.0, Ly=6.0, nu_2=1e-3,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2_phaseshift", init=dict(kmin=2.0, kmax=10.0, seed=11),
+         steps=10),
+    dict(name="ns2d_36x32_eulerps", nx=36, ny=32, Lx=2 * pi, Ly=5.0, nu_2=2e-3,
+         USE_CFL=False, deltat0=5e-3, type_time_scheme="Euler_phaseshift",
+         init=dict(kmin=2.0, kmax=9.0, seed=12), steps=10),
 ]
 
 CASES_3D = [
@@ -67,9 +74,19 @@ CASES_3D = [
     dict(name="ns3d_euler_tgv_32", nx=32, ny=32, nz=32, nu_2=1 / 1600, USE_CFL=True,
          deltat0=0.2, deltat_max=0.2, cfl_coef=None, type_time_scheme="Euler",
          init="tgv", steps=10),
+    dict(name="ns3d_rk2ps_20x15x10", nx=20, ny=15, nz=10, Lx=6.0, Ly=4.5, Lz=3.0,
+         nu_2=1e-2, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2_phaseshift", init="iso", seed=13, steps=10),
+    dict(name="ns3d_rk2psx_16x24x32_f", nx=16, ny=24, nz=32, nu_2=5e-3, f=0.5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2_phaseshift_exact", init="iso", seed=14, steps=10),
+    dict(name="ns3d_eulerps_32", nx=32, ny=32, nz=32, nu_2=2e-3, USE_CFL=False,
+         deltat0=2e-3, type_time_scheme="Euler_phaseshift", init="iso", seed=15,
+         steps=10),
 ]
 
-SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3}
+SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
+                "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
 
 
 def _kw(case, keys):

@@ -61,6 +61,9 @@ def run_3d(shape, precision, steps, **kw):
     ((32, 64, 64), {"type_time_scheme": "RK2", "USE_CFL": True}),
     ((64, 64, 32), {"type_time_scheme": "RK2_trapezoid", "f": 0.3}),
     ((32, 32, 64), {"type_time_scheme": "Euler", "dt": 2e-3}),
+    ((32, 64, 64), {"type_time_scheme": "RK2_phaseshift", "USE_CFL": True}),
+    ((64, 32, 32), {"type_time_scheme": "RK2_phaseshift_exact", "f": 0.4}),
+    ((32, 32, 32), {"type_time_scheme": "Euler_phaseshift", "dt": 2e-3}),
 ])
 def test_ns3d_fast_fp64_matches_oracle(cuda, shape, kw):
     sim, orc = run_3d(shape, "float64", 4, **kw)
@@ -95,9 +98,11 @@ def test_ns3d_fast_tendency_matches_oracle(cuda):
     assert rel(tend, ref) < 1e-12
 
 
-@pytest.mark.parametrize("shape,beta,cfl", [((128, 128), 0.0, False), ((64, 256), 2.0, True),
-                                            ((512, 512), 0.0, False)])
-def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl):
+@pytest.mark.parametrize("shape,beta,cfl,scheme", [
+    ((128, 128), 0.0, False, "RK4"), ((64, 256), 2.0, True, "RK4"),
+    ((512, 512), 0.0, False, "RK4"), ((128, 64), 1.0, True, "RK2_phaseshift"),
+    ((64, 128), 0.0, False, "RK2_trapezoid"), ((128, 128), 0.5, False, "Euler_phaseshift")])
+def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl, scheme):
     from fluidsim_gb300.init_fields import noise_rot_2d
     from fluidsim_gb300.solvers import SimulNS2D
     from oracle.solvers import NS2DOracle
@@ -110,13 +115,14 @@ def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl):
     p.nu_2, p.nu_8, p.beta = 1e-3, 1e-14, beta
     ts = p.time_stepping
     ts.USE_CFL, ts.cfl_coef, ts.deltat0 = cfl, 0.5, 2e-3
+    ts.type_time_scheme = scheme
     ts.USE_T_END, ts.it_end = False, 5
     sim = SimulNS2D(p)
     rot = noise_rot_2d(nx, ny, *L, kmin=3, kmax=10, seed=4)
     sim.init_from_rotfft(rot)
     sim.time_stepping.start()
     orc = NS2DOracle(OperNumpy2D(nx, ny, *L), beta=beta, nu_2=1e-3, nu_8=1e-14,
-                     USE_CFL=cfl, cfl_coef=0.5, deltat0=2e-3)
+                     USE_CFL=cfl, cfl_coef=0.5, deltat0=2e-3, type_time_scheme=scheme)
     orc.init_from_rotfft(rot)
     orc.run(it_end=5)
     assert rel(sim.state.state_spect.cpu().numpy(), orc.state_spect) < 1e-12

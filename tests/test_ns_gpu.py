@@ -85,7 +85,8 @@ def test_ten_steps_fp64(cuda, name):
 
 
 @pytest.mark.parametrize("name", ["ns2d_256_c1", "ns3d_iso_24x16x32_f", "ns3d_tgv_32",
-                                  "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f"])
+                                  "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f", "ns2d_32_rk2ps",
+                                  "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()
