@@ -32,7 +32,7 @@ EXPORTED = (
     "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
     "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
-    "gbs_ns_is_dealiased", "gbs_ns_step",
+    "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
            "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
@@ -83,6 +83,7 @@ def _declare(lib):
         "gbs_ns_tendencies": (ctypes.c_int, [P, P, P, P]),
         "gbs_ns_step_rk4": (ctypes.c_int, [P, P, DP, DP, ctypes.c_int, P]),
         "gbs_ns_step": (ctypes.c_int, [P, ctypes.c_int, P, DP, DP, ctypes.c_int, P]),
+        "gbs_ns_set_projection": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "gbs_ns_max_velocity": (ctypes.c_int, [P, P, DP, P]),
         "gbs_cfl_update": (ctypes.c_double, [ctypes.c_double] * 4),
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),

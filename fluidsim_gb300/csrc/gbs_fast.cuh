@@ -303,6 +303,7 @@ struct Geo {
   int has_f;
   int phase;             // multiply the input state by exp(i phi)
   double dx, dy, dz;     // grid spacings (phase factor)
+  int proj, no_vz_kz0;   // ns3d projection of the tendencies and the state
 };
 
 // Per-run parameters of a batched ensemble (null pointers: single run).
@@ -319,6 +320,8 @@ __device__ __forceinline__ Phys phys_of(const Geo& g) {
   q.nu8 = g.nu8;
   q.num4 = g.num4;
   q.k2_hypo0 = g.k2_hypo0;
+  q.proj = g.proj;
+  q.no_vz_kz0 = g.no_vz_kz0;
   return q;
 }
 

@@ -45,6 +45,7 @@ struct NSK {
   int TX, L, LP;
   int phase;          // multiply the input state by exp(i phi)
   double dx, dy, dz;  // grid spacings (phase factor)
+  int proj, no_vz_kz0;  // ns3d projection of the tendencies and the state
 };
 
 __device__ __forceinline__ bool removed(const NSK& q, int ix, int ky, int kz) {
@@ -58,6 +59,8 @@ __device__ __forceinline__ Phys phys(const NSK& q) {
   p.nu8 = q.nu8;
   p.num4 = q.num4;
   p.k2_hypo0 = q.k2_hypo0;
+  p.proj = q.proj;
+  p.no_vz_kz0 = q.no_vz_kz0;
   return p;
 }
 
@@ -1284,6 +1287,18 @@ int gbs_ns_timing_report(gbs_ns* h, double* ms, int64_t* count, int nkinds,
     if (count) count[k] = s->t_count[k];
   }
   if (launches) *launches = s->launches;
+  return GBS_OK;
+}
+
+int gbs_ns_set_projection(gbs_ns* h, int projection, int no_vz_kz0) {
+  gbs::clear_error();
+  if (!h || projection < GBS_PROJ_PERPK || projection > GBS_PROJ_POLOIDAL ||
+      (h->s.p.ndim != 3 && (projection != GBS_PROJ_PERPK || no_vz_kz0))) {
+    gbs::set_error("gbs_ns_set_projection: invalid argument (ns3d only)");
+    return GBS_EINVAL;
+  }
+  h->s.q.proj = h->s.geo.proj = projection;
+  h->s.q.no_vz_kz0 = h->s.geo.no_vz_kz0 = no_vz_kz0 ? 1 : 0;
   return GBS_OK;
 }
 

@@ -65,6 +65,8 @@ struct RKArgs {
 struct Phys {
   double nu2, nu4, nu8, num4;
   double k2_hypo0;  // K2 at (0, .., 1): the value f_d_hypo[0, .., 0] copies
+  int proj;         // ns3d projection: GBS_PROJ_PERPK / _TOROIDAL / _POLOIDAL
+  int no_vz_kz0;    // ns3d: vz(kz = 0) = 0 after the projection
 };
 
 // fluidsim/base/solvers/pseudo_spect.py:166-191
@@ -205,6 +207,46 @@ __device__ __forceinline__ void project3(C (&v)[3], T kx, T ky, T kz, T k2, bool
   v[2] = csub(v[2], cscale(t, kz));
 }
 
+// toroidal projection, operators3d.py:911-959: v = (e_phi . v) e_phi
+template <typename C, typename T>
+__device__ __forceinline__ void project_toroidal(C (&v)[3], T kx, T ky) {
+  T kh2 = kx * kx + ky * ky;
+  if (kh2 == T(0)) kh2 = T(1e-14);
+  const T t = sqrt(T(1) / kh2);
+  const T cp = kx * t, sp = ky * t;
+  const C tmp = cadd(cscale(v[0], -sp), cscale(v[1], cp));
+  v[0] = cscale(tmp, -sp);
+  v[1] = cscale(tmp, cp);
+  v[2] = mk<C>(0, 0);
+}
+
+// poloidal projection, operators3d.py:788-855: v = (e_theta . v) e_theta
+template <typename C, typename T>
+__device__ __forceinline__ void project_poloidal(C (&v)[3], T kx, T ky, T kz) {
+  const T kh2 = kx * kx + ky * ky;
+  T k2n = kh2 + kz * kz, kh2n = kh2;
+  if (kh2n == T(0)) kh2n = T(1e-14);
+  if (k2n == T(0)) k2n = T(1e-14);
+  const T inv_kh2 = T(1) / kh2n, inv_k2 = T(1) / k2n;
+  const T ct = kz * sqrt(inv_k2), st = sqrt(kh2 * inv_k2);
+  const T cp = kx * sqrt(inv_kh2), sp = ky * sqrt(inv_kh2);
+  const T a = ct * cp, b = ct * sp;
+  const C tmp = csub(cadd(cscale(v[0], a), cscale(v[1], b)), cscale(v[2], st));
+  v[0] = cscale(tmp, a);
+  v[1] = cscale(tmp, b);
+  v[2] = cscale(tmp, -st);
+}
+
+// project_state_spect, ns3d/solver.py:255-263
+template <typename C, typename T>
+__device__ __forceinline__ void project_state(const Phys& q, C (&v)[3], T kx, T ky, T kz,
+                                              T k2, bool k0) {
+  if (q.proj == 1) project_toroidal(v, kx, ky);
+  else if (q.proj == 2) project_poloidal(v, kx, ky, kz);
+  else project3(v, kx, ky, kz, k2, k0);
+  if (q.no_vz_kz0 && kz == T(0)) v[2] = mk<C>(0, 0);
+}
+
 // ns3d epilogue at one mode: N (already scaled by 1/N) -> projection,
 // dealiasing, then the stage `mode` (ns3d/solver.py:251-252,
 // ns3d/time_stepping.py:12-20).
@@ -213,7 +255,7 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
                                                 int64_t nK, C (&N)[3], T kx, T ky,
                                                 T kz, T k2, bool k0, bool rm,
                                                 const Phys& q) {
-  project3(N, kx, ky, kz, k2, k0);
+  project_state(q, N, kx, ky, kz, k2, k0);
   if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
   if (a.phase) {
 #pragma unroll
@@ -228,7 +270,7 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
     C Sn[3];
 #pragma unroll
     for (int f = 0; f < 3; ++f) Sn[f] = final_value<C, T>(mode, a, i + f * nK, N[f], sig);
-    project3(Sn, kx, ky, kz, k2, k0);
+    project_state(q, Sn, kx, ky, kz, k2, k0);
     if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
     C* So = static_cast<C*>(a.Sout);
 #pragma unroll

@@ -392,10 +392,18 @@ class SimulNS3D(_SimulBase):
         tm = params._set_child("turb_model", attribs={"enable": False, "type": ""})
         tm._set_child("smagorinsky", attribs={"C": 0.18})
 
+    _PROJECTIONS = {None: 0, "toroidal": 1, "vortical": 1, "poloidal": 2}
+
     def __init__(self, params):
-        if params.no_vz_kz0 or params.projection is not None:
-            raise NotImplementedError("no_vz_kz0 / toroidal / poloidal projections")
+        if params.projection not in self._PROJECTIONS:
+            # ns3d/solver.py:171-174
+            raise ValueError("No known projection for params.projection = "
+                             f"{params.projection}")
         super().__init__(params)
+        # ns3d/solver.py:147-175: projection of the tendencies and the state
+        _lib.check(self._lib.gbs_ns_set_projection(
+            self._solver, self._PROJECTIONS[params.projection], int(bool(params.no_vz_kz0))),
+            "gbs_ns_set_projection")
         self.is_turb_model_enabled = False
         self._closure = None
         if params.forcing.enable:

@@ -288,6 +288,17 @@ int gbs_ns_spectrum_size(gbs_ns* solver, int64_t* nk);
 int gbs_ns_spectrum(gbs_ns* solver, const void* state_spect, double* spectrum,
                     void* stream);
 
+/* ns3d projection of the tendencies and of the state after each step
+ * (Simul.project_state_spect, fluidsim/solvers/ns3d/solver.py:147-175,
+ * 255-263): params.projection None / "toroidal" ("vortical") / "poloidal"
+ * -> project_perpk3d / project_toroidal / project_poloidal
+ * (fluidsim/operators/operators3d.py:788-959); no_vz_kz0 != 0 also zeroes
+ * vz at kz = 0. */
+#define GBS_PROJ_PERPK 0
+#define GBS_PROJ_TOROIDAL 1
+#define GBS_PROJ_POLOIDAL 2
+int gbs_ns_set_projection(gbs_ns* solver, int projection, int no_vz_kz0);
+
 /* *out = 1 when every mode that the 2/3 truncation removes is +0 (all bits
  * zero) in every field of state_spect, else 0; synchronises the stream.  A
  * step may then be called with GBS_STEP_DEALIASED and gives exactly the

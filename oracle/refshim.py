@@ -27,6 +27,8 @@ they pull in the parameter/IO machinery; the Simul objects are wired by hand
 below instead of by ``SimulBase.__init__``.
 """
 
+import ast
+import copy
 import importlib.util
 import sys
 import types
@@ -224,6 +226,14 @@ def load_reference(root):
     m["ns3d_ts"] = _module("fluidsim.solvers.ns3d.time_stepping",
                            fs / "solvers" / "ns3d" / "time_stepping.py")
 
+    # the reference's toroidal / poloidal projectors (methods of its
+    # OperatorsPseudoSpectral3D, whose module needs fluidfft): their function
+    # definitions are taken from operators3d.py as written and bound to the
+    # numpy operator by make_ns3d
+    ops_path = fs / "operators" / "operators3d.py"
+    for name in ("project_toroidal", "project_poloidal"):
+        m[name] = _reference_method(ops_path, "OperatorsPseudoSpectral3D", name)
+
     # turbulence model: the reference's Smagorinsky + stress tensor, with the
     # SimulExtender plumbing of turb_model/base.py replaced by a stand-in
     _module("fluidsim.base.turb_model", package=True)
@@ -241,6 +251,23 @@ def load_reference(root):
     m["smagorinsky"] = _module("fluidsim.base.turb_model.smagorinsky",
                                fs / "base" / "turb_model" / "smagorinsky.py")
     return m
+
+
+def _reference_method(path, class_name, name):
+    """Function object of method ``name`` of class ``class_name`` in the
+    reference source file ``path``, compiled from that file (decorators such
+    as transonic's ``boost`` dropped, annotations resolved to placeholders)."""
+    tree = ast.parse(Path(path).read_text(), filename=str(path))
+    for node in tree.body:
+        if isinstance(node, ast.ClassDef) and node.name == class_name:
+            for item in node.body:
+                if isinstance(item, ast.FunctionDef) and item.name == name:
+                    item.decorator_list = []
+                    mod = ast.Module(body=[item], type_ignores=[])
+                    ns = {"np": np, "Ac": object, "Af": object}
+                    exec(compile(mod, str(path), "exec"), ns)
+                    return ns[name]
+    raise LookupError(f"{class_name}.{name} not found in {path}")
 
 
 def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
@@ -279,14 +306,19 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
 
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
-              cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4"):
+              cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4",
+              projection=None, no_vz_kz0=False):
     """A reference ns3d ``Simul`` wired around ``oper``."""
     Simul = mods["ns3d_solver"].Simul
     sim = object.__new__(Simul)
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
                          deltat_max, cfl_coef,
-                         {"f": f, "no_vz_kz0": False, "projection": None},
+                         {"f": f, "no_vz_kz0": no_vz_kz0, "projection": projection},
                          type_time_scheme)
+    if projection is not None:
+        oper = copy.copy(oper)
+        for name in ("project_toroidal", "project_poloidal"):
+            setattr(oper, name, types.MethodType(mods[name], oper))
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
     mods["ns3d_state"].StateNS3D._complete_info_solver(info.solver)
     sim.info = info

@@ -300,8 +300,14 @@ class NS3DOracle(_SolverBase):
     nvar = 3
     keys_phys = ("vx", "vy", "vz")  # ns3d/state.py:20
 
-    def __init__(self, oper: OperNumpy3D, f=None, turb_model=None, **kw):
+    def __init__(self, oper: OperNumpy3D, f=None, turb_model=None, projection=None,
+                 no_vz_kz0=False, **kw):
         self.f = f
+        # ns3d/solver.py:147-175
+        self._projector = {None: oper.project_perpk3d, "toroidal": oper.project_toroidal,
+                           "vortical": oper.project_toroidal,
+                           "poloidal": oper.project_poloidal}[projection]
+        self.no_vz_kz0 = no_vz_kz0
         # callable (oper, vx_fft, vy_fft, vz_fft) -> forcing (3, *shapeK)
         self.turb_model = turb_model
         super().__init__(oper, **kw)
@@ -325,8 +331,10 @@ class NS3DOracle(_SolverBase):
         self.statespect_from_statephys()
 
     def project_state_spect(self, S):
-        """``ns3d/solver.py:255-263`` (default projector ``project_perpk3d``)."""
-        self.oper.project_perpk3d(S[0], S[1], S[2])
+        """``ns3d/solver.py:255-263``."""
+        self._projector(S[0], S[1], S[2])
+        if self.no_vz_kz0:
+            S[2][self.oper.Kz == 0] = 0.0
 
     def tendencies_nonlin(self, state_spect=None):
         """``ns3d/solver.py:180-253``."""

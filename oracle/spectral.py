@@ -202,6 +202,34 @@ class OperNumpy3D:
         vy -= self.Ky * tmp
         vz -= self.Kz * tmp
 
+    def project_toroidal(self, vx, vy, vz):
+        """In place v = (e_phi . v) e_phi, e_phi = (-sin phi_k, cos phi_k, 0)
+        (``fluidsim/operators/operators3d.py:911-959``)."""
+        kh2 = self.Kx**2 + self.Ky**2
+        kh2 = np.where(kh2 == 0, 1e-14, kh2)
+        t = np.sqrt(1.0 / kh2)
+        cp, sp = self.Kx * t, self.Ky * t
+        tmp = -sp * vx + cp * vy
+        vx[...] = -sp * tmp
+        vy[...] = cp * tmp
+        vz[...] = 0.0
+
+    def project_poloidal(self, vx, vy, vz):
+        """In place v = (e_theta . v) e_theta, e_theta = (cos theta cos phi,
+        cos theta sin phi, -sin theta) (``operators3d.py:788-855``)."""
+        kh2 = self.Kx**2 + self.Ky**2
+        k2n = kh2 + self.Kz**2
+        kh2n = np.where(kh2 == 0, 1e-14, kh2)
+        k2n = np.where(k2n == 0, 1e-14, k2n)
+        inv_kh2, inv_k2 = 1.0 / kh2n, 1.0 / k2n
+        ct = self.Kz * np.sqrt(inv_k2)
+        st = np.sqrt(kh2 * inv_k2)
+        cp, sp = self.Kx * np.sqrt(inv_kh2), self.Ky * np.sqrt(inv_kh2)
+        tmp = ct * cp * vx + ct * sp * vy - st * vz
+        vx[...] = ct * cp * tmp
+        vy[...] = ct * sp * tmp
+        vz[...] = -st * tmp
+
     def dealiasing_variable(self, arr):
         if self._has_to_dealiase:
             arr[self.where_dealiased.astype(bool)] = 0.0

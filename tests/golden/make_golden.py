@@ -83,7 +83,15 @@ CASES_3D = [
     dict(name="ns3d_eulerps_32", nx=32, ny=32, nz=32, nu_2=2e-3, USE_CFL=False,
          deltat0=2e-3, type_time_scheme="Euler_phaseshift", init="iso", seed=15,
          steps=10),
+    dict(name="ns3d_toroidal_24x20x16", nx=24, ny=20, nz=16, nu_2=5e-3, f=1.0,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, projection="toroidal",
+         init="iso", seed=16, steps=10),
+    dict(name="ns3d_poloidal_32_novz", nx=32, ny=32, nz=32, nu_2=5e-3, USE_CFL=True,
+         deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, projection="poloidal", no_vz_kz0=True,
+         init="iso", seed=17, steps=10),
 ]
+
+PROJECTION_CODES = {None: 0, "toroidal": 1, "vortical": 1, "poloidal": 2}
 
 SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
                 "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
@@ -135,8 +143,9 @@ def run_3d(mods, case):
         v0 = isotropic_3d(nx, ny, nz, *L, seed=case["seed"])
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef", "type_time_scheme"])
+    proj = dict(projection=case.get("projection"), no_vz_kz0=case.get("no_vz_kz0", False))
     sim = refshim.make_ns3d(mods, oper, f=case.get("f"),
-                            smagorinsky_C=case.get("smagorinsky_C"), **kw)
+                            smagorinsky_C=case.get("smagorinsky_C"), **proj, **kw)
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
@@ -147,7 +156,7 @@ def run_3d(mods, case):
 
         def turb(o, vx, vy, vz):
             return smagorinsky_forcing(o, vx, vy, vz, C=C)
-    orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **kw)
+    orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **proj, **kw)
     orc.init_from_vxvyvzfft(*[c.copy() for c in v0])
     assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
@@ -178,6 +187,8 @@ def _params_array(case):
            for k in keys if k in case}
     out["p_scheme"] = np.asarray(SCHEME_CODES[case.get("type_time_scheme", "RK4")],
                                  dtype=np.float64)
+    out["p_projection"] = np.asarray(PROJECTION_CODES[case.get("projection")], dtype=np.float64)
+    out["p_no_vz_kz0"] = np.asarray(float(case.get("no_vz_kz0", False)))
     return out
 
 

@@ -9,7 +9,9 @@ CASES_2D = ["ns2d_32_cfl", "ns2d_48x40_beta", "ns2d_256_c1", "ns2d_32_euler", "n
             "ns2d_32_rk2ps", "ns2d_36x32_eulerps"]
 CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20x24x16",
             "ns3d_rk2_20x15x10", "ns3d_heun_24x16x32_f", "ns3d_euler_tgv_32",
-            "ns3d_rk2ps_20x15x10", "ns3d_rk2psx_16x24x32_f", "ns3d_eulerps_32"]
+            "ns3d_rk2ps_20x15x10", "ns3d_rk2psx_16x24x32_f", "ns3d_eulerps_32",
+            "ns3d_toroidal_24x20x16", "ns3d_poloidal_32_novz"]
+PROJECTIONS = {0: None, 1: "toroidal", 2: "poloidal"}
 SCHEME_NAMES = {0: "RK4", 1: "Euler", 2: "RK2", 3: "RK2_trapezoid", 4: "Euler_phaseshift",
                 5: "RK2_phaseshift", 6: "RK2_phaseshift_exact"}
 
@@ -26,6 +28,12 @@ def load(name):
 def scheme(p):
     """type_time_scheme of a fixture (RK4 when it records none)."""
     return SCHEME_NAMES[int(p["scheme"])] if p.get("scheme") is not None else "RK4"
+
+
+def projection_kwargs(p):
+    """params.projection / no_vz_kz0 of an ns3d fixture."""
+    return {"projection": PROJECTIONS[int(p.get("projection") or 0)],
+            "no_vz_kz0": bool(p.get("no_vz_kz0") or 0)}
 
 
 def solver_kwargs(p):

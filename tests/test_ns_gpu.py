@@ -6,7 +6,7 @@ the first tendency); FP32: relative L2 <= 1e-5 after 10 steps.
 import numpy as np
 import pytest
 
-from golden_cases import CASES_2D, CASES_3D, lengths, load, scheme
+from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, scheme
 
 pytestmark = pytest.mark.gpu
 
@@ -29,6 +29,8 @@ def make_sim(name, precision="float64"):
         params.oper.nz = int(p["nz"])
         params.oper.Lz = L[2]
         params.f = p.get("f")
+        for k, v in projection_kwargs(p).items():
+            setattr(params, k, v)
         if p.get("smagorinsky_C") is not None:
             params.turb_model.enable = True
             params.turb_model.type = "smagorinsky"

@@ -6,7 +6,7 @@ Fixtures (``tests/golden/*.npz``) come from the reference's own time-scheme
 import numpy as np
 import pytest
 
-from golden_cases import CASES_2D, CASES_3D, lengths, load, solver_kwargs
+from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, solver_kwargs
 from oracle.spectral import OperNumpy2D, OperNumpy3D
 from oracle.solvers import NS2DOracle, NS3DOracle
 from oracle.turb import smagorinsky_forcing
@@ -25,7 +25,8 @@ def make_oracle(name):
 
             def turb(o, vx, vy, vz):
                 return smagorinsky_forcing(o, vx, vy, vz, C=C)
-        orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **solver_kwargs(p))
+        orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **projection_kwargs(p),
+                         **solver_kwargs(p))
     orc.state_spect[:] = d["S_init"]
     orc.state_phys[:] = d["phys_init"]
     return orc, d, p
@@ -62,6 +63,8 @@ def test_reference_tendency_conserves_energy(name):
         pytest.skip("Taylor-Green at t=0: the tendency is round-off only")
     if "smag" in name:
         pytest.skip("with a turbulence model the tendency dissipates energy")
+    if "toroidal" in name or "poloidal" in name:
+        pytest.skip("the projected tendency acts on an unprojected initial state")
     orc, d, _ = make_oracle(name)
     S, F = d["S_init"], d["tend0"]
     T = np.real(np.conj(F) * S).sum(axis=0)
