@@ -21,9 +21,9 @@ static int ensA(const Geo& g, const void* S, void* W, const void* tw, int nb, cu
   using C = cplx<float>;
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
-  int rc = prep(kf2_inv_y<float, LOGN, TX>, smem);
+  int rc = prep(kf2_inv_y<float, LOGN, TX, false>, smem);
   if (rc) return rc;
-  kf2_inv_y<float, LOGN, TX><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
+  kf2_inv_y<float, LOGN, TX, false><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
       static_cast<const C*>(S), static_cast<C*>(W), g, static_cast<const C*>(tw));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -49,9 +49,9 @@ static int ensC(const Geo& g, const void* F, const void* tw, int mode, const RKA
   using C = cplx<float>;
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
-  int rc = prep(kf2_fwd_y<float, LOGN, TX>, smem);
+  int rc = prep(kf2_fwd_y<float, LOGN, TX, false>, smem);
   if (rc) return rc;
-  kf2_fwd_y<float, LOGN, TX><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
+  kf2_fwd_y<float, LOGN, TX, false><<<dim3(ceil_div(g.ncx, TX), 1, nb), TH, smem, st>>>(
       static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a, pr);
   GBS_CHECK_LAUNCH();
   return GBS_OK;

@@ -304,6 +304,8 @@ struct Geo {
   int phase;             // multiply the input state by exp(i phi)
   double dx, dy, dz;     // grid spacings (phase factor)
   int proj, no_vz_kz0;   // ns3d projection of the tendencies and the state
+  double N2;             // ns3d.strat: Brunt-Vaisala frequency squared
+  int strat;             // ns3d.strat: 4 state fields (vx, vy, vz, b)
 };
 
 // Per-run parameters of a batched ensemble (null pointers: single run).
@@ -329,8 +331,9 @@ __device__ __forceinline__ int iy_of(const Geo& g, int b) {
   return (g.nky_keep == g.ny || b < g.kcy) ? b : b + (g.ny - g.nky_keep);
 }
 
-// A: inverse z pass with the curl (6 output fields, one after the other).
-template <typename T, int LOGN, int TX>
+// A: inverse z pass with the curl (6 output fields, one after the other;
+// ST: a 7th, the buoyancy b).
+template <typename T, int LOGN, int TX, bool ST, bool PH>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks_lo(TX * (1 << LOGN) / 8))
 kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           const cplx<T>* __restrict__ twz) {
@@ -347,7 +350,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
 #pragma unroll 1
-  for (int f = 0; f < 6; ++f) {
+  for (int f = 0; f < (ST ? 7 : 6); ++f) {
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -355,8 +358,8 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
       C x = mk<C>(0, 0);
       if (valid && (!g.pr || kept(p, P::N, g.kcz))) {
         const int64_t i = base + p * plane;
-        if (f < 3) {
-          x = S[i + f * nK];
+        if (f < 3 || f == 6) {
+          x = S[i + (f == 6 ? 3 : f) * nK];
         } else {
           const T kz = T(g.dkz * kadim(p, P::N));
           C a, b;
@@ -368,7 +371,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           const C d = mk<C>(ka * a.x - kb * b.x, ka * a.y - kb * b.y);
           x = mk<C>(-d.y, d.x);
         }
-        if (g.phase)
+        if (PH)
           x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
                                          T(g.dkz * kadim(p, P::N))));
         if (f == 5 && g.has_f && ix == 0 && iy == 0 && p == 0) x.x += T(g.f);
@@ -387,9 +390,11 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 }
 
 // B: x pass.  6 fields x L rows; C2R, v x omega, R2C of the 3 products.
+// ST (ns3d.strat): 7 fields (+ b), 6 products (v x omega, v b).
 
-template <typename T, int LOGM, int L>
-__global__ void __launch_bounds__(6 * L * (1 << LOGM) / 8, min_blocks(6 * L * (1 << LOGM) / 8))
+template <typename T, int LOGM, int L, bool ST>
+__global__ void __launch_bounds__((ST ? 7 : 6) * L * (1 << LOGM) / 8,
+                                  min_blocks((ST ? 7 : 6) * L * (1 << LOGM) / 8))
 kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
   using C = cplx<T>;
@@ -439,6 +444,12 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
     p0[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
     p0[L * LS] = mk<C>(vz.x * ox.x - vx.x * oz.x, vz.y * ox.y - vx.y * oz.y);
     p0[2 * L * LS] = mk<C>(vx.x * oy.x - vy.x * ox.x, vx.y * oy.y - vy.y * ox.y);
+    if (ST) {  // v b for the divergence of the buoyancy flux
+      const C b = p0[6 * L * LS];
+      p0[3 * L * LS] = mk<C>(vx.x * b.x, vx.y * b.y);
+      p0[4 * L * LS] = mk<C>(vy.x * b.x, vy.y * b.y);
+      p0[5 * L * LS] = mk<C>(vz.x * b.x, vz.y * b.y);
+    }
     if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
       mx = fmax(mx, fmax(fabs(vx.x), fabs(vx.y)));
       my = fmax(my, fmax(fabs(vy.x), fabs(vy.y)));
@@ -447,7 +458,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
   __syncthreads();
   if (vmax) block_max3(mx, my, mz, vmax);
-  const bool act = f < 3;
+  const bool act = f < (ST ? 6 : 3);
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
@@ -475,8 +486,14 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 }
 
 // C: forward z pass + 1/N + projection + dealiasing + RK4 stage.
-template <typename T, int LOGN, int TX>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+// ST (ns3d.strat, strat/solver.py:194-216): 6 product fields; the last three
+// (v b) are combined after their transforms into the divergence
+// i k . (v b)^ (kept in registers, then in a 4th slot), fz += b and
+// fb = -div - N^2 vz from the state the tendency is evaluated on.
+// (its field slots limit it to ~1024 resident threads per SM, so it is
+// compiled for that occupancy: <= 64 registers)
+template <typename T, int LOGN, int TX, bool ST, bool EXT>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks_lo(TX * (1 << LOGN) / 8))
 kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
           int mode, RKArgs a) {
   using C = cplx<T>;
@@ -490,17 +507,33 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
   const int64_t plane = (int64_t)g.ny * g.nkx;
   const int64_t nK = plane * g.nz;
   const int64_t base = (int64_t)iy * g.nkx + ix;
+  C dv[8];  // ST: i k . (v b)^ at the positions jt + outm(i) N/8
 #pragma unroll 1
-  for (int f = 0; f < 3; ++f) {
+  for (int f = 0; f < (ST ? 6 : 3); ++f) {
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r)
       v[r] = valid ? F[f * nK + base + (jt + r * N8) * plane] : mk<C>(0, 0);
-    C* slot = buf + f * N * TX;
+    C* slot = buf + (ST && f > 3 ? 3 : f) * N * TX;
     auto acc = [&](int p) -> C& { return slot[swz<C>(p * TX + c)]; };
     run<-1, LOGN>(v, jt, true, acc, twz, 1);
+    if (!ST || f < 3) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = v[i];
+      for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = v[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const T kj = f == 3 ? T(g.dkx * ix)
+                            : (f == 4 ? T(g.dky * kadim(iy, g.ny))
+                                      : T(g.dkz * kadim(jt + P::outm(i) * N8, N)));
+        const C t = mk<C>(-kj * v[i].y, kj * v[i].x);
+        dv[i] = f == 3 ? t : cadd(dv[i], t);
+      }
+      if (f == 5) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = dv[i];
+      }
+    }
   }
   __syncthreads();
   if (!valid) return;
@@ -516,22 +549,31 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
     if (g.pr && rm) continue;  // stays zero in S, tmp and tmp1
     const int64_t i = base + iz * plane;
     const T kz = T(g.dkz * kzi);
-    C N3[3];
+    constexpr int NV = ST ? 4 : 3;
+    C N3[NV];
 #pragma unroll
-    for (int ff = 0; ff < 3; ++ff) N3[ff] = cscale(buf[ff * N * TX + swz<C>(iz * TX + c)], inv_n);
+    for (int ff = 0; ff < NV; ++ff) N3[ff] = cscale(buf[ff * N * TX + swz<C>(iz * TX + c)], inv_n);
+    if (ST) {
+      const C* in = static_cast<const C*>(a.in);
+      const C vz = in[i + 2 * nK], b = in[i + 3 * nK];
+      N3[2] = cadd(N3[2], b);
+      const T n2 = T(g.N2);
+      N3[NV - 1] = mk<C>(-N3[NV - 1].x - n2 * vz.x, -N3[NV - 1].y - n2 * vz.y);
+    }
     if (a.add) {
 #pragma unroll
-      for (int ff = 0; ff < 3; ++ff) N3[ff] = cadd(N3[ff], static_cast<const C*>(a.add)[i + ff * nK]);
+      for (int ff = 0; ff < NV; ++ff)
+        N3[ff] = cadd(N3[ff], static_cast<const C*>(a.add)[i + ff * nK]);
     }
     const T k2 = kx * kx + ky * ky + kz * kz;
     const bool k0 = (ix == 0 && kyi == 0 && kzi == 0);
-    stage_epilogue3<C, T>(mode, a, i, nK, N3, kx, ky, kz, k2, k0, rm, q);
+    stage_epilogue3<C, T, NV, EXT>(mode, a, i, nK, N3, kx, ky, kz, k2, k0, rm, q);
   }
 }
 
 // ----------------------------------------------------- ns2d kernels
 // A: inverse y pass; fields ux, uy, d_x rot, d_y rot.
-template <typename T, int LOGN, int TX>
+template <typename T, int LOGN, int TX, bool PH>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
 kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           const cplx<T>* __restrict__ twy) {
@@ -557,7 +599,7 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
         C w = S[(int64_t)p * g.nkx + ix];
         const int kyi = kadim(p, P::N);
         const T ky = T(g.dky * kyi);
-        if (g.phase) w = cmul(w, phase_factor<C, T>(T(g.dx), T(g.dy), T(0), kx, ky, T(0)));
+        if (PH) w = cmul(w, phase_factor<C, T>(T(g.dx), T(g.dy), T(0), kx, ky, T(0)));
         T cc;
         if (f == 0 || f == 1) {
           const T k2 = kx * kx + ky * ky;
@@ -667,7 +709,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 }
 
 // C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
-template <typename T, int LOGN, int TX>
+template <typename T, int LOGN, int TX, bool EXT>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
 kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
           int mode, RKArgs a, PerRun pr) {
@@ -709,7 +751,7 @@ kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
     const bool rm = ix >= g.kcx || iabs(kyi) >= g.kcy;
     if (g.pr && rm) continue;
     const T ky = T(g.dky * kyi);
-    stage_epilogue1<C, T>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
+    stage_epilogue1<C, T, EXT>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
                           kx, ky, ix == 0 && kyi == 0, rm, q);
   }
 }

@@ -125,39 +125,46 @@ int c2r_rows(int nx, const void* k, void* x, int64_t nrows, const void* twx, cud
   return GBS_OK;
 }
 
-template <typename T, int LOGN>
+template <typename T, int LOGN, bool ST, bool PH>
 static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
   using C = cplx<T>;
   constexpr int TX = tx_invz<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
-  int rc = prep(kf3_inv_z<T, LOGN, TX>, smem);
+  int rc = prep(kf3_inv_z<T, LOGN, TX, ST, PH>, smem);
   if (rc) return rc;
   dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);
-  kf3_inv_z<T, LOGN, TX><<<grid, TH, smem, st>>>(static_cast<const C*>(S),
-                                                static_cast<C*>(W), g,
-                                                static_cast<const C*>(tw));
+  kf3_inv_z<T, LOGN, TX, ST, PH><<<grid, TH, smem, st>>>(static_cast<const C*>(S),
+                                                    static_cast<C*>(W), g,
+                                                    static_cast<const C*>(tw));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
 
 template <typename T>
 int A3(const Geo& g, const void* S, void* W, const void* twz, cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.nz), return (A3_launch<T, LG>(g, S, W, twz, st)));
+  if (g.strat) {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (A3_launch<T, LG, true, false>(g, S, W, twz, st)));
+  } else if (g.phase) {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (A3_launch<T, LG, false, true>(g, S, W, twz, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (A3_launch<T, LG, false, false>(g, S, W, twz, st)));
+  }
   return GBS_OK;
 }
 
-template <typename T, int LOGM>
+template <typename T, int LOGM, bool ST>
 static int B3_launch(const Geo& g, const void* W, void* F, const void* tw,
                      unsigned long long* vmax, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int L = rows_x<T, LOGM, 6>();
+  constexpr int NF = ST ? 7 : 6;
+  constexpr int L = rows_x<T, LOGM, NF>();
   constexpr int M = 1 << LOGM;
-  constexpr int TH = 6 * L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)6 * L * M;
-  int rc = prep(kf3_x<T, LOGM, L>, smem);
+  constexpr int TH = NF * L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)NF * L * M;
+  int rc = prep(kf3_x<T, LOGM, L, ST>, smem);
   if (rc) return rc;
-  kf3_x<T, LOGM, L><<<ceil_div((int64_t)g.nz * g.ny, L), TH, smem, st>>>(
+  kf3_x<T, LOGM, L, ST><<<ceil_div((int64_t)g.nz * g.ny, L), TH, smem, st>>>(
       static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -166,22 +173,36 @@ static int B3_launch(const Geo& g, const void* W, void* F, const void* tw,
 template <typename T>
 int B3(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
        cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.M), return (B3_launch<T, LG>(g, W, F, twx, vmax, st)));
+  if (g.strat) {
+    GBS_LOG_SWITCH(ilog2(g.M), return (B3_launch<T, LG, true>(g, W, F, twx, vmax, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.M), return (B3_launch<T, LG, false>(g, W, F, twx, vmax, st)));
+  }
   return GBS_OK;
 }
 
-template <typename T, int LOGN>
+// ns3d.strat keeps 4 field slots: narrower column tiles keep them within
+// ~64 KB of shared memory
+template <typename T, int LOGN, bool ST>
+constexpr int tx_c3() {
+  constexpr int tx = tx_fwdz<T>();
+  if (!ST) return tx;
+  constexpr int cap = (64 * 1024) / (4 * (1 << LOGN) * (int)sizeof(cplx<T>));
+  return cap >= tx ? tx : (cap >= 4 ? 4 : (cap >= 2 ? 2 : 1));
+}
+
+template <typename T, int LOGN, bool ST, bool EXT>
 static int C3_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
                      cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_fwdz<T>();
+  constexpr int TX = tx_c3<T, LOGN, ST>();
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = sizeof(C) * (size_t)3 * (1 << LOGN) * TX;
-  int rc = prep(kf3_fwd_z<T, LOGN, TX>, smem);
+  const size_t smem = sizeof(C) * (size_t)(ST ? 4 : 3) * (1 << LOGN) * TX;
+  int rc = prep(kf3_fwd_z<T, LOGN, TX, ST, EXT>, smem);
   if (rc) return rc;
   dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);
-  kf3_fwd_z<T, LOGN, TX><<<grid, TH, smem, st>>>(static_cast<const C*>(F), g,
-                                                static_cast<const C*>(tw), mode, a);
+  kf3_fwd_z<T, LOGN, TX, ST, EXT><<<grid, TH, smem, st>>>(static_cast<const C*>(F), g,
+                                                    static_cast<const C*>(tw), mode, a);
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
@@ -189,19 +210,30 @@ static int C3_launch(const Geo& g, const void* F, const void* tw, int mode, cons
 template <typename T>
 int C3(const Geo& g, const void* F, const void* twz, int mode, const RKArgs& a,
        cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG>(g, F, twz, mode, a, st)));
+  // RK4 stages and plain tendencies with the default projector use the lean
+  // epilogue
+  const bool ext = mode > kRK3 || a.phase || g.proj != 0 || g.no_vz_kz0;
+  if (g.strat && ext) {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG, true, true>(g, F, twz, mode, a, st)));
+  } else if (g.strat) {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG, true, false>(g, F, twz, mode, a, st)));
+  } else if (ext) {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG, false, true>(g, F, twz, mode, a, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.nz), return (C3_launch<T, LG, false, false>(g, F, twz, mode, a, st)));
+  }
   return GBS_OK;
 }
 
-template <typename T, int LOGN>
+template <typename T, int LOGN, bool PH>
 static int A2_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
   using C = cplx<T>;
   constexpr int TX = tx_cols<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
-  int rc = prep(kf2_inv_y<T, LOGN, TX>, smem);
+  int rc = prep(kf2_inv_y<T, LOGN, TX, PH>, smem);
   if (rc) return rc;
-  kf2_inv_y<T, LOGN, TX><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
+  kf2_inv_y<T, LOGN, TX, PH><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
       static_cast<const C*>(S), static_cast<C*>(W), g, static_cast<const C*>(tw));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -209,7 +241,11 @@ static int A2_launch(const Geo& g, const void* S, void* W, const void* tw, cudaS
 
 template <typename T>
 int A2(const Geo& g, const void* S, void* W, const void* twy, cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.ny), return (A2_launch<T, LG>(g, S, W, twy, st)));
+  if (g.phase) {
+    GBS_LOG_SWITCH(ilog2(g.ny), return (A2_launch<T, LG, true>(g, S, W, twy, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.ny), return (A2_launch<T, LG, false>(g, S, W, twy, st)));
+  }
   return GBS_OK;
 }
 
@@ -236,16 +272,16 @@ int B2(const Geo& g, const void* W, void* F, const void* twx, unsigned long long
   return GBS_OK;
 }
 
-template <typename T, int LOGN>
+template <typename T, int LOGN, bool PH>
 static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
                      cudaStream_t st) {
   using C = cplx<T>;
   constexpr int TX = tx_cols<T>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
-  int rc = prep(kf2_fwd_y<T, LOGN, TX>, smem);
+  int rc = prep(kf2_fwd_y<T, LOGN, TX, PH>, smem);
   if (rc) return rc;
-  kf2_fwd_y<T, LOGN, TX><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
+  kf2_fwd_y<T, LOGN, TX, PH><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
       static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a, PerRun{});
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -254,7 +290,11 @@ static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, cons
 template <typename T>
 int C2(const Geo& g, const void* F, const void* twy, int mode, const RKArgs& a,
        cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.ny), return (C2_launch<T, LG>(g, F, twy, mode, a, st)));
+  if (mode > kRK3 || a.phase) {
+    GBS_LOG_SWITCH(ilog2(g.ny), return (C2_launch<T, LG, true>(g, F, twy, mode, a, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.ny), return (C2_launch<T, LG, false>(g, F, twy, mode, a, st)));
+  }
   return GBS_OK;
 }
 

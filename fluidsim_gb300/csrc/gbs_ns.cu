@@ -529,9 +529,10 @@ static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, bool
     ca.es = g.nkx;
     ca.os = (int64_t)g.ny * g.nkx;
     ca.fs = s->nK;
+    const int nW = g.strat ? 7 : 6, nF = g.strat ? 6 : 3;
     {
       LaunchScope ls(s, 1, st);
-      rc = fast::col<T>(g.ny, s->W, s->W, ca, g.nz, 6, s->tw[1], 1.0, +1, st);
+      rc = fast::col<T>(g.ny, s->W, s->W, ca, g.nz, nW, s->tw[1], 1.0, +1, st);
     }
     if (rc) return rc;
     {
@@ -543,7 +544,7 @@ static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, bool
     ca.kc_out = kcy_in;
     {
       LaunchScope ls(s, 3, st);
-      rc = fast::col<T>(g.ny, s->F, s->F, ca, g.nz, 3, s->tw[1], 1.0, -1, st);
+      rc = fast::col<T>(g.ny, s->F, s->F, ca, g.nz, nF, s->tw[1], 1.0, -1, st);
     }
     return rc;
   }
@@ -668,6 +669,7 @@ template <typename T>
 static int tendencies(Solver* s, const void* S, void* tend, cudaStream_t st) {
   RKArgs a{};
   a.tend = tend;
+  a.in = S;
   int rc = eval<T>(s, S, kTend, a, false, st);
   if (rc) return rc;
   rc = turb_stage<T>(s, S, a, st);
@@ -776,6 +778,11 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     const void* in = stages[k].input == 0 ? S : (stages[k].input == 1 ? s->tmp : s->tmp1);
     const int m = stages[k].mode;
     a.phase = stages[k].phase;
+    a.in = in;
+    if (s->p.strat && stages[k].phase) {
+      set_error("phase-shift schemes are not implemented for ns3d.strat");
+      return GBS_EINVAL;
+    }
     rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr, stages[k].phase != 0);
     if (rc) return rc;
     if (k == 0 && cfl) {
@@ -822,14 +829,15 @@ static int max_velocity(Solver* s, const void* S, double* out, cudaStream_t st) 
 // sums reduced in a fixed order (deterministic for a given launch shape).
 constexpr int kRedBlocks = 304;
 constexpr int kRedThreads = 256;
-constexpr int kNQ = 6;
+constexpr int kNQ = 9;
 
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
-k_means(const cplx<T>* __restrict__ S, NSK q, int ndim, double* partial) {
+k_means(const cplx<T>* __restrict__ S, NSK q, int ndim, int strat, double inv_N2,
+        double* partial) {
   using C = cplx<T>;
   const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
-  double acc[kNQ] = {0, 0, 0, 0, 0, 0};
+  double acc[kNQ] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int ix = (int)(i % q.nkx);
@@ -860,6 +868,13 @@ k_means(const cplx<T>* __restrict__ S, NSK q, int ndim, double* partial) {
       acc[3] += w * ez;
       acc[4] += w * fd * 2 * e;
       acc[5] += w * fh * 2 * e;
+      if (strat) {  // ns3d/strat/output/spatial_means.py:27-61
+        const C bb = S[i + 3 * nK];
+        const double ea = 0.5 * inv_N2 * ((double)bb.x * bb.x + (double)bb.y * bb.y);
+        acc[6] += w * ea;
+        acc[7] += w * fd * 2 * ea;
+        acc[8] += w * fh * 2 * ea;
+      }
     } else {
       const C rt = S[i];
       const double z = 0.5 * ((double)rt.x * rt.x + (double)rt.y * rt.y);
@@ -895,8 +910,10 @@ __global__ void k_sum_partials(const double* partial, int nb, double* out) {
 
 template <typename T>
 static int spatial_means(Solver* s, const void* S, double* out, cudaStream_t st) {
+  const double inv_N2 = s->p.strat ? 1.0 / (s->p.N * s->p.N) : 0.0;
   k_means<T><<<kRedBlocks, kRedThreads, 0, st>>>(static_cast<const cplx<T>*>(S),
-                                                  s->q, s->p.ndim, s->dred);
+                                                  s->q, s->p.ndim, s->p.strat, inv_N2,
+                                                  s->dred);
   GBS_CHECK_LAUNCH();
   k_sum_partials<<<1, 32, 0, st>>>(s->dred, kRedBlocks, s->dred + kNQ * kRedBlocks);
   GBS_CHECK_LAUNCH();
@@ -1023,8 +1040,13 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   if ((p.ndim != 2 && p.ndim != 3) || (p.dtype != GBS_F32 && p.dtype != GBS_F64) ||
       p.nx < 2 || p.nx % 2 || p.ny < 1 || p.nz < 1 || (p.ndim == 2 && p.nz != 1) ||
       p.nx > 65536 || p.ny > 65535 || p.nz > 65536 || !(p.Lx > 0) || !(p.Ly > 0) ||
-      (p.ndim == 3 && !(p.Lz > 0))) {
+      (p.ndim == 3 && !(p.Lz > 0)) || (p.strat && p.ndim != 3)) {
     gbs::set_error("gbs_ns_create: invalid parameters (nx must be even)");
+    return GBS_EINVAL;
+  }
+  if (p.strat && !gbs::fast::supported(p.ndim, (int)p.nx, (int)p.ny, (int)p.nz)) {
+    gbs::set_error("gbs_ns_create: ns3d.strat runs on power-of-two grids (32..1024 per "
+                   "axis, nx/2 >= 32)");
     return GBS_EINVAL;
   }
   gbs_ns* h = new (std::nothrow) gbs_ns();
@@ -1032,7 +1054,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   Solver* s = &h->s;
   memset(s, 0, sizeof(*s));
   s->p = p;
-  s->nvar = p.ndim == 3 ? 3 : 1;
+  s->nvar = p.ndim == 3 ? (p.strat ? 4 : 3) : 1;
   gbs::NSK& q = s->q;
   q.nx = (int)p.nx;
   q.ny = (int)p.ny;
@@ -1061,10 +1083,12 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   int ns[3] = {q.nx, q.ny, q.nz};
   for (int a = 0; a < 3 && !rc; ++a) rc = gbs::twiddle_alloc(&s->tw[a], ns[a], p.dtype, 0);
   const size_t fb = s->csize * s->nK;
-  const int nW = p.ndim == 3 ? 6 : 4;
+  // inverse-transformed fields (v, omega (+ b)) and products (v x omega (+ v b))
+  const int nW = p.ndim == 3 ? (p.strat ? 7 : 6) : 4;
+  const int nF = p.ndim == 3 ? (p.strat ? 6 : 3) : 1;
   if (!rc) {
     if (cudaMalloc(&s->W, fb * nW) != cudaSuccess ||
-        cudaMalloc(&s->F, fb * s->nvar) != cudaSuccess ||
+        cudaMalloc(&s->F, fb * nF) != cudaSuccess ||
         cudaMalloc(&s->tmp, fb * s->nvar) != cudaSuccess ||
         cudaMalloc(&s->tmp1, fb * s->nvar) != cudaSuccess ||
         cudaMalloc(&s->dmax, 4 * sizeof(unsigned long long)) != cudaSuccess ||
@@ -1072,7 +1096,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
         cudaMalloc(&s->dred, sizeof(double) * (gbs::kNQ * gbs::kRedBlocks + 16)) != cudaSuccess ||
         cudaMallocHost(&s->hbuf, 8 * sizeof(double)) != cudaSuccess) {
       gbs::set_error("gbs_ns_create: device allocation failed (%zu MB requested)",
-                     (size_t)(fb * (nW + 3 * s->nvar) >> 20));
+                     (size_t)(fb * (nW + nF + 2 * s->nvar) >> 20));
       rc = GBS_ENOMEM;
     }
   }
@@ -1103,6 +1127,8 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
     g.inv_n = q.inv_n;
     g.k2_hypo0 = q.k2_hypo0;
     g.has_f = q.has_f;
+    g.strat = p.strat ? 1 : 0;
+    g.N2 = p.N * p.N;
   }
   if (!rc) {
     // tmp / tmp1 start at zero so that modes never written stay zero

@@ -35,14 +35,17 @@ __device__ __forceinline__ bool final_stage(int mode) {
 // Phase factor exp(i phi), phi = (dx kx + dy ky + dz kz) / 2 of the
 // phase-shift schemes (pseudo_spect.py:282-300), computed in the working
 // precision from the wavenumbers of the mode.
-__device__ __forceinline__ void tsincos(float x, float* s, float* c) { sincosf(x, s, c); }
-__device__ __forceinline__ void tsincos(double x, double* s, double* c) { sincos(x, s, c); }
+// sin and cos of pi x: the argument reduction of sincospi is exact and
+// short (no large-argument path, which would cost local memory in every
+// kernel that carries the phase-shift branch)
+__device__ __forceinline__ void tsincospi(float x, float* s, float* c) { sincospif(x, s, c); }
+__device__ __forceinline__ void tsincospi(double x, double* s, double* c) { sincospi(x, s, c); }
 
 template <typename C, typename T>
 __device__ __forceinline__ C phase_factor(T dx, T dy, T dz, T kx, T ky, T kz) {
   const T phi = T(0.5) * (dx * kx + dy * ky + dz * kz);
   T sn, cs;
-  tsincos(phi, &sn, &cs);
+  tsincospi(phi * T(0.31830988618379067154), &sn, &cs);  // phi / pi
   return mk<C>(cs, sn);
 }
 
@@ -59,6 +62,7 @@ struct RKArgs {
   void* tmp2;       // third buffer of RK2_phaseshift_exact
   int phase;        // divide the tendency by exp(i phi) (shifted evaluation)
   double dx, dy, dz;  // grid spacings (phase factor)
+  const void* in;   // state the tendency is evaluated on (ns3d.strat: b, vz)
 };
 
 // Viscosities for sigma(k) = f_d + f_d_hypo.
@@ -94,10 +98,12 @@ __device__ __forceinline__ float dexp(float x) { return expf(x); }
 //   kEuler (S + dt N) E                          pseudo_spect.py:51-60,279
 //   kR2b   S E + dt E2 N                         pseudo_spect.py:63-67,517
 //   kHeunB tmp1 + dt/2 N, tmp1 = (S + dt/2 N0) E pseudo_spect.py:567-569
-template <typename C, typename T>
+// EXT: compiled with the modes of the schemes other than RK4 (the fast
+// kernels instantiate an RK4-only variant, which keeps their epilogue lean).
+template <typename C, typename T, bool EXT>
 __device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C N, T sigma) {
   const T dt = T(a.dt);
-  if (mode == kRK3) {
+  if (!EXT || mode == kRK3) {
     const C t = static_cast<const C*>(a.tmp)[i];
     const T c6 = dt / T(6);
     return mk<C>(t.x + c6 * N.x, t.y + c6 * N.y);
@@ -130,12 +136,13 @@ __device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C
 // Intermediate stage update at one mode (RK4: pseudo_spect.py:898-984;
 // RK2 first stage: 505-512; RK2_trapezoid first stage: 559-567), same
 // evaluation order as the numpy expressions there.
-template <typename C, typename T>
+template <typename C, typename T, bool EXT>
 __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
                                          C N, T sigma) {
   const T dt = T(a.dt);
   C* tmp = static_cast<C*>(a.tmp);
   C* tmp1 = static_cast<C*>(a.tmp1);
+  if (!EXT && mode > kRK2) return;
   if (mode == kRK0) {
     const C S = static_cast<const C*>(a.S)[i];
     T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
@@ -156,6 +163,8 @@ __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
     C t = tmp[i];
     tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
     tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  } else if (!EXT) {
+    return;
   } else if (mode == kR2a) {
     const C S = static_cast<const C*>(a.S)[i];
     const T E2 = dexp(-dt / T(2) * sigma);
@@ -196,8 +205,8 @@ __device__ __forceinline__ C unshift(const RKArgs& a, C N, T kx, T ky, T kz) {
 }
 
 // project_perpk3d: v -= k (k.v)/|k|^2; the k = 0 mode is left unchanged
-template <typename C, typename T>
-__device__ __forceinline__ void project3(C (&v)[3], T kx, T ky, T kz, T k2, bool k0) {
+template <typename C, typename T, int NV>
+__device__ __forceinline__ void project3(C (&v)[NV], T kx, T ky, T kz, T k2, bool k0) {
   if (k0) return;
   const T inv = T(1) / k2;
   C t = mk<C>((kx * v[0].x + ky * v[1].x + kz * v[2].x) * inv,
@@ -208,8 +217,8 @@ __device__ __forceinline__ void project3(C (&v)[3], T kx, T ky, T kz, T k2, bool
 }
 
 // toroidal projection, operators3d.py:911-959: v = (e_phi . v) e_phi
-template <typename C, typename T>
-__device__ __forceinline__ void project_toroidal(C (&v)[3], T kx, T ky) {
+template <typename C, typename T, int NV>
+__device__ __forceinline__ void project_toroidal(C (&v)[NV], T kx, T ky) {
   T kh2 = kx * kx + ky * ky;
   if (kh2 == T(0)) kh2 = T(1e-14);
   const T t = sqrt(T(1) / kh2);
@@ -221,8 +230,8 @@ __device__ __forceinline__ void project_toroidal(C (&v)[3], T kx, T ky) {
 }
 
 // poloidal projection, operators3d.py:788-855: v = (e_theta . v) e_theta
-template <typename C, typename T>
-__device__ __forceinline__ void project_poloidal(C (&v)[3], T kx, T ky, T kz) {
+template <typename C, typename T, int NV>
+__device__ __forceinline__ void project_poloidal(C (&v)[NV], T kx, T ky, T kz) {
   const T kh2 = kx * kx + ky * ky;
   T k2n = kh2 + kz * kz, kh2n = kh2;
   if (kh2n == T(0)) kh2n = T(1e-14);
@@ -237,70 +246,90 @@ __device__ __forceinline__ void project_poloidal(C (&v)[3], T kx, T ky, T kz) {
   v[2] = cscale(tmp, -st);
 }
 
-// project_state_spect, ns3d/solver.py:255-263
-template <typename C, typename T>
-__device__ __forceinline__ void project_state(const Phys& q, C (&v)[3], T kx, T ky, T kz,
-                                              T k2, bool k0) {
+// project_state_spect, ns3d/solver.py:255-263: the velocity (v[0..2]) is
+// projected; no_vz_kz0 zeroes vz and, with a buoyancy field (nv = 4), b at
+// kz = 0
+template <typename C, typename T, int NV, bool EXT = true>
+__device__ __forceinline__ void project_state(const Phys& q, C (&v)[NV], T kx, T ky,
+                                              T kz, T k2, bool k0) {
+  if (!EXT) {  // the default projector only
+    project3(v, kx, ky, kz, k2, k0);
+    return;
+  }
   if (q.proj == 1) project_toroidal(v, kx, ky);
   else if (q.proj == 2) project_poloidal(v, kx, ky, kz);
   else project3(v, kx, ky, kz, k2, k0);
-  if (q.no_vz_kz0 && kz == T(0)) v[2] = mk<C>(0, 0);
+  if (q.no_vz_kz0 && kz == T(0)) {
+    v[2] = mk<C>(0, 0);
+    if (NV == 4) v[NV - 1] = mk<C>(0, 0);
+  }
 }
 
-// ns3d epilogue at one mode: N (already scaled by 1/N) -> projection,
+// ns3d epilogue at one mode for NV state fields (3: ns3d; 4: ns3d.strat,
+// velocity then buoyancy): N (already scaled by 1/N) -> projection,
 // dealiasing, then the stage `mode` (ns3d/solver.py:251-252,
-// ns3d/time_stepping.py:12-20).
-template <typename C, typename T>
+// ns3d/strat/solver.py:209-216, ns3d/time_stepping.py:12-20).
+// EXT: compiled with the modes of the other schemes, the phase-shift branch
+// and the other projections (the fast kernels instantiate a variant for RK4
+// with the default projector).
+template <typename C, typename T, int NV, bool EXT = true>
 __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64_t i,
-                                                int64_t nK, C (&N)[3], T kx, T ky,
+                                                int64_t nK, C (&N)[NV], T kx, T ky,
                                                 T kz, T k2, bool k0, bool rm,
                                                 const Phys& q) {
-  project_state(q, N, kx, ky, kz, k2, k0);
-  if (rm) N[0] = N[1] = N[2] = mk<C>(0, 0);
-  if (a.phase) {
+  project_state<C, T, NV, EXT>(q, N, kx, ky, kz, k2, k0);
+  if (rm) {
 #pragma unroll
-    for (int f = 0; f < 3; ++f) N[f] = unshift<C, T>(a, N[f], kx, ky, kz);
+    for (int f = 0; f < NV; ++f) N[f] = mk<C>(0, 0);
+  }
+  if (EXT && a.phase) {
+    const C e = phase_factor<C, T>(T(a.dx), T(a.dy), T(a.dz), kx, ky, kz);
+#pragma unroll
+    for (int f = 0; f < NV; ++f) N[f] = cmulc(N[f], e);
   }
   if (mode == kTend) {
     C* o = static_cast<C*>(a.tend);
 #pragma unroll
-    for (int f = 0; f < 3; ++f) o[i + f * nK] = N[f];
-  } else if (final_stage(mode)) {
+    for (int f = 0; f < NV; ++f) o[i + f * nK] = N[f];
+  } else if (EXT ? final_stage(mode) : mode == kRK3) {
     const T sig = (mode == kRK3 || mode == kHeunB) ? T(0) : freq_lin<T>(q, k2, k0);
-    C Sn[3];
+    C Sn[NV];
 #pragma unroll
-    for (int f = 0; f < 3; ++f) Sn[f] = final_value<C, T>(mode, a, i + f * nK, N[f], sig);
-    project_state(q, Sn, kx, ky, kz, k2, k0);
-    if (rm) Sn[0] = Sn[1] = Sn[2] = mk<C>(0, 0);
+    for (int f = 0; f < NV; ++f) Sn[f] = final_value<C, T, EXT>(mode, a, i + f * nK, N[f], sig);
+    project_state<C, T, NV, EXT>(q, Sn, kx, ky, kz, k2, k0);
+    if (rm) {
+#pragma unroll
+      for (int f = 0; f < NV; ++f) Sn[f] = mk<C>(0, 0);
+    }
     C* So = static_cast<C*>(a.Sout);
 #pragma unroll
-    for (int f = 0; f < 3; ++f) So[i + f * nK] = Sn[f];
+    for (int f = 0; f < NV; ++f) So[i + f * nK] = Sn[f];
     if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
   } else {
     const T sig = freq_lin<T>(q, k2, k0);
 #pragma unroll
-    for (int f = 0; f < 3; ++f) rk_update<C, T>(mode, a, i + f * nK, N[f], sig);
+    for (int f = 0; f < NV; ++f) rk_update<C, T, EXT>(mode, a, i + f * nK, N[f], sig);
   }
 }
 
 // ns2d epilogue at one mode (no projection).
-template <typename C, typename T>
+template <typename C, typename T, bool EXT = true>
 __device__ __forceinline__ void stage_epilogue1(int mode, const RKArgs& a, int64_t i,
                                                 C N, T kx, T ky, bool k0, bool rm,
                                                 const Phys& q) {
   const T k2 = kx * kx + ky * ky;
   if (rm) N = mk<C>(0, 0);
-  if (a.phase) N = unshift<C, T>(a, N, kx, ky, T(0));
+  if (EXT && a.phase) N = unshift<C, T>(a, N, kx, ky, T(0));
   if (mode == kTend) {
     static_cast<C*>(a.tend)[i] = N;
-  } else if (final_stage(mode)) {
+  } else if (EXT ? final_stage(mode) : mode == kRK3) {
     const T sig = (mode == kRK3 || mode == kHeunB) ? T(0) : freq_lin<T>(q, k2, k0);
-    C Sn = final_value<C, T>(mode, a, i, N, sig);
+    C Sn = final_value<C, T, EXT>(mode, a, i, N, sig);
     if (rm) Sn = mk<C>(0, 0);
     static_cast<C*>(a.Sout)[i] = Sn;
     if (isnan(Sn.x) || isnan(Sn.y)) atomicOr(a.nan_flag, 1);
   } else {
-    rk_update<C, T>(mode, a, i, N, freq_lin<T>(q, k2, k0));
+    rk_update<C, T, EXT>(mode, a, i, N, freq_lin<T>(q, k2, k0));
   }
 }
 

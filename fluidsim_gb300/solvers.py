@@ -227,12 +227,15 @@ class Output:
             self.spatial_means_series.append({"t": ts.t, **self.compute_spatial_means()})
 
     def compute_spatial_means(self):
-        out = (ctypes.c_double * 6)()
+        out = (ctypes.c_double * 9)()
         sim = self.sim
         _lib.check(sim._lib.gbs_ns_spatial_means(
             sim._solver, ctypes.c_void_p(sim.state.state_spect.data_ptr()), out,
             current_stream_handle()), "gbs_ns_spatial_means")
-        return dict(zip(sim._means_keys, list(out)))
+        means = dict(zip(sim._means_keys, list(out)))
+        if "EA" in means:  # ns3d.strat: kinetic + potential
+            means["E"] = means["EK"] + means["EA"]
+        return means
 
     def compute_energy(self):
         return self.compute_spatial_means()["E"]
@@ -445,6 +448,42 @@ class SimulNS3D(_SimulBase):
 
     def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
         """``ns3d/state.py:124-130``: set, then phys -> spect round trip."""
+        self.state.init_statespect_from(vx_fft=vx_fft, vy_fft=vy_fft, vz_fft=vz_fft)
+        X = self.state.state_phys
+        self.oper.opfft.fft_as_arg(X.contiguous(), self.state.state_spect)
+        self.state._phys = None
+
+
+class SimulNS3DStrat(SimulNS3D):
+    """``fluidsim.solvers.ns3d.strat.solver.Simul`` on GB300: Boussinesq
+    equations with a constant Brunt-Vaisala frequency ``params.N``; state
+    (vx_fft, vy_fft, vz_fft, b_fft), tendencies
+    ``P(v x omega) + b e_z`` and ``-div(v b) - N^2 v_z``
+    (``ns3d/strat/solver.py:138-216``).  Power-of-two grids only."""
+
+    keys_state_spect = ("vx_fft", "vy_fft", "vz_fft", "b_fft")
+    keys_state_phys = ("vx", "vy", "vz", "b")  # ns3d/strat/state.py:18-24
+    _means_keys = ("EK", "EKx", "EKy", "EKz", "epsK", "epsK_hypo", "EA", "epsA",
+                   "epsA_hypo")
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        SimulNS3D._complete_params_with_default(params)
+        params._set_attribs({"N": 1.0})  # ns3d/strat/solver.py:124-128
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        p.strat = 1
+        p.N = float(self.params.N)
+        return p
+
+    def _statephys_from_statespect(self, S):
+        X = torch.empty((4,) + self.oper.shapeX, dtype=self.oper.rdtype, device=self.oper.device)
+        self.oper.opfft.ifft_as_arg(S.contiguous(), X)
+        return X
+
+    def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
+        """``ns3d/strat/state.py:26-32``: b = 0, then phys -> spect round trip."""
         self.state.init_statespect_from(vx_fft=vx_fft, vy_fft=vy_fft, vz_fft=vz_fft)
         X = self.state.state_phys
         self.oper.opfft.fft_as_arg(X.contiguous(), self.state.state_spect)

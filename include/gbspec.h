@@ -98,6 +98,9 @@ typedef struct gbs_ns_params {
   int has_f;    /* ns3d: 1 when params.f is not None                   */
   int64_t kcut_x, kcut_y, kcut_z;
   int dtype;
+  int strat;    /* ns3d.strat (fluidsim/solvers/ns3d/strat/solver.py): state
+                   (vx, vy, vz, b), power-of-two grids only              */
+  double N;     /* ns3d.strat: Brunt-Vaisala frequency (params.N)        */
 } gbs_ns_params;
 
 int gbs_ns_create(const gbs_ns_params* params, gbs_ns** solver);
@@ -264,8 +267,11 @@ double gbs_cfl_update(double dt, double tmp, double cfl_coef,
 /* FP64 spatial means from the spectral state (Hermitian-weighted sums,
  * fluidsim/solvers/ns2d/output/spatial_means.py:23-36,
  * fluidsim/solvers/ns3d/output/spatial_means.py:23-40).
- * out (host): ns2d {E, Z, epsK, epsK_hypo, epsZ, epsZ_hypo};
- *             ns3d {E, Ex, Ey, Ez, epsK, epsK_hypo}.  Synchronises. */
+ * out (host, 9 doubles): ns2d {E, Z, epsK, epsK_hypo, epsZ, epsZ_hypo, 0, 0, 0};
+ *   ns3d {EK, EKx, EKy, EKz, epsK, epsK_hypo, EA, epsA, epsA_hypo} with the
+ *   potential-energy terms of ns3d.strat (EA = |b|^2 / (2 N^2),
+ *   ns3d/strat/output/spatial_means.py:27-61; zero otherwise).
+ *   Synchronises. */
 int gbs_ns_spatial_means(gbs_ns* solver, const void* state_spect, double* out,
                          void* stream);
 

@@ -225,6 +225,11 @@ def load_reference(root):
                               fs / "solvers" / "ns3d" / "state.py")
     m["ns3d_ts"] = _module("fluidsim.solvers.ns3d.time_stepping",
                            fs / "solvers" / "ns3d" / "time_stepping.py")
+    _module("fluidsim.solvers.ns3d.strat", package=True)
+    m["ns3d_strat_solver"] = _module("fluidsim.solvers.ns3d.strat.solver",
+                                     fs / "solvers" / "ns3d" / "strat" / "solver.py")
+    m["ns3d_strat_state"] = _module("fluidsim.solvers.ns3d.strat.state",
+                                    fs / "solvers" / "ns3d" / "strat" / "state.py")
 
     # the reference's toroidal / poloidal projectors (methods of its
     # OperatorsPseudoSpectral3D, whose module needs fluidfft): their function
@@ -307,25 +312,29 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
               cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4",
-              projection=None, no_vz_kz0=False):
-    """A reference ns3d ``Simul`` wired around ``oper``."""
-    Simul = mods["ns3d_solver"].Simul
+              projection=None, no_vz_kz0=False, N=None):
+    """A reference ns3d ``Simul`` wired around ``oper`` (with ``N`` given:
+    the ns3d.strat ``Simul`` and ``StateNS3DStrat``)."""
+    strat = N is not None
+    Simul = (mods["ns3d_strat_solver"] if strat else mods["ns3d_solver"]).Simul
+    State = mods["ns3d_strat_state"].StateNS3DStrat if strat else mods["ns3d_state"].StateNS3D
     sim = object.__new__(Simul)
+    extra = {"f": f, "no_vz_kz0": no_vz_kz0, "projection": projection}
+    if strat:
+        extra["N"] = N
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
-                         deltat_max, cfl_coef,
-                         {"f": f, "no_vz_kz0": no_vz_kz0, "projection": projection},
-                         type_time_scheme)
+                         deltat_max, cfl_coef, extra, type_time_scheme)
     if projection is not None:
         oper = copy.copy(oper)
         for name in ("project_toroidal", "project_poloidal"):
             setattr(oper, name, types.MethodType(mods[name], oper))
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
-    mods["ns3d_state"].StateNS3D._complete_info_solver(info.solver)
+    State._complete_info_solver(info.solver)
     sim.info = info
     sim.oper = oper
     sim.output = _OutputStub()
     sim.is_forcing_enabled = False
-    sim.state = mods["ns3d_state"].StateNS3D(sim)
+    sim.state = State(sim)
     sim.state.state_spect[:] = 0.0
     sim.state.state_phys[:] = 0.0
     sim._init_projection()

@@ -314,12 +314,12 @@ class NS3DOracle(_SolverBase):
 
     def statephys_from_statespect(self):
         """``fluidsim/base/state.py:326-333``."""
-        for ik in range(3):
+        for ik in range(self.nvar):
             self.state_phys[ik] = self.oper.ifft(self.state_spect[ik])
 
     def statespect_from_statephys(self):
         """``fluidsim/base/state.py:318-325``."""
-        for ik in range(3):
+        for ik in range(self.nvar):
             self.state_spect[ik] = self.oper.fft(self.state_phys[ik])
 
     def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
@@ -335,6 +335,8 @@ class NS3DOracle(_SolverBase):
         self._projector(S[0], S[1], S[2])
         if self.no_vz_kz0:
             S[2][self.oper.Kz == 0] = 0.0
+            if self.nvar == 4:  # b_fft
+                S[3][self.oper.Kz == 0] = 0.0
 
     def tendencies_nonlin(self, state_spect=None):
         """``ns3d/solver.py:180-253``."""
@@ -347,7 +349,7 @@ class NS3DOracle(_SolverBase):
             oz_fft[0, 0, 0] += self.f
         ox, oy, oz = oper.ifft(ox_fft), oper.ifft(oy_fft), oper.ifft(oz_fft)
         if state_spect is None:
-            vx, vy, vz = self.state_phys
+            vx, vy, vz = self.state_phys[:3]
         else:
             vx, vy, vz = oper.ifft(vx_fft), oper.ifft(vy_fft), oper.ifft(vz_fft)
         # fluidfft vector_product(v, omega) = v x omega
@@ -375,7 +377,7 @@ class NS3DOracle(_SolverBase):
 
     def compute_time_increment_CLF(self):
         """``base.py:320-339`` (``_compute_time_increment_CLF_uxuyuz``)."""
-        vx, vy, vz = self.state_phys
+        vx, vy, vz = self.state_phys[:3]
         o = self.oper
         tmp = (max_abs(vx) / o.deltax + max_abs(vy) / o.deltay
                + max_abs(vz) / o.deltaz)
@@ -396,3 +398,63 @@ class NS3DOracle(_SolverBase):
         s = self.oper.sum_wavenumbers
         return {"E": s(e_fft), "epsK": s(f_d * 2 * e_fft),
                 "epsK_hypo": s(f_d_hypo * 2 * e_fft)}
+
+
+class NS3DStratOracle(NS3DOracle):
+    """ns3d.strat: ``fluidsim/solvers/ns3d/strat/solver.py`` + ``state.py``."""
+
+    nvar = 4
+    keys_phys = ("vx", "vy", "vz", "b")  # ns3d/strat/state.py:18-24
+
+    def __init__(self, oper: OperNumpy3D, N=1.0, **kw):
+        self.N = N
+        super().__init__(oper, **kw)
+
+    def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
+        """``ns3d/strat/state.py:26-32``: b = 0, then the phys/spect round trip."""
+        self.state_spect[3] = 0.0
+        super().init_from_vxvyvzfft(vx_fft, vy_fft, vz_fft)
+
+    def tendencies_nonlin(self, state_spect=None):
+        """``ns3d/strat/solver.py:138-216``."""
+        oper = self.oper
+        S = self.state_spect if state_spect is None else state_spect
+        vx_fft, vy_fft, vz_fft, b_fft = S[0], S[1], S[2], S[3]
+        ox_fft, oy_fft, oz_fft = oper.rotfft_from_vecfft(vx_fft, vy_fft, vz_fft)
+        if self.f is not None:
+            oz_fft = oz_fft.copy()
+            oz_fft[0, 0, 0] += self.f
+        ox, oy, oz = oper.ifft(ox_fft), oper.ifft(oy_fft), oper.ifft(oz_fft)
+        if state_spect is None:
+            vx, vy, vz, b = self.state_phys
+        else:
+            vx, vy, vz = oper.ifft(vx_fft), oper.ifft(vy_fft), oper.ifft(vz_fft)
+            b = oper.ifft(b_fft)
+        F = np.empty_like(self.state_spect)
+        F[0] = oper.fft(vy * oz - vz * oy)
+        F[1] = oper.fft(vz * ox - vx * oz)
+        F[2] = oper.fft(vx * oy - vy * ox)
+        F[2] += b_fft
+        div_vb_fft = oper.div_vb_fft_from_vb(vx, vy, vz, b)
+        F[3] = -div_vb_fft - self.N**2 * vz_fft  # compute_fb_fft, solver.py:19-23
+        self.project_state_spect(F)
+        oper.dealiasing(F)
+        return F
+
+    def energy_fft(self):
+        """Kinetic + potential, ``ns3d/strat/output/__init__.py:74-84``."""
+        S = self.state_spect
+        return 0.5 * (np.abs(S[0]) ** 2 + np.abs(S[1]) ** 2 + np.abs(S[2]) ** 2
+                      + np.abs(S[3]) ** 2 / self.N**2)
+
+    def spatial_means(self):
+        """``ns3d/strat/output/spatial_means.py:27-61`` (EK, EA, dissipations)."""
+        f_d, f_d_hypo = compute_freq_diss(self.oper, self.nu_2, self.nu_4,
+                                          self.nu_8, self.nu_m4)
+        S = self.state_spect
+        ek = 0.5 * (np.abs(S[0]) ** 2 + np.abs(S[1]) ** 2 + np.abs(S[2]) ** 2)
+        ea = 0.5 * np.abs(S[3]) ** 2 / self.N**2
+        s = self.oper.sum_wavenumbers
+        return {"E": s(ek) + s(ea), "EK": s(ek), "EA": s(ea), "epsK": s(f_d * 2 * ek),
+                "epsK_hypo": s(f_d_hypo * 2 * ek), "epsA": s(f_d * 2 * ea),
+                "epsA_hypo": s(f_d_hypo * 2 * ea)}

@@ -202,6 +202,13 @@ class OperNumpy3D:
         vy -= self.Ky * tmp
         vz -= self.Kz * tmp
 
+    def div_vb_fft_from_vb(self, vx, vy, vz, b):
+        """Spectral divergence of v b for physical fields (fluidfft's
+        ``div_vb_fft_from_vb``, restated from its definition:
+        i (kx FFT(vx b) + ky FFT(vy b) + kz FFT(vz b)))."""
+        return 1j * (self.Kx * self.fft(vx * b) + self.Ky * self.fft(vy * b)
+                     + self.Kz * self.fft(vz * b))
+
     def project_toroidal(self, vx, vy, vz):
         """In place v = (e_phi . v) e_phi, e_phi = (-sin phi_k, cos phi_k, 0)
         (``fluidsim/operators/operators3d.py:911-959``)."""

@@ -24,7 +24,7 @@ sys.path.insert(0, str(HERE.parent.parent))
 
 from oracle import refshim  # noqa: E402
 from oracle.spectral import OperNumpy2D, OperNumpy3D  # noqa: E402
-from oracle.solvers import NS2DOracle, NS3DOracle  # noqa: E402
+from oracle.solvers import NS2DOracle, NS3DOracle, NS3DStratOracle  # noqa: E402
 from oracle.turb import smagorinsky_forcing  # noqa: E402
 from fluidsim_gb300.init_fields import (  # noqa: E402
     isotropic_3d, noise_rot_2d, taylor_green_3d)
@@ -89,6 +89,12 @@ CASES_3D = [
     dict(name="ns3d_poloidal_32_novz", nx=32, ny=32, nz=32, nu_2=5e-3, USE_CFL=True,
          deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, projection="poloidal", no_vz_kz0=True,
          init="iso", seed=17, steps=10),
+    dict(name="ns3d_strat_64x32x32", nx=64, ny=32, nz=32, Lx=2 * pi, Ly=pi, Lz=pi,
+         nu_2=2e-3, N=2.0, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=0.5,
+         init="iso", seed=18, b_seed=19, steps=10),
+    dict(name="ns3d_strat_64_f_rk2", nx=64, ny=64, nz=64, nu_2=1e-3, N=4.0, f=0.5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None, type_time_scheme="RK2",
+         init="iso", seed=20, b_seed=21, steps=10),
 ]
 
 PROJECTION_CODES = {None: 0, "toroidal": 1, "vortical": 1, "poloidal": 2}
@@ -144,9 +150,15 @@ def run_3d(mods, case):
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef", "type_time_scheme"])
     proj = dict(projection=case.get("projection"), no_vz_kz0=case.get("no_vz_kz0", False))
+    strat = case.get("N") is not None
     sim = refshim.make_ns3d(mods, oper, f=case.get("f"),
-                            smagorinsky_C=case.get("smagorinsky_C"), **proj, **kw)
+                            smagorinsky_C=case.get("smagorinsky_C"), N=case.get("N"),
+                            **proj, **kw)
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
+    if strat:  # a buoyancy field as well (set after the velocity round trip)
+        b0 = isotropic_3d(nx, ny, nz, *L, seed=case["b_seed"])[0]
+        sim.state.state_spect.set_var("b_fft", b0)
+        sim.state.statephys_from_statespect()
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
     tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
@@ -156,8 +168,14 @@ def run_3d(mods, case):
 
         def turb(o, vx, vy, vz):
             return smagorinsky_forcing(o, vx, vy, vz, C=C)
-    orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **proj, **kw)
+    if strat:
+        orc = NS3DStratOracle(oper, N=case["N"], f=case.get("f"), **proj, **kw)
+    else:
+        orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **proj, **kw)
     orc.init_from_vxvyvzfft(*[c.copy() for c in v0])
+    if strat:
+        orc.state_spect[3] = b0
+        orc.statephys_from_statespect()
     assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
                                rtol=0, atol=1e-13 * np.abs(tend0).max())
@@ -181,7 +199,7 @@ def run_3d(mods, case):
 def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
             "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
-            "smagorinsky_C"]
+            "smagorinsky_C", "N"]
     out = {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
                                   dtype=np.float64)
            for k in keys if k in case}

@@ -16,11 +16,14 @@ TOL_F32 = 1e-5
 
 def make_sim(name, precision="float64"):
     import torch
-    from fluidsim_gb300.solvers import SimulNS2D, SimulNS3D
+    from fluidsim_gb300.solvers import SimulNS2D, SimulNS3D, SimulNS3DStrat
     d, p = load(name)
     ndim = 2 if name.startswith("ns2d") else 3
-    Simul = SimulNS2D if ndim == 2 else SimulNS3D
+    Simul = SimulNS2D if ndim == 2 else (SimulNS3DStrat if p.get("N") is not None
+                                         else SimulNS3D)
     params = Simul.create_default_params()
+    if p.get("N") is not None:
+        params.N = p["N"]
     params.precision = precision
     params.oper.nx, params.oper.ny = int(p["nx"]), int(p["ny"])
     L = lengths(p, ndim)
@@ -88,7 +91,8 @@ def test_ten_steps_fp64(cuda, name):
 
 @pytest.mark.parametrize("name", ["ns2d_256_c1", "ns3d_iso_24x16x32_f", "ns3d_tgv_32",
                                   "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f", "ns2d_32_rk2ps",
-                                  "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f"])
+                                  "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f",
+                                  "ns3d_strat_64_f_rk2"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()
@@ -96,7 +100,8 @@ def test_ten_steps_fp32(cuda, name):
     assert err < TOL_F32, err
 
 
-@pytest.mark.parametrize("name", ["ns2d_48x40_beta", "ns3d_iso_24x16x32_f"])
+@pytest.mark.parametrize("name", ["ns2d_48x40_beta", "ns3d_iso_24x16x32_f",
+                                  "ns3d_strat_64x32x32"])
 def test_spatial_means_match_oracle(cuda, name):
     from test_oracle_golden import make_oracle
     sim, d, _ = make_sim(name)
@@ -105,8 +110,8 @@ def test_spatial_means_match_oracle(cuda, name):
     ref = orc.spatial_means()
     for k, v in ref.items():
         assert np.isclose(got[k], v, rtol=1e-12, atol=1e-300), k
-    k, E = sim.output.compute_spectrum()
-    assert np.isclose(E.sum() * (k[1] - k[0]), got["E"], rtol=1e-12)
+    k, E = sim.output.compute_spectrum()  # kinetic energy spectrum
+    assert np.isclose(E.sum() * (k[1] - k[0]), got.get("EK", got["E"]), rtol=1e-12)
 
 
 def test_tendency_conserves_energy_gpu(cuda):
@@ -115,6 +120,19 @@ def test_tendency_conserves_energy_gpu(cuda):
     S = sim.state.state_spect
     F = sim.tendencies_nonlin(S)
     T = (F.conj() * S).real.sum(dim=0)
+    ratio = sim.oper.sum_wavenumbers(T) / sim.oper.sum_wavenumbers(T.abs())
+    assert abs(ratio) < 1e-14
+
+
+def test_strat_tendency_conserves_energy_gpu(cuda):
+    """``ns3d/strat/test_solver.py:34-58`` on the GPU path: kinetic plus
+    potential (b weighted by 1 / N^2) energy transfer sums to zero."""
+    sim, d, p = make_sim("ns3d_strat_64x32x32")
+    S = sim.state.state_spect
+    F = sim.tendencies_nonlin(S)
+    T = (F.conj() * S).real
+    T[3] /= p["N"] ** 2
+    T = T.sum(dim=0)
     ratio = sim.oper.sum_wavenumbers(T) / sim.oper.sum_wavenumbers(T.abs())
     assert abs(ratio) < 1e-14
 

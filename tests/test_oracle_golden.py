@@ -8,7 +8,7 @@ import pytest
 
 from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, solver_kwargs
 from oracle.spectral import OperNumpy2D, OperNumpy3D
-from oracle.solvers import NS2DOracle, NS3DOracle
+from oracle.solvers import NS2DOracle, NS3DOracle, NS3DStratOracle
 from oracle.turb import smagorinsky_forcing
 
 
@@ -25,8 +25,12 @@ def make_oracle(name):
 
             def turb(o, vx, vy, vz):
                 return smagorinsky_forcing(o, vx, vy, vz, C=C)
-        orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **projection_kwargs(p),
-                         **solver_kwargs(p))
+        if p.get("N") is not None:
+            orc = NS3DStratOracle(oper, N=p["N"], f=p.get("f"), **projection_kwargs(p),
+                                  **solver_kwargs(p))
+        else:
+            orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **projection_kwargs(p),
+                             **solver_kwargs(p))
     orc.state_spect[:] = d["S_init"]
     orc.state_phys[:] = d["phys_init"]
     return orc, d, p
@@ -65,9 +69,12 @@ def test_reference_tendency_conserves_energy(name):
         pytest.skip("with a turbulence model the tendency dissipates energy")
     if "toroidal" in name or "poloidal" in name:
         pytest.skip("the projected tendency acts on an unprojected initial state")
-    orc, d, _ = make_oracle(name)
+    orc, d, p = make_oracle(name)
     S, F = d["S_init"], d["tend0"]
-    T = np.real(np.conj(F) * S).sum(axis=0)
+    T = np.real(np.conj(F) * S)
+    if p.get("N") is not None:  # ns3d/strat/test_solver.py:34-58: b weighted by 1/N^2
+        T[3] /= p["N"] ** 2
+    T = T.sum(axis=0)
     ratio = orc.oper.sum_wavenumbers(T) / orc.oper.sum_wavenumbers(np.abs(T))
     assert abs(ratio) < 1e-14
 
