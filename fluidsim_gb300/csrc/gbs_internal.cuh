@@ -14,10 +14,14 @@ namespace gbs {
 void set_error(const char* fmt, ...);
 void clear_error();
 
+// On failure the runtime's last-error state is consumed as well, so that a
+// non-sticky error (an invalid argument) is not reported again by the next
+// launch check of an unrelated call.
 #define GBS_CUDA_TRY(expr)                                                  \
   do {                                                                      \
     cudaError_t _e = (expr);                                                \
     if (_e != cudaSuccess) {                                                \
+      (void)cudaGetLastError();                                             \
       ::gbs::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr,          \
                        cudaGetErrorString(_e));                             \
       return GBS_ECUDA;                                                     \

@@ -367,6 +367,8 @@ k2_fwd_y_rk(const cplx<T>* __restrict__ F, NSK q, const cplx<T>* __restrict__ tw
 constexpr int kKinds = 5;     // A, inverse y, B, forward y, C
 constexpr int kMaxEv = 2048;  // event pairs recorded before a harvest
 
+constexpr int kHostBuf = 16;  // doubles in the pinned host mirror
+
 struct Solver {
   gbs_ns_params p;
   NSK q;
@@ -382,7 +384,7 @@ struct Solver {
   unsigned long long* dmax;  // 3 maxima (double bits)
   int* dflag;
   double* dred;              // reduction partials
-  double* hbuf;              // pinned host mirror (8 doubles)
+  double* hbuf;              // pinned host mirror (kHostBuf doubles)
   // per-kernel timing (CUDA events on the launching stream) + launch count
   int timing;
   int nev;                  // event pairs in use
@@ -830,6 +832,7 @@ static int max_velocity(Solver* s, const void* S, double* out, cudaStream_t st) 
 constexpr int kRedBlocks = 304;
 constexpr int kRedThreads = 256;
 constexpr int kNQ = 9;
+static_assert(kNQ <= kHostBuf, "the spatial means are read back through hbuf");
 
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
@@ -1094,7 +1097,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
         cudaMalloc(&s->dmax, 4 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&s->dflag, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&s->dred, sizeof(double) * (gbs::kNQ * gbs::kRedBlocks + 16)) != cudaSuccess ||
-        cudaMallocHost(&s->hbuf, 8 * sizeof(double)) != cudaSuccess) {
+        cudaMallocHost(&s->hbuf, gbs::kHostBuf * sizeof(double)) != cudaSuccess) {
       gbs::set_error("gbs_ns_create: device allocation failed (%zu MB requested)",
                      (size_t)(fb * (nW + nF + 2 * s->nvar) >> 20));
       rc = GBS_ENOMEM;
