@@ -49,6 +49,13 @@ template <int S, typename C> GBS_HD C mul_si(C a) {
   return S > 0 ? mk<C>(-a.y, a.x) : mk<C>(a.y, -a.x);
 }
 
+#ifdef __CUDACC__
+// 1 / x correctly rounded (the IEEE quotient 1 / x): the reciprocal
+// intrinsic in FP32, plain division in FP64.
+__device__ __forceinline__ float crcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double crcp(double x) { return 1.0 / x; }
+#endif
+
 GBS_HD bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 GBS_HD int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
 

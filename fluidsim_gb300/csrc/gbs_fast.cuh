@@ -603,7 +603,7 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
         T cc;
         if (f == 0 || f == 1) {
           const T k2 = kx * kx + ky * ky;
-          const T inv = (ix == 0 && kyi == 0) ? T(0) : T(1) / k2;
+          const T inv = (ix == 0 && kyi == 0) ? T(0) : crcp(k2);
           cc = f == 0 ? ky * inv : -(kx * inv);
         } else {
           cc = f == 2 ? kx : ky;

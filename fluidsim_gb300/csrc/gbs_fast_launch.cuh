@@ -18,9 +18,17 @@ namespace fast {
 #ifndef GBS_TX_FWDZ
 #define GBS_TX_FWDZ 8
 #endif
-template <typename T> constexpr int tx_cols() { return sizeof(T) == 4 ? GBS_TX_COL : 4; }
-template <typename T> constexpr int tx_invz() { return sizeof(T) == 4 ? GBS_TX_INVZ : 4; }
-template <typename T> constexpr int tx_fwdz() { return sizeof(T) == 4 ? GBS_TX_FWDZ : 4; }
+// (capped so that a CTA has at most 1024 threads: TX * N / 8 <= 1024)
+constexpr int tx_cap(int tx, int logn) { return tx * (1 << logn) / 8 <= 1024 ? tx : 8192 >> logn; }
+template <typename T, int LOGN> constexpr int tx_cols() {
+  return tx_cap(sizeof(T) == 4 ? GBS_TX_COL : 4, LOGN);
+}
+template <typename T, int LOGN> constexpr int tx_invz() {
+  return tx_cap(sizeof(T) == 4 ? GBS_TX_INVZ : 4, LOGN);
+}
+template <typename T, int LOGN> constexpr int tx_fwdz() {
+  return tx_cap(sizeof(T) == 4 ? GBS_TX_FWDZ : 4, LOGN);
+}
 // rows per CTA for the x passes
 template <typename T, int LOGM, int NF> constexpr int rows_x() {
   constexpr int M8 = (1 << LOGM) / 8;
@@ -56,7 +64,7 @@ template <typename T, int LOGN, int DIR>
 static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, int nfields,
                       const void* tw, double scale, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T>();
+  constexpr int TX = tx_cols<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
@@ -128,7 +136,7 @@ int c2r_rows(int nx, const void* k, void* x, int64_t nrows, const void* twx, cud
 template <typename T, int LOGN, bool ST, bool PH>
 static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_invz<T>();
+  constexpr int TX = tx_invz<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf3_inv_z<T, LOGN, TX, ST, PH>, smem);
@@ -185,7 +193,7 @@ int B3(const Geo& g, const void* W, void* F, const void* twx, unsigned long long
 // ~64 KB of shared memory
 template <typename T, int LOGN, bool ST>
 constexpr int tx_c3() {
-  constexpr int tx = tx_fwdz<T>();
+  constexpr int tx = tx_fwdz<T, LOGN>();
   if (!ST) return tx;
   constexpr int cap = (64 * 1024) / (4 * (1 << LOGN) * (int)sizeof(cplx<T>));
   return cap >= tx ? tx : (cap >= 4 ? 4 : (cap >= 2 ? 2 : 1));
@@ -228,7 +236,7 @@ int C3(const Geo& g, const void* F, const void* twz, int mode, const RKArgs& a,
 template <typename T, int LOGN, bool PH>
 static int A2_launch(const Geo& g, const void* S, void* W, const void* tw, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T>();
+  constexpr int TX = tx_cols<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf2_inv_y<T, LOGN, TX, PH>, smem);
@@ -276,7 +284,7 @@ template <typename T, int LOGN, bool PH>
 static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, const RKArgs& a,
                      cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T>();
+  constexpr int TX = tx_cols<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf2_fwd_y<T, LOGN, TX, PH>, smem);

@@ -208,7 +208,7 @@ __device__ __forceinline__ C unshift(const RKArgs& a, C N, T kx, T ky, T kz) {
 template <typename C, typename T, int NV>
 __device__ __forceinline__ void project3(C (&v)[NV], T kx, T ky, T kz, T k2, bool k0) {
   if (k0) return;
-  const T inv = T(1) / k2;
+  const T inv = crcp(k2);
   C t = mk<C>((kx * v[0].x + ky * v[1].x + kz * v[2].x) * inv,
               (kx * v[0].y + ky * v[1].y + kz * v[2].y) * inv);
   v[0] = csub(v[0], cscale(t, kx));
@@ -277,11 +277,39 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
                                                 int64_t nK, C (&N)[NV], T kx, T ky,
                                                 T kz, T k2, bool k0, bool rm,
                                                 const Phys& q) {
-  project_state<C, T, NV, EXT>(q, N, kx, ky, kz, k2, k0);
-  if (rm) {
+  if constexpr (!EXT) {  // RK4 stages and plain tendencies, default projector
+    // (zeroing by explicit assignments: the same as unrolled loops, but
+    // ptxas allocates the unrolled-loop form with spills here)
+    project3(N, kx, ky, kz, k2, k0);
+    if (rm) N[0] = N[1] = N[2] = N[NV - 1] = mk<C>(0, 0);
+    if (mode == kTend) {
+      C* o = static_cast<C*>(a.tend);
 #pragma unroll
-    for (int f = 0; f < NV; ++f) N[f] = mk<C>(0, 0);
+      for (int f = 0; f < NV; ++f) o[i + f * nK] = N[f];
+    } else if (mode == kRK3) {
+      const C* tmp = static_cast<const C*>(a.tmp);
+      const T c6 = T(a.dt) / T(6);
+      C Sn[NV];
+#pragma unroll
+      for (int f = 0; f < NV; ++f) {
+        const C t = tmp[i + f * nK];
+        Sn[f] = mk<C>(t.x + c6 * N[f].x, t.y + c6 * N[f].y);
+      }
+      project3(Sn, kx, ky, kz, k2, k0);
+      if (rm) Sn[0] = Sn[1] = Sn[2] = Sn[NV - 1] = mk<C>(0, 0);
+      C* So = static_cast<C*>(a.Sout);
+#pragma unroll
+      for (int f = 0; f < NV; ++f) So[i + f * nK] = Sn[f];
+      if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
+    } else {
+      const T sig = freq_lin<T>(q, k2, k0);
+#pragma unroll
+      for (int f = 0; f < NV; ++f) rk_update<C, T, false>(mode, a, i + f * nK, N[f], sig);
+    }
+    return;
   }
+  project_state<C, T, NV, EXT>(q, N, kx, ky, kz, k2, k0);
+  if (rm) N[0] = N[1] = N[2] = N[NV - 1] = mk<C>(0, 0);
   if (EXT && a.phase) {
     const C e = phase_factor<C, T>(T(a.dx), T(a.dy), T(a.dz), kx, ky, kz);
 #pragma unroll
@@ -297,10 +325,7 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
 #pragma unroll
     for (int f = 0; f < NV; ++f) Sn[f] = final_value<C, T, EXT>(mode, a, i + f * nK, N[f], sig);
     project_state<C, T, NV, EXT>(q, Sn, kx, ky, kz, k2, k0);
-    if (rm) {
-#pragma unroll
-      for (int f = 0; f < NV; ++f) Sn[f] = mk<C>(0, 0);
-    }
+    if (rm) Sn[0] = Sn[1] = Sn[2] = Sn[NV - 1] = mk<C>(0, 0);
     C* So = static_cast<C*>(a.Sout);
 #pragma unroll
     for (int f = 0; f < NV; ++f) So[i + f * nK] = Sn[f];
