@@ -77,6 +77,18 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def replica_rate(elapsed_ms, steps, world, dist=None, device="cpu"):
+    """Whole-job steps/s of ``world`` independent replicas that each ran
+    ``steps`` steps: all ranks' steps over the slowest rank's time (max over
+    ranks through ``dist``).  Returns (steps/s, slowest elapsed ms)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    return world * steps / (elapsed_ms / 1000.0), elapsed_ms
+
+
 def initial_state(n, ny=None, nz=None):
     from fluidsim_gb300.init_fields import isotropic_3d
     ny, nz = ny or n, nz or n
@@ -317,11 +329,7 @@ def main():
     launches = ctypes.c_int64()
     _lib.check(lib.gbs_ns_timing_report(sim._solver, ms, cnt, 5, ctypes.byref(launches)))
     _lib.check(lib.gbs_ns_timing(sim._solver, 0))
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    steps_per_s = world * args.steps / (elapsed_ms / 1000.0)
+    steps_per_s, elapsed_ms = replica_rate(elapsed_ms, args.steps, world, dist, "cuda")
 
     # roofline of the dominant kernel (largest share of the timed region)
     field_bytes = v0.shape[1] * v0.shape[2] * (n // 2 + 1) * 8  # complex64
@@ -347,6 +355,8 @@ def main():
     host_in.copy_(S)
     host_out = torch.empty_like(host_in, pin_memory=True)
     e_steps = max(3, args.steps // 4)
+    if dist:
+        dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -356,7 +366,7 @@ def main():
         host_out.copy_(S, non_blocking=True)
     e1.record()
     torch.cuda.synchronize()
-    e2e_rate = world * e_steps / (e0.elapsed_time(e1) / 1000.0)
+    e2e_rate, _ = replica_rate(e0.elapsed_time(e1), e_steps, world, dist, "cuda")
     state_bytes = S.numel() * S.element_size()
 
     line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
