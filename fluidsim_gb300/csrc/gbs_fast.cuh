@@ -63,6 +63,27 @@ __device__ __forceinline__ bool kept(int p, int n, int kc) {
   return p < kc || p > n - kc;
 }
 
+// Fetch the line holding p into L2 (writes no register).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Block coordinates of the CTA d places after this one in launch order (x
+// fastest); false for d <= 0 or past the end of the grid.  CTAs start about
+// in this order, so with d = the number of CTAs resident on the GPU the CTA
+// named starts about when this one ends: fetching its inputs into L2 now
+// overlaps their DRAM latency with this CTA's transforms.
+__device__ __forceinline__ bool cta_ahead(int d, int& bx, int& by, int& bz) {
+  if (d <= 0) return false;
+  const int64_t gx = gridDim.x, gy = gridDim.y;
+  const int64_t lin = (blockIdx.z * gy + blockIdx.y) * gx + blockIdx.x + d;
+  if (lin >= gx * gy * gridDim.z) return false;
+  bx = (int)(lin % gx);
+  by = (int)((lin / gx) % gy);
+  bz = (int)(lin / (gx * gy));
+  return true;
+}
+
 // exp(-2 pi i r / 16), r = 0..8: the x-pass pre/post-processing twiddle of
 // position jt + r M/8 of a 2M-point real line is tw[jt] times this factor.
 template <typename C>
@@ -183,6 +204,7 @@ struct ColArgs {
   int ncols;
   int kc_in, kc_out;
   int64_t es, os, fs;
+  int pf;  // L2 prefetch distance in CTAs (0: none); set by the launcher
 };
 
 template <typename T, int LOGN, int TX, int DIR>
@@ -196,6 +218,15 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
   const int col = blockIdx.x * TX + c;
   const bool valid = col < a.ncols;
   const int64_t base = blockIdx.z * a.fs + blockIdx.y * a.os + col;
+  int bx, by, bz;
+  if ((c == 0 || c == TX - 1) && cta_ahead(a.pf, bx, by, bz) && bx * TX + c < a.ncols) {
+    const int64_t bp = bz * a.fs + by * a.os + bx * TX + c;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int p = jt + r * P::N8;
+      if (kept(p, P::N, a.kc_in)) prefetch_l2(in + bp + p * a.es);
+    }
+  }
   C v[8];
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
@@ -331,15 +362,23 @@ __device__ __forceinline__ int iy_of(const Geo& g, int b) {
   return (g.nky_keep == g.ny || b < g.kcy) ? b : b + (g.ny - g.nky_keep);
 }
 
-// A: inverse z pass with the curl (6 output fields, one after the other;
-// ST: a 7th, the buoyancy b).
+// A: inverse z pass with the curl: W = (vx, vy, vz, ox, oy, oz) (ST: + b).
+// kx and ky are constant along a z line, so the curl needs only two more
+// transforms (the inverse transform commutes with multiplying by them):
+//   Tv = IFFT(v),  Dx = IFFT(i kz vx),  Dy = IFFT(i kz vy),
+//   ox = i ky Tz - Dy,  oy = Dx - i kx Tz,  oz = i kx Ty - i ky Tx,
+// 5 transforms instead of 6.  The transform kept for a later combination
+// (Ty, then Tz) waits in shared memory, each thread reading back only what
+// it wrote.
 template <typename T, int LOGN, int TX, bool ST, bool PH>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks_lo(TX * (1 << LOGN) / 8))
 kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
           const cplx<T>* __restrict__ twz) {
   using C = cplx<T>;
   using P = Line<LOGN>;
+  constexpr int TH = TX * P::N8;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
+  C* hold = buf + P::N * TX;
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
   const int ix = blockIdx.x * TX + c;
   const int iy = iy_of(g, blockIdx.y);
@@ -349,41 +388,56 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const int64_t base = (int64_t)iy * g.nkx + ix;
   const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  // job j: source field, whether it is multiplied by i kz
+  //   0: Ty   1: Tx (-> vx, oz)   2: Tz   3: Dy (-> ox)   4: Dx (-> oy)   5: b
 #pragma unroll 1
-  for (int f = 0; f < (ST ? 7 : 6); ++f) {
+  for (int j = 0; j < (ST ? 6 : 5); ++j) {
+    const int src = j == 0 || j == 3 ? 1 : (j == 1 || j == 4 ? 0 : (j == 2 ? 2 : 3));
+    const bool dz = j == 3 || j == 4;
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int p = jt + r * P::N8;
       C x = mk<C>(0, 0);
       if (valid && (!g.pr || kept(p, P::N, g.kcz))) {
-        const int64_t i = base + p * plane;
-        if (f < 3 || f == 6) {
-          x = S[i + (f == 6 ? 3 : f) * nK];
-        } else {
+        x = S[base + p * plane + src * nK];
+        if (dz) {
           const T kz = T(g.dkz * kadim(p, P::N));
-          C a, b;
-          T ka, kb;
-          // omega = i k x v: (ky vz - kz vy, kz vx - kx vz, kx vy - ky vx)
-          if (f == 3) { a = S[i + 2 * nK]; b = S[i + nK]; ka = ky; kb = kz; }
-          else if (f == 4) { a = S[i]; b = S[i + 2 * nK]; ka = kz; kb = kx; }
-          else { a = S[i + nK]; b = S[i]; ka = kx; kb = ky; }
-          const C d = mk<C>(ka * a.x - kb * b.x, ka * a.y - kb * b.y);
-          x = mk<C>(-d.y, d.x);
+          x = mk<C>(-kz * x.y, kz * x.x);
         }
         if (PH)
           x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
                                          T(g.dkz * kadim(p, P::N))));
-        if (f == 5 && g.has_f && ix == 0 && iy == 0 && p == 0) x.x += T(g.f);
       }
       v[r] = x;
     }
     run<+1, LOGN>(v, jt, true, acc, twz, 1);
-    if (valid) {
+    if (j == 0 || j == 2) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) hold[i * TH + threadIdx.x] = v[i];
+    }
+    if (!valid) continue;
+    C* Wo;
+    if (j <= 2 || j == 5) {
+      Wo = W + (j == 0 ? 1 : (j == 1 ? 0 : (j == 2 ? 2 : 6))) * nK;
+    } else {
+      Wo = W + (j == 3 ? 3 : 4) * nK;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const int p = jt + P::outm(i) * P::N8;
-        W[f * nK + base + p * plane] = v[i];
+        const C h = hold[i * TH + threadIdx.x];  // Tz
+        v[i] = j == 3 ? mk<C>(-ky * h.y - v[i].x, ky * h.x - v[i].y)
+                      : mk<C>(v[i].x + kx * h.y, v[i].y - kx * h.x);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) Wo[base + (jt + P::outm(i) * P::N8) * plane] = v[i];
+    if (j == 1) {  // oz = i kx Ty - i ky Tx (+ f: the k = 0 mode of the column kx = ky = 0)
+      const T fz = (g.has_f && ix == 0 && iy == 0) ? T(g.f) : T(0);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const C h = hold[i * TH + threadIdx.x];  // Ty
+        W[5 * nK + base + (jt + P::outm(i) * P::N8) * plane] =
+            mk<C>(-kx * h.y + ky * v[i].y + fz, kx * h.x - ky * v[i].x);
       }
     }
   }

@@ -1,6 +1,8 @@
 // Launch shapes and runtime dispatch for the compile-time-size kernels.
 #pragma once
 
+#include <cstdlib>
+
 #include "gbs_fast.cuh"
 #include "gbs_fast_api.h"
 
@@ -47,6 +49,29 @@ static int prep(K kernel, size_t smem) {
   return GBS_OK;
 }
 
+// L2 prefetch distance of the plain column passes: the CTAs resident on the
+// whole GPU (x GBS_PF from the environment, default 1; 0 turns it off).
+// (Measured at 512^3 FP32: inverse y -9 %, forward y -15 %; the same
+// prefetch slowed the curl / x / forward-z kernels, which do not use it.)
+static double env_knob(const char* name, double dflt) {
+  const char* e = getenv(name);
+  return e && *e ? atof(e) : dflt;
+}
+
+template <typename K>
+static int prefetch_distance(K kernel, int threads, size_t smem) {
+  static const double scale = env_knob("GBS_PF", 1.0);
+  int nb = 0, dev = 0, nsm = 0;
+  if (scale <= 0) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess ||
+      cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return (int)(nb * nsm * scale);
+}
+
 #define GBS_LOG_SWITCH(logv, BODY)                    \
   switch (logv) {                                     \
     case 5: { constexpr int LG = 5; BODY; } break;    \
@@ -69,9 +94,12 @@ static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, i
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
   if (rc) return rc;
+  static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR>, TH, smem);
+  ColArgs ap = a;
+  ap.pf = pf;
   dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
   kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
-                                                 static_cast<C*>(out), a,
+                                                 static_cast<C*>(out), ap,
                                                  static_cast<const C*>(tw), T(scale));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -138,7 +166,7 @@ static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaS
   using C = cplx<T>;
   constexpr int TX = tx_invz<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  const size_t smem = 2 * sizeof(C) * (size_t)(1 << LOGN) * TX;  // exchange + hold
   int rc = prep(kf3_inv_z<T, LOGN, TX, ST, PH>, smem);
   if (rc) return rc;
   dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);
