@@ -68,6 +68,23 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// Asynchronous copy of one complex value into shared memory (zeros when
+// !on; src must then still be a valid address).  Completion: cp_async_wait().
+template <typename C>
+__device__ __forceinline__ void cp_async_or_zero(C* dst, const C* src, bool on) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(C) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src),
+                 "r"(on ? 8 : 0));
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src),
+                 "r"(on ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // Block coordinates of the CTA d places after this one in launch order (x
 // fastest); false for d <= 0 or past the end of the grid.  CTAs start about
 // in this order, so with d = the number of CTAs resident on the GPU the CTA
@@ -368,8 +385,9 @@ __device__ __forceinline__ int iy_of(const Geo& g, int b) {
 //   Tv = IFFT(v),  Dx = IFFT(i kz vx),  Dy = IFFT(i kz vy),
 //   ox = i ky Tz - Dy,  oy = Dx - i kx Tz,  oz = i kx Ty - i ky Tx,
 // 5 transforms instead of 6.  The transform kept for a later combination
-// (Ty, then Tz) waits in shared memory, each thread reading back only what
-// it wrote.
+// (Ty, then Tz) waits in shared memory, and the inputs of the next transform
+// are copied asynchronously into shared memory while the current one runs;
+// each thread reads back only what it wrote in both.
 template <typename T, int LOGN, int TX, bool ST, bool PH>
 __global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks_lo(TX * (1 << LOGN) / 8))
 kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
@@ -379,6 +397,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   constexpr int TH = TX * P::N8;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   C* hold = buf + P::N * TX;
+  C* stage = hold + P::N * TX;
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
   const int ix = blockIdx.x * TX + c;
   const int iy = iy_of(g, blockIdx.y);
@@ -390,25 +409,38 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
   // job j: source field, whether it is multiplied by i kz
   //   0: Ty   1: Tx (-> vx, oz)   2: Tz   3: Dy (-> ox)   4: Dx (-> oy)   5: b
-#pragma unroll 1
-  for (int j = 0; j < (ST ? 6 : 5); ++j) {
-    const int src = j == 0 || j == 3 ? 1 : (j == 1 || j == 4 ? 0 : (j == 2 ? 2 : 3));
-    const bool dz = j == 3 || j == 4;
-    C v[8];
+  auto src_of = [](int j) { return j == 0 || j == 3 ? 1 : (j == 1 || j == 4 ? 0 : (j == 2 ? 2 : 3)); };
+  auto fetch = [&](int j) {
+    const C* Sf = S + src_of(j) * nK + base;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int p = jt + r * P::N8;
-      C x = mk<C>(0, 0);
-      if (valid && (!g.pr || kept(p, P::N, g.kcz))) {
-        x = S[base + p * plane + src * nK];
-        if (dz) {
-          const T kz = T(g.dkz * kadim(p, P::N));
-          x = mk<C>(-kz * x.y, kz * x.x);
-        }
-        if (PH)
-          x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
-                                         T(g.dkz * kadim(p, P::N))));
+      const bool on = valid && (!g.pr || kept(p, P::N, g.kcz));
+      cp_async_or_zero(&stage[r * TH + threadIdx.x], on ? Sf + p * plane : S, on);
+    }
+    cp_async_commit();
+  };
+  constexpr int NJ = ST ? 6 : 5;
+  fetch(0);
+#pragma unroll 1
+  for (int j = 0; j < NJ; ++j) {
+    const bool dz = j == 3 || j == 4;
+    C v[8];
+    cp_async_wait();
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = stage[r * TH + threadIdx.x];
+    if (j + 1 < NJ) fetch(j + 1);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int p = jt + r * P::N8;
+      C x = v[r];
+      if (dz) {
+        const T kz = T(g.dkz * kadim(p, P::N));
+        x = mk<C>(-kz * x.y, kz * x.x);
       }
+      if (PH)
+        x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
+                                       T(g.dkz * kadim(p, P::N))));
       v[r] = x;
     }
     run<+1, LOGN>(v, jt, true, acc, twz, 1);
@@ -445,6 +477,39 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 
 // B: x pass.  6 fields x L rows; C2R, v x omega, R2C of the 3 products.
 // ST (ns3d.strat): 7 fields (+ b), 6 products (v x omega, v b).
+
+// The products in physical space, in place in the field slots (slot of
+// field f, row l at (f L + l) LS; each position of each row handled by one
+// thread), and the CFL maxima of |v| over the CTA's rows.  Every thread of
+// the CTA calls it; it ends with a barrier.
+template <typename T, int L, int LS, bool ST>
+__device__ __forceinline__ void x_products(cplx<T>* buf, int64_t nrows,
+                                           unsigned long long* vmax) {
+  using C = cplx<T>;
+  T mx = 0, my = 0, mz = 0;
+  for (int idx = threadIdx.x; idx < L * LS; idx += blockDim.x) {
+    const int ll = idx / LS, j = idx % LS;
+    C* p0 = buf + ll * LS + swz<C>(j);
+    const C vx = p0[0], vy = p0[L * LS], vz = p0[2 * L * LS];
+    const C ox = p0[3 * L * LS], oy = p0[4 * L * LS], oz = p0[5 * L * LS];
+    p0[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
+    p0[L * LS] = mk<C>(vz.x * ox.x - vx.x * oz.x, vz.y * ox.y - vx.y * oz.y);
+    p0[2 * L * LS] = mk<C>(vx.x * oy.x - vy.x * ox.x, vx.y * oy.y - vy.y * ox.y);
+    if (ST) {  // v b for the divergence of the buoyancy flux
+      const C b = p0[6 * L * LS];
+      p0[3 * L * LS] = mk<C>(vx.x * b.x, vx.y * b.y);
+      p0[4 * L * LS] = mk<C>(vy.x * b.x, vy.y * b.y);
+      p0[5 * L * LS] = mk<C>(vz.x * b.x, vz.y * b.y);
+    }
+    if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
+      mx = fmax(mx, fmax(fabs(vx.x), fabs(vx.y)));
+      my = fmax(my, fmax(fabs(vy.x), fabs(vy.y)));
+      mz = fmax(mz, fmax(fabs(vz.x), fabs(vz.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, mz, vmax);
+}
 
 template <typename T, int LOGM, int L, bool ST>
 __global__ void __launch_bounds__((ST ? 7 : 6) * L * (1 << LOGM) / 8,
@@ -488,30 +553,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
   __syncthreads();
-  // products (each position of each row handled by one thread)
-  T mx = 0, my = 0, mz = 0;
-  for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
-    const int ll = idx / M, j = idx % M;
-    C* p0 = buf + ll * LS + padp<LOGM, C>(j);
-    const C vx = p0[0], vy = p0[L * LS], vz = p0[2 * L * LS];
-    const C ox = p0[3 * L * LS], oy = p0[4 * L * LS], oz = p0[5 * L * LS];
-    p0[0] = mk<C>(vy.x * oz.x - vz.x * oy.x, vy.y * oz.y - vz.y * oy.y);
-    p0[L * LS] = mk<C>(vz.x * ox.x - vx.x * oz.x, vz.y * ox.y - vx.y * oz.y);
-    p0[2 * L * LS] = mk<C>(vx.x * oy.x - vy.x * ox.x, vx.y * oy.y - vy.y * ox.y);
-    if (ST) {  // v b for the divergence of the buoyancy flux
-      const C b = p0[6 * L * LS];
-      p0[3 * L * LS] = mk<C>(vx.x * b.x, vx.y * b.y);
-      p0[4 * L * LS] = mk<C>(vy.x * b.x, vy.y * b.y);
-      p0[5 * L * LS] = mk<C>(vz.x * b.x, vz.y * b.y);
-    }
-    if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
-      mx = fmax(mx, fmax(fabs(vx.x), fabs(vx.y)));
-      my = fmax(my, fmax(fabs(vy.x), fabs(vy.y)));
-      mz = fmax(mz, fmax(fabs(vz.x), fabs(vz.y)));
-    }
-  }
-  __syncthreads();
-  if (vmax) block_max3(mx, my, mz, vmax);
+  x_products<T, L, M, ST>(buf, nrows, vmax);
   const bool act = f < (ST ? 6 : 3);
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
@@ -562,12 +604,33 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
   const int64_t nK = plane * g.nz;
   const int64_t base = (int64_t)iy * g.nkx + ix;
   C dv[8];  // ST: i k . (v b)^ at the positions jt + outm(i) N/8
+  // !ST: the inputs of field f + 1 are copied asynchronously into its (still
+  // unused) slot while field f is transformed
+  constexpr int TH = TX * N8;
+  auto fetch = [&](int f) {
+    C* st = buf + f * N * TX;
+    const C* Ff = F + f * nK + base;
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+      cp_async_or_zero(&st[r * TH + threadIdx.x], valid ? Ff + (jt + r * N8) * plane : F, valid);
+    cp_async_commit();
+  };
+  if (!ST) fetch(0);
 #pragma unroll 1
   for (int f = 0; f < (ST ? 6 : 3); ++f) {
     C v[8];
+    if (ST) {
 #pragma unroll
-    for (int r = 0; r < 8; ++r)
-      v[r] = valid ? F[f * nK + base + (jt + r * N8) * plane] : mk<C>(0, 0);
+      for (int r = 0; r < 8; ++r)
+        v[r] = valid ? F[f * nK + base + (jt + r * N8) * plane] : mk<C>(0, 0);
+    } else {
+      cp_async_wait();
+      const C* st = buf + f * N * TX;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = st[r * TH + threadIdx.x];
+      if (f < 2) fetch(f + 1);
+      __syncthreads();  // the slot becomes the exchange buffer
+    }
     C* slot = buf + (ST && f > 3 ? 3 : f) * N * TX;
     auto acc = [&](int p) -> C& { return slot[swz<C>(p * TX + c)]; };
     run<-1, LOGN>(v, jt, true, acc, twz, 1);

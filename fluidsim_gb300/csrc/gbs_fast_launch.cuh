@@ -38,12 +38,12 @@ template <typename T, int LOGM, int NF> constexpr int rows_x() {
   return budget / M8 > 0 ? budget / M8 : 1;
 }
 
+// (the opt-in is set for every size: static shared memory, e.g. of the CFL
+// reduction, counts against the 48 KB default too)
 template <typename K>
 static int prep(K kernel, size_t smem) {
-  if (smem > 48 * 1024) {
-    GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-  }
+  GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
   GBS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                     cudaSharedmemCarveoutMaxShared));
   return GBS_OK;
@@ -166,7 +166,7 @@ static int A3_launch(const Geo& g, const void* S, void* W, const void* tw, cudaS
   using C = cplx<T>;
   constexpr int TX = tx_invz<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = 2 * sizeof(C) * (size_t)(1 << LOGN) * TX;  // exchange + hold
+  const size_t smem = 3 * sizeof(C) * (size_t)(1 << LOGN) * TX;  // exchange, hold, stage
   int rc = prep(kf3_inv_z<T, LOGN, TX, ST, PH>, smem);
   if (rc) return rc;
   dim3 grid(ceil_div(g.ncx, TX), g.nky_keep);

@@ -24,7 +24,7 @@ def run_3d(shape, precision, steps, **kw):
     from oracle.solvers import NS3DOracle
     from oracle.spectral import OperNumpy3D
     nz, ny, nx = shape
-    L = (2 * pi, 2 * pi * ny / nx, 2 * pi * nz / nx)
+    L = kw.get("L", (2 * pi, 2 * pi * ny / nx, 2 * pi * nz / nx))
     p = SimulNS3D.create_default_params()
     p.precision = precision
     p.oper.nx, p.oper.ny, p.oper.nz = nx, ny, nz
@@ -80,6 +80,47 @@ def test_ns3d_fast_fp32_error(cuda):
     assert rel(got, orc.state_spect) < 1e-5
 
 
+def test_ns3d_fast_fp32_nx512_error(cuda):
+    """nx = 512 in FP32 runs the 16 x 16 x pass (CFL maxima and f included)."""
+    # a 2 pi cube: the energetic modes (|k| ~ 4) vary along y and z too
+    sim, orc = run_3d((32, 32, 512), "float32", 6, USE_CFL=True, cfl_coef=0.5, f=0.7,
+                      L=(2 * pi,) * 3)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
+    assert abs(sim.time_stepping.deltat - orc.deltat) <= 1e-5 * orc.deltat
+
+
+def test_ns3d_strat_fast_fp32_nx512_error(cuda):
+    """ns3d.strat with nx = 512 in FP32 (the 7-field 16 x 16 x pass)."""
+    import torch
+    from fluidsim_gb300.init_fields import isotropic_3d
+    from fluidsim_gb300.solvers import SimulNS3DStrat
+    from oracle.solvers import NS3DStratOracle
+    from oracle.spectral import OperNumpy3D
+    nz, ny, nx = 32, 32, 512
+    L = (2 * pi,) * 3
+    p = SimulNS3DStrat.create_default_params()
+    p.precision = "float32"
+    p.N = 2.0
+    p.oper.nx, p.oper.ny, p.oper.nz = nx, ny, nz
+    p.oper.Lx, p.oper.Ly, p.oper.Lz = L
+    p.nu_2 = 2e-3
+    ts = p.time_stepping
+    ts.USE_CFL, ts.deltat0, ts.USE_T_END, ts.it_end = False, 5e-3, False, 5
+    sim = SimulNS3DStrat(p)
+    v0 = isotropic_3d(nx, ny, nz, *L, seed=11)
+    b0 = isotropic_3d(nx, ny, nz, *L, seed=12)[0]
+    sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2], b_fft=b0)
+    sim.time_stepping.start()
+    orc = NS3DStratOracle(OperNumpy3D(nx, ny, nz, *L), N=2.0, nu_2=2e-3, deltat0=5e-3)
+    orc.state_spect[:3] = v0
+    orc.state_spect[3] = b0
+    orc.statephys_from_statespect()
+    orc.run(it_end=5)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
+
+
 def test_ns3d_fast_tendency_matches_oracle(cuda):
     import torch
     from fluidsim_gb300.init_fields import isotropic_3d
@@ -128,8 +169,10 @@ def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl, scheme):
     assert rel(sim.state.state_spect.cpu().numpy(), orc.state_spect) < 1e-12
 
 
-@pytest.mark.parametrize("precision", ["float32", "float64"])
-def test_pruned_step_is_bit_identical_and_detected(cuda, precision):
+@pytest.mark.parametrize("precision,shape", [("float32", (64, 64, 64)),
+                                             ("float64", (64, 64, 64)),
+                                             ("float32", (32, 32, 512))])
+def test_pruned_step_is_bit_identical_and_detected(cuda, precision, shape):
     """gbs_ns_is_dealiased accepts only states that are +0 outside the 2/3
     box; on such a state the pruned step equals the unpruned one bit for
     bit."""
@@ -139,13 +182,15 @@ def test_pruned_step_is_bit_identical_and_detected(cuda, precision):
     from fluidsim_gb300.fft import current_stream_handle
     from fluidsim_gb300.init_fields import isotropic_3d
     from fluidsim_gb300.solvers import SimulNS3D
-    n = 64
+    nz, ny, nx = shape
+    L = (2 * pi,) * 3
     p = SimulNS3D.create_default_params()
     p.precision = precision
-    p.oper.nx = p.oper.ny = p.oper.nz = n
+    p.oper.nx, p.oper.ny, p.oper.nz = nx, ny, nz
+    p.oper.Lx, p.oper.Ly, p.oper.Lz = L
     p.nu_2 = 1e-3
     sim = SimulNS3D(p)
-    v0 = isotropic_3d(n, n, n, seed=5)
+    v0 = isotropic_3d(nx, ny, nz, *L, seed=5)
     sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2])
     sim.oper.dealiasing(sim.state.state_spect)
     lib, h = sim._lib, sim._solver
