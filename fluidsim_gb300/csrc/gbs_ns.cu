@@ -385,6 +385,7 @@ struct Solver {
   int* dflag;
   double* dred;              // reduction partials
   double* hbuf;              // pinned host mirror (kHostBuf doubles)
+  double* hbuf_dev;          // the same memory in the device address space
   // per-kernel timing (CUDA events on the launching stream) + launch count
   int timing;
   int nev;                  // event pairs in use
@@ -679,6 +680,26 @@ static int tendencies(Solver* s, const void* S, void* tend, cudaStream_t st) {
   return finish<T>(s, kTend, a, st);
 }
 
+// Small results (maxima, flags, means) reach the host through the pinned
+// mirror, written by a kernel in the device address space of that host
+// memory rather than copied: a copy would wait behind the bulk transfers
+// that other streams may have queued on the copy engines.
+__global__ void k_publish(const unsigned* __restrict__ src, unsigned* dst, int nwords) {
+  if (threadIdx.x < nwords) dst[threadIdx.x] = src[threadIdx.x];
+}
+
+// bytes (a multiple of 4, at most 128) from device memory to hbuf[slot...];
+// waits for the stream
+static int publish(Solver* s, const void* src, int slot, size_t bytes, cudaStream_t st) {
+  k_publish<<<1, 32, 0, st>>>(static_cast<const unsigned*>(src),
+                              reinterpret_cast<unsigned*>(s->hbuf_dev + slot),
+                              (int)(bytes / sizeof(unsigned)));
+  GBS_CHECK_LAUNCH();
+  ++s->launches;
+  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  return GBS_OK;
+}
+
 double cfl_rule(double dt, double tmp, double cfl, double dtmax) {
   // fluidsim/base/time_stepping/base.py:334-354
   double deltat_CFL = tmp > 0 ? cfl / tmp : dtmax;
@@ -788,9 +809,8 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr, stages[k].phase != 0);
     if (rc) return rc;
     if (k == 0 && cfl) {
-      GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
-                                   cudaMemcpyDeviceToHost, st));
-      GBS_CUDA_TRY(cudaStreamSynchronize(st));
+      rc = publish(s, s->dmax, 0, 3 * sizeof(double), st);
+      if (rc) return rc;
       *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
     }
     a.dt = *dt;
@@ -800,9 +820,8 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     if (rc) return rc;
   }
   if (check_nan) {
-    GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf + 4, s->dflag, sizeof(int),
-                                 cudaMemcpyDeviceToHost, st));
-    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    rc = publish(s, s->dflag, 4, sizeof(int), st);
+    if (rc) return rc;
     int flag;
     memcpy(&flag, s->hbuf + 4, sizeof(int));
     if (flag) {
@@ -819,9 +838,8 @@ static int max_velocity(Solver* s, const void* S, double* out, cudaStream_t st) 
   GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
   int rc = eval<T>(s, S, kTend, a, true, st);
   if (rc) return rc;
-  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dmax, 3 * sizeof(double),
-                               cudaMemcpyDeviceToHost, st));
-  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  rc = publish(s, s->dmax, 0, 3 * sizeof(double), st);
+  if (rc) return rc;
   for (int i = 0; i < s->p.ndim; ++i) out[i] = s->hbuf[i];
   return GBS_OK;
 }
@@ -920,9 +938,8 @@ static int spatial_means(Solver* s, const void* S, double* out, cudaStream_t st)
   GBS_CHECK_LAUNCH();
   k_sum_partials<<<1, 32, 0, st>>>(s->dred, kRedBlocks, s->dred + kNQ * kRedBlocks);
   GBS_CHECK_LAUNCH();
-  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf, s->dred + kNQ * kRedBlocks,
-                               kNQ * sizeof(double), cudaMemcpyDeviceToHost, st));
-  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  const int rc = publish(s, s->dred + kNQ * kRedBlocks, 0, kNQ * sizeof(double), st);
+  if (rc) return rc;
   for (int k = 0; k < kNQ; ++k) out[k] = s->hbuf[k];
   return GBS_OK;
 }
@@ -1097,7 +1114,9 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
         cudaMalloc(&s->dmax, 4 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&s->dflag, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&s->dred, sizeof(double) * (gbs::kNQ * gbs::kRedBlocks + 16)) != cudaSuccess ||
-        cudaMallocHost(&s->hbuf, gbs::kHostBuf * sizeof(double)) != cudaSuccess) {
+        cudaHostAlloc(&s->hbuf, gbs::kHostBuf * sizeof(double), cudaHostAllocMapped) !=
+            cudaSuccess ||
+        cudaHostGetDevicePointer(&s->hbuf_dev, s->hbuf, 0) != cudaSuccess) {
       gbs::set_error("gbs_ns_create: device allocation failed (%zu MB requested)",
                      (size_t)(fb * (nW + nF + 2 * s->nvar) >> 20));
       rc = GBS_ENOMEM;
@@ -1348,8 +1367,8 @@ int gbs_ns_is_dealiased(gbs_ns* h, const void* S, int* out, void* stream) {
         static_cast<const float2*>(S), s->q, s->nvar, s->dflag);
   GBS_CHECK_LAUNCH();
   ++s->launches;
-  GBS_CUDA_TRY(cudaMemcpyAsync(s->hbuf + 5, s->dflag, sizeof(int), cudaMemcpyDeviceToHost, st));
-  GBS_CUDA_TRY(cudaStreamSynchronize(st));
+  const int rc = gbs::publish(s, s->dflag, 5, sizeof(int), st);
+  if (rc) return rc;
   int flag;
   memcpy(&flag, s->hbuf + 5, sizeof(int));
   *out = flag ? 0 : 1;
