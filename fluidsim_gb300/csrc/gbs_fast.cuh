@@ -50,8 +50,12 @@ struct Line {
 // Shared-memory swizzle: XOR the element index inside each 128-byte bank
 // sweep (E = 128 / sizeof(C) elements) with the index of the sweep, so the
 // strided Stockham writes, the unit-stride reads and the column-tile
-// accesses all spread over the 32 banks.  A permutation inside every
-// E-aligned group, so any E-aligned slot keeps its extent.
+// accesses spread over the 32 banks.  A permutation inside every E-aligned
+// group, so any E-aligned slot keeps its extent.  (Two 8-byte writes of a
+// half-warp still share a bank in the first-stage writes of the 8-column
+// tiles and the second-stage writes of the rows, 1.2x the ideal wavefronts;
+// XOR-ing with x ^ (x << 1) instead removes that but its extra address
+// arithmetic made the issue-bound passes 5-13 % slower at 512^3.)
 template <typename C>
 __device__ __forceinline__ int swz(int q) {
   constexpr int E = 128 / sizeof(C);
@@ -284,21 +288,26 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
   for (int r = 0; r < 8; ++r) v[r] = valid ? xc[jt + r * M8] : mk<C>(0, 0);
   C* slot = buf + l * LS;
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
-  run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
+  constexpr bool WARP = Line<LOGM>::N8 <= 32;
+  run<-1, LOGM, WARP>(v, jt, true, acc, twx, 2);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
-  __syncthreads();
+  if (WARP) __syncwarp(); else __syncthreads();
+  if (!valid) return;
+  // X[k] and X[M - k] -> spectrum k = jt + r M/8 (and k = M for jt = 0),
+  // the twiddle derived from tw[jt] as in the x pass
+  const C t0 = twx[jt];
   const T h = T(0.5);
-  for (int idx = threadIdx.x; idx < L * NKX; idx += blockDim.x) {
-    const int k = idx % NKX, ll = idx / NKX;
-    const int64_t rr = (int64_t)blockIdx.x * L + ll;
-    if (rr >= nrows) continue;
-    const C* sl = buf + ll * LS;
-    C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
-    C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
+  C* o = out + row * NKX;
+#pragma unroll
+  for (int r = 0; r <= 8; ++r) {
+    if (r == 8 && jt != 0) continue;
+    const int k = r < 8 ? jt + r * M8 : M;
+    const C a = acc(k == M ? 0 : k);
+    const C b = cconj(acc(k == 0 ? 0 : M - k));
     const C s = cadd(a, b), d = csub(a, b);
-    const C wd = cmul(twx[k], d);
-    out[rr * NKX + k] = cscale(mk<C>(h * (s.x + wd.y), h * (s.y - wd.x)), scale);
+    const C wd = cmul(r < 8 ? twx_at(twx, t0, jt, r, M8) : twx[M], d);
+    o[k] = cscale(mk<C>(h * (s.x + wd.y), h * (s.y - wd.x)), scale);
   }
 }
 
