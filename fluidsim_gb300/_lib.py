@@ -32,6 +32,8 @@ EXPORTED = (
     "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
     "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
+    "gbs_ens2d_mixed_create", "gbs_ens2d_mixed_destroy", "gbs_ens2d_mixed_step",
+    "gbs_ens2d_mixed_set_tuning",
     "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
@@ -107,6 +109,13 @@ def _declare(lib):
         "gbs_ens2d_set_tuning": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
         "gbs_ens2d_step": (ctypes.c_int, [P, P, ctypes.c_int, ctypes.c_int, P]),
         "gbs_ens2d_nan_flag": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "gbs_ens2d_mixed_create": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int,
+                                                  ctypes.POINTER(P)]),
+        "gbs_ens2d_mixed_destroy": (ctypes.c_int, [P]),
+        "gbs_ens2d_mixed_set_tuning": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int,
+                                                      ctypes.c_int]),
+        "gbs_ens2d_mixed_step": (ctypes.c_int, [P, ctypes.POINTER(P), ctypes.c_int,
+                                                ctypes.c_int, P]),
         "gbs_spectral_resample": (ctypes.c_int, [I64P, I64P, ctypes.c_int, DP,
                                                  ctypes.c_double, ctypes.c_int, P, P, P]),
         "gbs_products6": (ctypes.c_int, [P, P, ctypes.c_int64, P, ctypes.c_int, P]),

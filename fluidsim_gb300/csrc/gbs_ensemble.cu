@@ -89,6 +89,133 @@ static int ensC(const Geo& g, const void* F, const void* tw, int mode, const RKA
       return GBS_EINVAL;                              \
   }
 
+// ------------------------------------------------ one launch for all sizes
+// Groups of different sizes advanced by one launch per pass: every CTA finds
+// its group from the launch's CTA offsets and runs that size's compiled
+// body.  All CTAs of a launch have TH threads and TH * 64 bytes of shared
+// memory: the column passes take TH * 8 / ny columns per CTA, the x pass
+// 2 TH / (nx / 2) rows.  TH per pass is the autotuner's choice.
+constexpr int kMixMax = 4;
+
+struct MixGroup {
+  Geo g;
+  const void* in;  // stage input (the state or tmp1)
+  void *W, *F;
+  const void *twx, *twy;
+  RKArgs a;
+  PerRun pr;
+  int logy, logm;
+  int ctaA, ctaB, ctaC;  // CTAs per run of each pass
+  int startA, startB, startC;
+};
+
+struct MixArgs {
+  MixGroup grp[kMixMax];
+  int ngroups;
+  int mode;
+};
+
+__device__ __forceinline__ int mix_group(const MixArgs& m, int pass) {
+  int gi = 0;
+  for (int k = 1; k < m.ngroups; ++k) {
+    const int st = pass == 0 ? m.grp[k].startA : (pass == 1 ? m.grp[k].startB : m.grp[k].startC);
+    if ((int)blockIdx.x >= st) gi = k;
+  }
+  return gi;
+}
+
+// column width for ny = 2^LOGN at TH threads (>= 4 is checked on the host)
+template <int TH, int LOGN> struct MixTX {
+  static constexpr int v = (TH * 8 >> LOGN) < 1 ? 1 : (TH * 8 >> LOGN);
+};
+template <int TH, int LOGM> struct MixRows {
+  static constexpr int v = (2 * TH >> LOGM) < 1 ? 1 : (2 * TH >> LOGM);
+};
+
+template <int TH>
+__global__ void __launch_bounds__(TH, min_blocks(TH)) kmix_inv_y(const __grid_constant__ MixArgs m) {
+  const MixGroup& G = m.grp[mix_group(m, 0)];
+  const int local = blockIdx.x - G.startA;
+  const uint3 b = make_uint3(local % G.ctaA, 0, local / G.ctaA);
+  const float2* S = static_cast<const float2*>(G.in);
+  float2* W = static_cast<float2*>(G.W);
+  const float2* tw = static_cast<const float2*>(G.twy);
+  switch (G.logy) {
+    case 6: kf2_inv_y_body<float, 6, MixTX<TH, 6>::v, false>(S, W, G.g, tw, b); break;
+    case 7: kf2_inv_y_body<float, 7, MixTX<TH, 7>::v, false>(S, W, G.g, tw, b); break;
+    case 8: kf2_inv_y_body<float, 8, MixTX<TH, 8>::v, false>(S, W, G.g, tw, b); break;
+    default: kf2_inv_y_body<float, 9, MixTX<TH, 9>::v, false>(S, W, G.g, tw, b); break;
+  }
+}
+
+template <int TH>
+__global__ void __launch_bounds__(TH, TH >= 512 ? 2 : 1024 / TH)
+kmix_x(const __grid_constant__ MixArgs m) {
+  const MixGroup& G = m.grp[mix_group(m, 1)];
+  const int local = blockIdx.x - G.startB;
+  const uint3 b = make_uint3(local % G.ctaB, local / G.ctaB, 0);
+  const float2* W = static_cast<const float2*>(G.W);
+  float2* F = static_cast<float2*>(G.F);
+  const float2* tw = static_cast<const float2*>(G.twx);
+  switch (G.logm) {
+    case 5: kf2_x_body<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 6: kf2_x_body<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 7: kf2_x_body<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 8: kf2_x_body<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
+    default: kf2_x_body<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
+  }
+}
+
+template <int TH>
+__global__ void __launch_bounds__(TH, min_blocks_lo(TH)) kmix_fwd_y(const __grid_constant__ MixArgs m) {
+  const MixGroup& G = m.grp[mix_group(m, 2)];
+  const int local = blockIdx.x - G.startC;
+  const uint3 b = make_uint3(local % G.ctaC, 0, local / G.ctaC);
+  const float2* F = static_cast<const float2*>(G.F);
+  const float2* tw = static_cast<const float2*>(G.twy);
+  switch (G.logy) {
+    case 6: kf2_fwd_y_body<float, 6, MixTX<TH, 6>::v, false>(F, G.g, tw, m.mode, G.a, G.pr, b); break;
+    case 7: kf2_fwd_y_body<float, 7, MixTX<TH, 7>::v, false>(F, G.g, tw, m.mode, G.a, G.pr, b); break;
+    case 8: kf2_fwd_y_body<float, 8, MixTX<TH, 8>::v, false>(F, G.g, tw, m.mode, G.a, G.pr, b); break;
+    default: kf2_fwd_y_body<float, 9, MixTX<TH, 9>::v, false>(F, G.g, tw, m.mode, G.a, G.pr, b); break;
+  }
+}
+
+#define GBS_MIX_TH(th, BODY)                          \
+  switch (th) {                                       \
+    case 128: { constexpr int THV = 128; BODY; } break; \
+    case 256: { constexpr int THV = 256; BODY; } break; \
+    case 512: { constexpr int THV = 512; BODY; } break; \
+    default:                                          \
+      set_error("ensemble: thread count not compiled"); \
+      return GBS_EINVAL;                              \
+  }
+
+template <int TH> static int mixA(const MixArgs& m, int ncta, cudaStream_t st) {
+  const size_t smem = (size_t)TH * 64;
+  int rc = prep(kmix_inv_y<TH>, smem);
+  if (rc) return rc;
+  kmix_inv_y<TH><<<ncta, TH, smem, st>>>(m);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+template <int TH> static int mixB(const MixArgs& m, int ncta, cudaStream_t st) {
+  const size_t smem = (size_t)TH * 64;
+  int rc = prep(kmix_x<TH>, smem);
+  if (rc) return rc;
+  kmix_x<TH><<<ncta, TH, smem, st>>>(m);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+template <int TH> static int mixC(const MixArgs& m, int ncta, cudaStream_t st) {
+  const size_t smem = (size_t)TH * 64;
+  int rc = prep(kmix_fwd_y<TH>, smem);
+  if (rc) return rc;
+  kmix_fwd_y<TH><<<ncta, TH, smem, st>>>(m);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
 }  // namespace fast
 
 struct Ensemble {
@@ -134,9 +261,153 @@ static int ens_eval(Ensemble* e, const void* in, int mode, const RKArgs& a, bool
   return rc;
 }
 
+// Groups stepped by one launch per pass (they are not owned).
+struct EnsembleMix {
+  Ensemble* e[fast::kMixMax];
+  int n;
+  int thA, thB, thC;  // threads per CTA of the inverse, x and forward passes
+};
+
+// every group's tiles at these thread counts: columns 4..64 wide, >= 1 row
+static bool mix_fits(const EnsembleMix* x, int thA, int thB, int thC) {
+  for (int k = 0; k < x->n; ++k) {
+    const Ensemble* e = x->e[k];
+    for (int th : {thA, thC}) {
+      const int tx = th * 8 / e->ny;
+      if (tx < 4 || tx > 64) return false;
+    }
+    if (2 * thB / (e->nx / 2) < 1) return false;
+  }
+  return true;
+}
+
+static int mix_eval(EnsembleMix* x, void* const* states, int mode, bool pr, cudaStream_t st) {
+  fast::MixArgs m;
+  memset(&m, 0, sizeof(m));
+  m.ngroups = x->n;
+  m.mode = mode;
+  int a0 = 0, b0 = 0, c0 = 0;
+  for (int k = 0; k < x->n; ++k) {
+    Ensemble* e = x->e[k];
+    fast::MixGroup& G = m.grp[k];
+    G.g = e->geo;
+    G.g.pr = pr ? 1 : 0;
+    G.g.ncx = pr ? (G.g.kcx < G.g.nkx ? G.g.kcx : G.g.nkx) : G.g.nkx;
+    G.in = mode == kRK0 ? states[k] : e->tmp1;
+    G.W = e->W;
+    G.F = e->F;
+    G.twx = e->twx;
+    G.twy = e->twy;
+    G.a.S = states[k];
+    G.a.Sout = states[k];
+    G.a.tmp = e->tmp;
+    G.a.tmp1 = e->tmp1;
+    G.a.nan_flag = e->dflag;
+    G.pr = fast::PerRun{e->nu2, e->nu8, e->dt};
+    G.logy = ilog2(e->ny);
+    G.logm = ilog2(e->nx / 2);
+    G.ctaA = ceil_div(G.g.ncx, x->thA * 8 / e->ny);
+    G.ctaB = ceil_div(e->ny, 2 * x->thB / (e->nx / 2));
+    G.ctaC = ceil_div(G.g.ncx, x->thC * 8 / e->ny);
+    G.startA = a0;
+    G.startB = b0;
+    G.startC = c0;
+    a0 += G.ctaA * e->nruns;
+    b0 += G.ctaB * e->nruns;
+    c0 += G.ctaC * e->nruns;
+  }
+  int rc = GBS_OK;
+  GBS_MIX_TH(x->thA, rc = fast::mixA<THV>(m, a0, st));
+  if (rc) return rc;
+  GBS_MIX_TH(x->thB, rc = fast::mixB<THV>(m, b0, st));
+  if (rc) return rc;
+  GBS_MIX_TH(x->thC, rc = fast::mixC<THV>(m, c0, st));
+  return rc;
+}
+
 }  // namespace gbs
 
+struct gbs_ens2d_mixed {
+  gbs::EnsembleMix x;
+};
+
 extern "C" {
+
+int gbs_ens2d_mixed_create(gbs_ens2d* const* groups, int ngroups, gbs_ens2d_mixed** out) {
+  gbs::clear_error();
+  if (!out || !groups || ngroups < 1 || ngroups > gbs::fast::kMixMax) {
+    gbs::set_error("gbs_ens2d_mixed_create: 1..%d groups", gbs::fast::kMixMax);
+    return GBS_EINVAL;
+  }
+  *out = nullptr;
+  gbs_ens2d_mixed* h = new (std::nothrow) gbs_ens2d_mixed();
+  if (!h) return GBS_ENOMEM;
+  h->x.n = ngroups;
+  for (int k = 0; k < ngroups; ++k) {
+    if (!groups[k]) {
+      delete h;
+      gbs::set_error("gbs_ens2d_mixed_create: null group");
+      return GBS_EINVAL;
+    }
+    h->x.e[k] = &groups[k]->e;
+  }
+  h->x.thA = h->x.thB = h->x.thC = 512;
+  if (!gbs::mix_fits(&h->x, 512, 512, 512)) {
+    delete h;
+    gbs::set_error("gbs_ens2d_mixed_create: a group size has no single-launch tile");
+    return GBS_EINVAL;
+  }
+  *out = h;
+  return GBS_OK;
+}
+
+int gbs_ens2d_mixed_set_tuning(gbs_ens2d_mixed* h, int th_inverse, int th_x, int th_forward) {
+  gbs::clear_error();
+  auto ok = [](int t) { return t == 128 || t == 256 || t == 512; };
+  if (!h || !ok(th_inverse) || !ok(th_x) || !ok(th_forward) ||
+      !gbs::mix_fits(&h->x, th_inverse, th_x, th_forward)) {
+    gbs::set_error("gbs_ens2d_mixed_set_tuning: threads in {128, 256, 512} giving every "
+                   "group 4..64 columns and >= 1 row per CTA");
+    return GBS_EINVAL;
+  }
+  h->x.thA = th_inverse;
+  h->x.thB = th_x;
+  h->x.thC = th_forward;
+  return GBS_OK;
+}
+
+int gbs_ens2d_mixed_destroy(gbs_ens2d_mixed* h) {
+  delete h;
+  return GBS_OK;
+}
+
+// nsteps RK4 steps of every run of every group; states[k]: the state of group
+// k.  Three launches per RK4 stage for all the groups together.
+int gbs_ens2d_mixed_step(gbs_ens2d_mixed* h, void* const* states, int nsteps, int flags,
+                         void* stream) {
+  gbs::clear_error();
+  if (!h || !states || nsteps < 1) {
+    gbs::set_error("gbs_ens2d_mixed_step: invalid argument");
+    return GBS_EINVAL;
+  }
+  for (int k = 0; k < h->x.n; ++k) {
+    if (!states[k]) {
+      gbs::set_error("gbs_ens2d_mixed_step: null state");
+      return GBS_EINVAL;
+    }
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool pr = (flags & GBS_STEP_DEALIASED) != 0;
+  for (int it = 0; it < nsteps; ++it) {
+    const bool p = pr || it > 0;
+    for (int m = gbs::kRK0; m <= gbs::kRK3; ++m) {
+      const int rc = gbs::mix_eval(&h->x, states, m, p, st);
+      if (rc) return rc;
+    }
+  }
+  return GBS_OK;
+}
+
 
 int gbs_ens2d_create(int64_t nx, int64_t ny, double Lx, double Ly, int64_t nruns,
                      int64_t kcut_x, int64_t kcut_y, double beta, gbs_ens2d** out) {

@@ -698,20 +698,24 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
 }
 
 // ----------------------------------------------------- ns2d kernels
-// A: inverse y pass; fields ux, uy, d_x rot, d_y rot.
+// The ns2d passes are device functions of a block index `bid` (the CTA's
+// own blockIdx, or the one a multi-size ensemble launch assigns it).
+
+// A: inverse y pass; fields ux, uy, d_x rot, d_y rot.  bid = (column tile,
+// -, run).
 template <typename T, int LOGN, int TX, bool PH>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
-kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
-          const cplx<T>* __restrict__ twy) {
+__device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
+                                               cplx<T>* __restrict__ W, const Geo& g,
+                                               const cplx<T>* __restrict__ twy, uint3 bid) {
   using C = cplx<T>;
   using P = Line<LOGN>;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
-  const int ix = blockIdx.x * TX + c;
+  const int ix = bid.x * TX + c;
   const bool valid = ix < g.ncx;
   const int64_t nK = (int64_t)g.ny * g.nkx;
-  S += blockIdx.z * nK;  // run of a batched ensemble
-  W += blockIdx.z * 4 * nK;
+  S += bid.z * nK;  // run of a batched ensemble
+  W += bid.z * 4 * nK;
   const T kx = T(g.dkx * ix);
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
 #pragma unroll 1
@@ -747,11 +751,20 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   }
 }
 
-// B: x pass, compute_Frot = -ux d_x rot - uy (d_y rot + beta).
+template <typename T, int LOGN, int TX, bool PH>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
+          const cplx<T>* __restrict__ twy) {
+  kf2_inv_y_body<T, LOGN, TX, PH>(S, W, g, twy, blockIdx);
+}
+
+// B: x pass, compute_Frot = -ux d_x rot - uy (d_y rot + beta).  bid = (row
+// tile, run, -).
 template <typename T, int LOGM, int L>
-__global__ void __launch_bounds__(4 * L * (1 << LOGM) / 8, 2)
-kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
-      const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+__device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
+                                           cplx<T>* __restrict__ F, const Geo& g,
+                                           const cplx<T>* __restrict__ twx,
+                                           unsigned long long* vmax, uint3 bid) {
   using C = cplx<T>;
   using P = Line<LOGM>;
   constexpr int M = P::N, M8 = P::N8, LS = M;
@@ -761,10 +774,10 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int f = threadIdx.x / (M8 * L);
   const int64_t nrows = g.ny;
   const int64_t nK = nrows * g.nkx;
-  const int64_t row = (int64_t)blockIdx.x * L + l;
+  const int64_t row = (int64_t)bid.x * L + l;
   const bool valid = row < nrows;
-  W += blockIdx.y * 4 * nK;  // run of a batched ensemble
-  F += blockIdx.y * nK;
+  W += bid.y * 4 * nK;  // run of a batched ensemble
+  F += bid.y * nK;
   C* slot = buf + (f * L + l) * LS;
   auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
@@ -803,7 +816,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
     else
       res = mk<C>(-ux.x * px.x - uy.x * (py.x + beta), -ux.y * px.y - uy.y * (py.y + beta));
     p0[0] = res;
-    if (vmax && (int64_t)blockIdx.x * L + ll < nrows) {
+    if (vmax && (int64_t)bid.x * L + ll < nrows) {
       mx = fmax(mx, fmax(fabs(ux.x), fabs(ux.y)));
       my = fmax(my, fmax(fabs(uy.x), fabs(uy.y)));
     }
@@ -822,7 +835,7 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
   for (int idx = threadIdx.x; idx < L * nout; idx += blockDim.x) {
     const int k = idx % nout, ll = idx / nout;
-    const int64_t rr = (int64_t)blockIdx.x * L + ll;
+    const int64_t rr = (int64_t)bid.x * L + ll;
     if (rr >= nrows) continue;
     const C* sl = buf + ll * LS;
     C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
@@ -834,19 +847,27 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
 }
 
+template <typename T, int LOGM, int L>
+__global__ void __launch_bounds__(4 * L * (1 << LOGM) / 8, 2)
+kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
+      const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  kf2_x_body<T, LOGM, L>(W, F, g, twx, vmax, blockIdx);
+}
+
 // C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
+// bid = (column tile, -, run).
 template <typename T, int LOGN, int TX, bool EXT>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
-kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
-          int mode, RKArgs a, PerRun pr) {
+__device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Geo g,
+                                               const cplx<T>* __restrict__ twy, int mode,
+                                               RKArgs a, const PerRun& pr, uint3 bid) {
   using C = cplx<T>;
   using P = Line<LOGN>;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
-  const int ix = blockIdx.x * TX + c;
+  const int ix = bid.x * TX + c;
   const bool valid = ix < g.ncx;
   {  // run of a batched ensemble: its fields and parameters
-    const int64_t off = blockIdx.z * (int64_t)g.ny * g.nkx;
+    const int64_t off = bid.z * (int64_t)g.ny * g.nkx;
     F += off;
     if (a.S) a.S = static_cast<const C*>(a.S) + off;
     if (a.Sout) a.Sout = static_cast<C*>(a.Sout) + off;
@@ -855,9 +876,9 @@ kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
     if (a.tend) a.tend = static_cast<C*>(a.tend) + off;
     if (a.add) a.add = static_cast<const C*>(a.add) + off;
     if (pr.dt) {
-      a.dt = pr.dt[blockIdx.z];
-      g.nu2 = pr.nu2[blockIdx.z];
-      g.nu8 = pr.nu8[blockIdx.z];
+      a.dt = pr.dt[bid.z];
+      g.nu2 = pr.nu2[bid.z];
+      g.nu8 = pr.nu8[bid.z];
     }
   }
   C v[8];
@@ -880,6 +901,13 @@ kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
     stage_epilogue1<C, T, EXT>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
                           kx, ky, ix == 0 && kyi == 0, rm, q);
   }
+}
+
+template <typename T, int LOGN, int TX, bool EXT>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+kf2_fwd_y(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twy,
+          int mode, RKArgs a, PerRun pr) {
+  kf2_fwd_y_body<T, LOGN, TX, EXT>(F, g, twy, mode, a, pr, blockIdx);
 }
 
 }  // namespace fast

@@ -32,9 +32,12 @@ template <typename T, int LOGN> constexpr int tx_fwdz() {
   return tx_cap(sizeof(T) == 4 ? GBS_TX_FWDZ : 4, LOGN);
 }
 // rows per CTA for the x passes
+#ifndef GBS_X_THREADS
+#define GBS_X_THREADS 384
+#endif
 template <typename T, int LOGM, int NF> constexpr int rows_x() {
   constexpr int M8 = (1 << LOGM) / 8;
-  constexpr int budget = (sizeof(T) == 4 ? 384 : 192) / NF;
+  constexpr int budget = (sizeof(T) == 4 ? GBS_X_THREADS : 192) / NF;
   return budget / M8 > 0 ? budget / M8 : 1;
 }
 

@@ -1,11 +1,14 @@
 """Batched ensembles of independent ns2d runs of uneven grid sizes.
 
 Runs of one size are advanced together by ``gbs_ens2d_step`` (one launch
-per pass for the whole group, per-run nu_2, nu_8 and dt).  ``capture``
-records ``steps_per_graph`` RK4 steps of every group, each group on its own
-stream, into one CUDA graph; ``run`` replays it.  ``autotune`` times the
-compiled tile shapes of each group (column width of the y passes, rows per
-CTA of the x pass) and keeps the fastest.
+per pass for the whole group, per-run nu_2, nu_8 and dt).  The groups of
+different sizes either run on their own streams, or all together through
+``gbs_ens2d_mixed_step``: one launch per pass covers every run of every
+size.  ``capture`` records ``steps_per_graph`` RK4 steps of every group
+into one CUDA graph; ``run`` replays it.  ``autotune`` times the compiled
+tile shapes of each group (column width of the y passes, rows per CTA of
+the x pass), keeps the fastest, then times the single-launch mode against
+the per-group streams and keeps the faster.
 
 ``python -m fluidsim_gb300.ensemble`` runs the 96-run configuration (32 each
 at 128^2, 256^2, 512^2, float32, 500 steps) and prints one JSON line with
@@ -77,8 +80,20 @@ class EnsembleNS2D:
                                 "stream": torch.cuda.Stream()})
         self.graph = None
         self.steps_per_graph = 0
+        # single-launch mode: the groups, largest first (their CTAs start first)
+        order = sorted(range(len(self.groups)), key=lambda k: -self.groups[k]["n"])
+        self._mix_order = order
+        hs = (ctypes.c_void_p * len(order))(*[self.groups[k]["h"].value for k in order])
+        self._mix = ctypes.c_void_p()
+        _lib.check(self.lib.gbs_ens2d_mixed_create(hs, len(order), ctypes.byref(self._mix)),
+                   "gbs_ens2d_mixed_create")
+        self._mix_states = (ctypes.c_void_p * len(order))(
+            *[self.groups[k]["S"].data_ptr() for k in order])
+        self.mixed = False
 
     def __del__(self):
+        if getattr(self, "_mix", None):
+            self.lib.gbs_ens2d_mixed_destroy(self._mix)
         for g in getattr(self, "groups", []):
             self.lib.gbs_ens2d_destroy(g["h"])
 
@@ -93,6 +108,12 @@ class EnsembleNS2D:
 
     def step(self, nsteps=1):
         cur = torch.cuda.current_stream()
+        if self.mixed:
+            _lib.check(self.lib.gbs_ens2d_mixed_step(self._mix, self._mix_states, nsteps,
+                                                     _lib.GBS_STEP_DEALIASED,
+                                                     ctypes.c_void_p(cur.cuda_stream)),
+                       "ens2d_mixed_step")
+            return
         for g in self.groups:
             g["stream"].wait_stream(cur)
             self._step_group(g, nsteps, g["stream"])
@@ -120,6 +141,33 @@ class EnsembleNS2D:
             _lib.check(self.lib.gbs_ens2d_set_tuning(g["h"], *best[1]))
             table[g["n"]] = {"ms_per_step": best[0], "tx_inverse": best[1][0],
                              "rows_x": best[1][1], "tx_forward": best[1][2]}
+        # all groups per step: their own streams, or one launch per pass with
+        # the fastest threads per CTA of each pass
+        def time_all(steps):
+            self.step(1)  # warm
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self.step(steps)
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / steps
+
+        self.mixed = False
+        mode_ms = {"per_group_streams": time_all(steps)}
+        self.mixed = True
+        best_mix = None
+        for th in itertools.product((128, 256, 512), repeat=3):
+            if self.lib.gbs_ens2d_mixed_set_tuning(self._mix, *th) != _lib.GBS_OK:
+                continue  # some group has no tile at these thread counts
+            ms = time_all(steps)
+            if best_mix is None or ms < best_mix[0]:
+                best_mix = (ms, th)
+        _lib.check(self.lib.gbs_ens2d_mixed_set_tuning(self._mix, *best_mix[1]))
+        mode_ms["single_launch"] = best_mix[0]
+        self.mixed = mode_ms["single_launch"] < mode_ms["per_group_streams"]
+        table["all_groups_ms_per_step"] = mode_ms
+        table["single_launch_threads"] = dict(zip(("inverse", "x", "forward"), best_mix[1]))
+        table["mode"] = "single_launch" if self.mixed else "per_group_streams"
         self.reset()
         return table
 

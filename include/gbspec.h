@@ -208,6 +208,20 @@ int gbs_ens2d_step(gbs_ens2d* ens, void* state_spect, int nsteps, int flags,
                    void* stream);
 int gbs_ens2d_nan_flag(gbs_ens2d* ens, int* flag);
 
+/* Groups of different sizes stepped together: one launch per pass of an RK4
+ * stage covers every run of every group (up to 4 groups; they are not
+ * owned and must outlive the object).  states[k] is group k's state.
+ * Enqueue only, as gbs_ens2d_step. */
+typedef struct gbs_ens2d_mixed gbs_ens2d_mixed;
+int gbs_ens2d_mixed_create(gbs_ens2d* const* groups, int ngroups, gbs_ens2d_mixed** mixed);
+int gbs_ens2d_mixed_destroy(gbs_ens2d_mixed* mixed);
+/* threads per CTA of the inverse y, x and forward y launches (128, 256 or
+ * 512; default 512), within what every group's size allows */
+int gbs_ens2d_mixed_set_tuning(gbs_ens2d_mixed* mixed, int th_inverse, int th_x,
+                               int th_forward);
+int gbs_ens2d_mixed_step(gbs_ens2d_mixed* mixed, void* const* states, int nsteps, int flags,
+                         void* stream);
+
 /* Filtered-DNS data for the learned closure (no reference counterpart):
  *   gbs_spectral_resample: nfields spectral fields of shape_in (nz, ny, nx)
  *     onto shape_out, keeping |k_a| < m_a / 2, multiplied by the top-hat
