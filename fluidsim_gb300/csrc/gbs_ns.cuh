@@ -133,6 +133,29 @@ __device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C
   return mk<C>(S.x * E + c1 * Nd.x, S.y * E + c1 * Nd.y);
 }
 
+// RK4 stages 0-2 on values: S = S_0, t = tmp (read at stages 1 and 2);
+// pseudo_spect.py:898-984, same evaluation order as the numpy expressions.
+template <typename C, typename T>
+__device__ __forceinline__ void rk4_stage_values(int mode, T dt, T sigma, C N, C S, C t,
+                                                 C& tmp_out, C& tmp1_out) {
+  if (mode == kRK0) {
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c6 = dt / T(6), c2 = dt / T(2);
+    tmp_out = cscale(mk<C>(S.x + c6 * N.x, S.y + c6 * N.y), E);
+    tmp1_out = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
+  } else if (mode == kRK1) {
+    T E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c2 = dt / T(2);
+    tmp_out = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1_out = mk<C>(S.x * E2 + c2 * N.x, S.y * E2 + c2 * N.y);
+  } else {  // kRK2
+    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
+    T c3 = dt / T(3) * E2, c1 = dt * E2;
+    tmp_out = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
+    tmp1_out = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+  }
+}
+
 // Intermediate stage update at one mode (RK4: pseudo_spect.py:898-984;
 // RK2 first stage: 505-512; RK2_trapezoid first stage: 559-567), same
 // evaluation order as the numpy expressions there.
@@ -143,26 +166,13 @@ __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
   C* tmp = static_cast<C*>(a.tmp);
   C* tmp1 = static_cast<C*>(a.tmp1);
   if (!EXT && mode > kRK2) return;
-  if (mode == kRK0) {
+  if (mode >= kRK0 && mode <= kRK2) {
     const C S = static_cast<const C*>(a.S)[i];
-    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
-    T c6 = dt / T(6), c2 = dt / T(2);
-    tmp[i] = cscale(mk<C>(S.x + c6 * N.x, S.y + c6 * N.y), E);
-    tmp1[i] = cscale(mk<C>(S.x + c2 * N.x, S.y + c2 * N.y), E2);
-  } else if (mode == kRK1) {
-    const C S = static_cast<const C*>(a.S)[i];
-    T E2 = dexp(-dt / T(2) * sigma);
-    T c3 = dt / T(3) * E2, c2 = dt / T(2);
-    C t = tmp[i];
-    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
-    tmp1[i] = mk<C>(S.x * E2 + c2 * N.x, S.y * E2 + c2 * N.y);
-  } else if (mode == kRK2) {
-    const C S = static_cast<const C*>(a.S)[i];
-    T E = dexp(-dt * sigma), E2 = dexp(-dt / T(2) * sigma);
-    T c3 = dt / T(3) * E2, c1 = dt * E2;
-    C t = tmp[i];
-    tmp[i] = mk<C>(t.x + c3 * N.x, t.y + c3 * N.y);
-    tmp1[i] = mk<C>(S.x * E + c1 * N.x, S.y * E + c1 * N.y);
+    const C t = mode == kRK0 ? mk<C>(0, 0) : tmp[i];
+    C o, o1;
+    rk4_stage_values<C, T>(mode, dt, sigma, N, S, t, o, o1);
+    tmp[i] = o;
+    tmp1[i] = o1;
   } else if (!EXT) {
     return;
   } else if (mode == kR2a) {
@@ -272,6 +282,46 @@ __device__ __forceinline__ void project_state(const Phys& q, C (&v)[NV], T kx, T
 // EXT: compiled with the modes of the other schemes, the phase-shift branch
 // and the other projections (the fast kernels instantiate a variant for RK4
 // with the default projector).
+// The lean epilogue (RK4 stages, plain tendency, default projector) of one
+// position whose S_0 and tmp values the caller loaded (S0, T0; as many as
+// the stage reads): a pass can then load several positions' values before
+// storing any.  Same operations as stage_epilogue3<..., false>.
+template <typename C, typename T, int NV>
+__device__ __forceinline__ void stage_epilogue_rk4(int mode, const RKArgs& a, int64_t i,
+                                                   int64_t nK, C (&N)[NV], const C (&S0)[NV],
+                                                   const C (&T0)[NV], T kx, T ky, T kz, T k2,
+                                                   bool k0, bool rm, const Phys& q) {
+  project3(N, kx, ky, kz, k2, k0);
+  if (rm) N[0] = N[1] = N[2] = N[NV - 1] = mk<C>(0, 0);
+  if (mode == kTend) {
+    C* o = static_cast<C*>(a.tend);
+#pragma unroll
+    for (int f = 0; f < NV; ++f) o[i + f * nK] = N[f];
+  } else if (mode == kRK3) {
+    const T c6 = T(a.dt) / T(6);
+    C Sn[NV];
+#pragma unroll
+    for (int f = 0; f < NV; ++f) Sn[f] = mk<C>(T0[f].x + c6 * N[f].x, T0[f].y + c6 * N[f].y);
+    project3(Sn, kx, ky, kz, k2, k0);
+    if (rm) Sn[0] = Sn[1] = Sn[2] = Sn[NV - 1] = mk<C>(0, 0);
+    C* So = static_cast<C*>(a.Sout);
+#pragma unroll
+    for (int f = 0; f < NV; ++f) So[i + f * nK] = Sn[f];
+    if (isnan(Sn[0].x) || isnan(Sn[0].y)) atomicOr(a.nan_flag, 1);
+  } else {
+    const T sig = freq_lin<T>(q, k2, k0);
+    C* tmp = static_cast<C*>(a.tmp);
+    C* tmp1 = static_cast<C*>(a.tmp1);
+#pragma unroll
+    for (int f = 0; f < NV; ++f) {
+      C o, o1;
+      rk4_stage_values<C, T>(mode, T(a.dt), sig, N[f], S0[f], T0[f], o, o1);
+      tmp[i + f * nK] = o;
+      tmp1[i + f * nK] = o1;
+    }
+  }
+}
+
 template <typename C, typename T, int NV, bool EXT = true>
 __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64_t i,
                                                 int64_t nK, C (&N)[NV], T kx, T ky,
