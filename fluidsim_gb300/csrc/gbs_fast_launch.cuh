@@ -99,7 +99,9 @@ static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, i
   if (rc) return rc;
   static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR>, TH, smem);
   ColArgs ap = a;
-  ap.pf = pf;
+  // only for row-strided columns (y passes): with plane strides (z passes)
+  // the next wave's tiles span every plane
+  ap.pf = a.es * (int64_t)sizeof(C) <= 65536 ? pf : 0;
   dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
   kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
                                                  static_cast<C*>(out), ap,
