@@ -34,10 +34,11 @@ EXPORTED = (
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
     "gbs_ens2d_mixed_create", "gbs_ens2d_mixed_destroy", "gbs_ens2d_mixed_step",
     "gbs_ens2d_mixed_set_tuning",
-    "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection",
+    "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection", "gbs_ns_set_phase_shifts",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
-           "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
+           "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
+           "RK2_phaseshift_random": 8}
 
 
 class NSParams(ctypes.Structure):
@@ -87,6 +88,7 @@ def _declare(lib):
         "gbs_ns_step_rk4": (ctypes.c_int, [P, P, DP, DP, ctypes.c_int, P]),
         "gbs_ns_step": (ctypes.c_int, [P, ctypes.c_int, P, DP, DP, ctypes.c_int, P]),
         "gbs_ns_set_projection": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "gbs_ns_set_phase_shifts": (ctypes.c_int, [P, DP, DP]),
         "gbs_ns_max_velocity": (ctypes.c_int, [P, P, DP, P]),
         "gbs_cfl_update": (ctypes.c_double, [ctypes.c_double] * 4),
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),

@@ -359,7 +359,7 @@ struct Geo {
   double nu2, nu4, nu8, num4, beta, f, inv_n, k2_hypo0;
   int has_f;
   int phase;             // multiply the input state by exp(i phi)
-  double dx, dy, dz;     // grid spacings (phase factor)
+  double sx, sy, sz;     // phase shift lengths (phi = sx kx + sy ky + sz kz)
   int proj, no_vz_kz0;   // ns3d projection of the tendencies and the state
   double N2;             // ns3d.strat: Brunt-Vaisala frequency squared
   int strat;             // ns3d.strat: 4 state fields (vx, vy, vz, b)
@@ -448,7 +448,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
         x = mk<C>(-kz * x.y, kz * x.x);
       }
       if (PH)
-        x = cmul(x, phase_factor<C, T>(T(g.dx), T(g.dy), T(g.dz), kx, ky,
+        x = cmul(x, phase_factor<C, T>(T(g.sx), T(g.sy), T(g.sz), kx, ky,
                                        T(g.dkz * kadim(p, P::N))));
       v[r] = x;
     }
@@ -781,7 +781,7 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
         C w = S[(int64_t)p * g.nkx + ix];
         const int kyi = kadim(p, P::N);
         const T ky = T(g.dky * kyi);
-        if (PH) w = cmul(w, phase_factor<C, T>(T(g.dx), T(g.dy), T(0), kx, ky, T(0)));
+        if (PH) w = cmul(w, phase_factor<C, T>(T(g.sx), T(g.sy), T(0), kx, ky, T(0)));
         T cc;
         if (f == 0 || f == 1) {
           const T k2 = kx * kx + ky * ky;

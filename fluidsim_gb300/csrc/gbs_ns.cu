@@ -44,7 +44,7 @@ struct NSK {
   double k2_hypo0;  // K2 at (iz, iy, ix) = (0, 0, 1): f_d_hypo[0,..,0] source
   int TX, L, LP;
   int phase;          // multiply the input state by exp(i phi)
-  double dx, dy, dz;  // grid spacings (phase factor)
+  double sx, sy, sz;  // phase shift lengths (phi = sx kx + sy ky + sz kz)
   int proj, no_vz_kz0;  // ns3d projection of the tendencies and the state
 };
 
@@ -111,7 +111,7 @@ k3_inv_z_curl(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
       C vx = S[i], vy = S[i + nK], vz = S[i + 2 * nK];
       const T kx = T(q.dkx * ix), kz = T(q.dkz * kadim(iz, q.nz));
       if (q.phase) {
-        const C e = phase_factor<C, T>(T(q.dx), T(q.dy), T(q.dz), kx, ky, kz);
+        const C e = phase_factor<C, T>(T(q.sx), T(q.sy), T(q.sz), kx, ky, kz);
         vx = cmul(vx, e);
         vy = cmul(vy, e);
         vz = cmul(vz, e);
@@ -258,7 +258,7 @@ k2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, NSK q,
     if (ix < q.nkx) {
       C w = S[(int64_t)iy * q.nkx + ix];
       const T kx = T(q.dkx * ix), ky = T(q.dky * kadim(iy, q.ny));
-      if (q.phase) w = cmul(w, phase_factor<C, T>(T(q.dx), T(q.dy), T(0), kx, ky, T(0)));
+      if (q.phase) w = cmul(w, phase_factor<C, T>(T(q.sx), T(q.sy), T(0), kx, ky, T(0)));
       const T k2 = kx * kx + ky * ky;
       const T inv = (ix == 0 && kadim(iy, q.ny) == 0) ? T(0) : T(1) / k2;
       const T cx = ky * inv, cy = -(kx * inv);
@@ -386,6 +386,7 @@ struct Solver {
   double* dred;              // reduction partials
   double* hbuf;              // pinned host mirror (kHostBuf doubles)
   double* hbuf_dev;          // the same memory in the device address space
+  double shift[2][3];        // phase shifts alpha, beta (grid spacings per axis)
   // per-kernel timing (CUDA events on the launching stream) + launch count
   int timing;
   int nev;                  // event pairs in use
@@ -498,13 +499,20 @@ static int setup_shapes(Solver* s) {
 }
 
 // One tendency evaluation from `in`; kernel C runs `mode`.
-static fast::Geo geo_for(const Solver* s, bool pruned, bool phase = false) {
+// phase shift lengths of shift `phase` (1: alpha, 2: beta) in units of the
+// grid spacing times s->shift
+static void shift_lengths(const Solver* s, int phase, double* sx, double* sy, double* sz) {
+  const double* c = s->shift[phase == 2 ? 1 : 0];
+  *sx = c[0] * (s->p.Lx / s->p.nx);
+  *sy = c[1] * (s->p.Ly / s->p.ny);
+  *sz = s->p.ndim == 3 ? c[2] * (s->p.Lz / s->p.nz) : 0.0;
+}
+
+static fast::Geo geo_for(const Solver* s, bool pruned, int phase = 0) {
   fast::Geo g = s->geo;
   g.pr = pruned ? 1 : 0;
   g.phase = phase ? 1 : 0;
-  g.dx = s->p.Lx / s->p.nx;
-  g.dy = s->p.Ly / s->p.ny;
-  g.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
+  shift_lengths(s, phase, &g.sx, &g.sy, &g.sz);
   g.ncx = pruned ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
   const int nkeep = 2 * g.kcy - 1;
   g.nky_keep = (pruned && nkeep < g.ny) ? nkeep : g.ny;
@@ -513,7 +521,7 @@ static fast::Geo geo_for(const Solver* s, bool pruned, bool phase = false) {
 
 // compile-time-size path: same passes as the generic one, optionally pruned
 template <typename T>
-static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, bool phase,
+static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, int phase,
                      cudaStream_t st) {
   const fast::Geo g = geo_for(s, pruned, phase);
   unsigned long long* vmax = want_max ? s->dmax : nullptr;
@@ -570,14 +578,12 @@ static int finish_fast(Solver* s, int mode, const RKArgs& a, bool pruned, cudaSt
 
 template <typename T>
 static int eval(Solver* s, const void* in, int mode, const RKArgs& a,
-                bool want_max, cudaStream_t st, bool pruned = false, bool phase = false) {
+                bool want_max, cudaStream_t st, bool pruned = false, int phase = 0) {
   if (s->use_fast) return eval_fast<T>(s, in, pruned, want_max, phase, st);
   using C = cplx<T>;
   NSK q = s->q;
   q.phase = phase ? 1 : 0;
-  q.dx = s->p.Lx / s->p.nx;
-  q.dy = s->p.Ly / s->p.ny;
-  q.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
+  shift_lengths(s, phase, &q.sx, &q.sy, &q.sz);
   const C* twx = static_cast<const C*>(s->tw[0]);
   const C* twy = static_cast<const C*>(s->tw[1]);
   const C* twz = static_cast<const C*>(s->tw[2]);
@@ -726,7 +732,7 @@ static double cfl_tmp(const Solver* s, const double* m) {
 struct Stage {
   int input;  // 0: S, 1: tmp, 2: tmp1
   int mode;
-  int phase;  // shifted evaluation
+  int phase;  // shifted evaluation: 0 none, 1 shift alpha, 2 shift beta
 };
 static int scheme_stages(int scheme, Stage* st) {
   switch (scheme) {
@@ -752,6 +758,15 @@ static int scheme_stages(int scheme, Stage* st) {
       st[0] = {0, kStoreTmp1, 0}; st[1] = {0, kPSXb, 1};
       st[2] = {1, kStoreTmp2, 0}; st[3] = {1, kPSXd, 1};
       return 4;
+    // pseudo_spect.py:421-467: N_d = (N(alpha S)/alpha + N(beta S)/beta) / 2
+    case GBS_SCHEME_EULER_PHASESHIFT_RANDOM:
+      st[0] = {0, kStoreTmp, 1}; st[1] = {0, kEulerPS, 2};
+      return 2;
+    // pseudo_spect.py:641-710: N_0 = N(alpha S)/alpha, S_1 = (S + dt N_0) E,
+    // N_d = (N_0 + N(beta S_1)/beta) / 2
+    case GBS_SCHEME_RK2_PHASESHIFT_RANDOM:
+      st[0] = {0, kPS2a, 1}; st[1] = {1, kPS2b, 2};
+      return 2;
     default:
       return 0;
   }
@@ -791,24 +806,34 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
   a.tmp1 = s->tmp1;
   a.tmp2 = s->tmp2;
   a.nan_flag = s->dflag;
-  a.dx = s->p.Lx / s->p.nx;
-  a.dy = s->p.Ly / s->p.ny;
-  a.dz = s->p.ndim == 3 ? s->p.Lz / s->p.nz : 0.0;
   int rc;
   if (cfl) GBS_CUDA_TRY(cudaMemsetAsync(s->dmax, 0, 3 * sizeof(unsigned long long), st));
   if (check_nan) GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
+  // the CFL maxima are those of the physical state (base.py:320-339); a
+  // scheme whose first evaluation is shifted (RK2_phaseshift_random) gets
+  // them from an unshifted evaluation of its own
+  const bool cfl_apart = cfl && stages[0].phase != 0;
+  if (cfl_apart) {
+    a.in = S;
+    rc = eval<T>(s, S, kTend, a, true, st, pr, 0);
+    if (rc) return rc;
+    rc = publish(s, s->dmax, 0, 3 * sizeof(double), st);
+    if (rc) return rc;
+    *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
+  }
   for (int k = 0; k < nst; ++k) {
     const void* in = stages[k].input == 0 ? S : (stages[k].input == 1 ? s->tmp : s->tmp1);
     const int m = stages[k].mode;
     a.phase = stages[k].phase;
+    shift_lengths(s, stages[k].phase, &a.sx, &a.sy, &a.sz);
     a.in = in;
     if (s->p.strat && stages[k].phase) {
       set_error("phase-shift schemes are not implemented for ns3d.strat");
       return GBS_EINVAL;
     }
-    rc = eval<T>(s, in, m, a, k == 0 && cfl != nullptr, st, pr, stages[k].phase != 0);
+    rc = eval<T>(s, in, m, a, k == 0 && cfl && !cfl_apart, st, pr, stages[k].phase);
     if (rc) return rc;
-    if (k == 0 && cfl) {
+    if (k == 0 && cfl && !cfl_apart) {
       rc = publish(s, s->dmax, 0, 3 * sizeof(double), st);
       if (rc) return rc;
       *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
@@ -1125,6 +1150,8 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   if (!rc) rc = p.dtype == GBS_F64 ? gbs::setup_shapes<double>(s) : gbs::setup_shapes<float>(s);
   if (!rc) {
     s->use_fast = gbs::fast::supported(p.ndim, q.nx, q.ny, q.nz) ? 1 : 0;
+    for (int k = 0; k < 2; ++k)
+      for (int d = 0; d < 3; ++d) s->shift[k][d] = 0.5;
     gbs::fast::Geo& g = s->geo;
     g.nx = q.nx;
     g.ny = q.ny;
@@ -1192,7 +1219,7 @@ int gbs_ns_step(gbs_ns* h, int scheme, void* S, double* dt, const double* cfl, i
                 void* stream) {
   gbs::clear_error();
   if (!h || !S || !dt || !(*dt > 0) || scheme < GBS_SCHEME_RK4 ||
-      scheme > GBS_SCHEME_RK2_PHASESHIFT_EXACT) {
+      scheme > GBS_SCHEME_RK2_PHASESHIFT_RANDOM) {
     gbs::set_error("gbs_ns_step: invalid argument");
     return GBS_EINVAL;
   }
@@ -1347,6 +1374,23 @@ int gbs_ns_set_projection(gbs_ns* h, int projection, int no_vz_kz0) {
   }
   h->s.q.proj = h->s.geo.proj = projection;
   h->s.q.no_vz_kz0 = h->s.geo.no_vz_kz0 = no_vz_kz0 ? 1 : 0;
+  return GBS_OK;
+}
+
+int gbs_ns_set_phase_shifts(gbs_ns* h, const double* alpha, const double* beta) {
+  gbs::clear_error();
+  if (!h || !alpha || !beta) {
+    gbs::set_error("gbs_ns_set_phase_shifts: null argument");
+    return GBS_EINVAL;
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!std::isfinite(alpha[d]) || !std::isfinite(beta[d])) {
+      gbs::set_error("gbs_ns_set_phase_shifts: non-finite shift");
+      return GBS_EINVAL;
+    }
+    h->s.shift[0][d] = alpha[d];
+    h->s.shift[1][d] = beta[d];
+  }
   return GBS_OK;
 }
 

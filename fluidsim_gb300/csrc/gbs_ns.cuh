@@ -32,9 +32,11 @@ __device__ __forceinline__ bool final_stage(int mode) {
          mode == kEulerPS || mode == kPS2b || mode == kPSXd;
 }
 
-// Phase factor exp(i phi), phi = (dx kx + dy ky + dz kz) / 2 of the
-// phase-shift schemes (pseudo_spect.py:282-300), computed in the working
-// precision from the wavenumbers of the mode.
+// Phase factor exp(i phi), phi = sx kx + sy ky + sz kz, of the phase-shift
+// schemes: shift lengths (dx, dy, dz) / 2 for the fixed shift
+// (pseudo_spect.py:282-300), alpha_i d_i or beta_i d_i for the random ones
+// (operators3d.py:1128-1146, operators2d.py:618-631); computed in the
+// working precision from the wavenumbers of the mode.
 // sin and cos of pi x: the argument reduction of sincospi is exact and
 // short (no large-argument path, which would cost local memory in every
 // kernel that carries the phase-shift branch)
@@ -42,8 +44,8 @@ __device__ __forceinline__ void tsincospi(float x, float* s, float* c) { sincosp
 __device__ __forceinline__ void tsincospi(double x, double* s, double* c) { sincospi(x, s, c); }
 
 template <typename C, typename T>
-__device__ __forceinline__ C phase_factor(T dx, T dy, T dz, T kx, T ky, T kz) {
-  const T phi = T(0.5) * (dx * kx + dy * ky + dz * kz);
+__device__ __forceinline__ C phase_factor(T sx, T sy, T sz, T kx, T ky, T kz) {
+  const T phi = sx * kx + sy * ky + sz * kz;
   T sn, cs;
   tsincospi(phi * T(0.31830988618379067154), &sn, &cs);  // phi / pi
   return mk<C>(cs, sn);
@@ -61,7 +63,7 @@ struct RKArgs {
                     // tendency before projection and dealiasing
   void* tmp2;       // third buffer of RK2_phaseshift_exact
   int phase;        // divide the tendency by exp(i phi) (shifted evaluation)
-  double dx, dy, dz;  // grid spacings (phase factor)
+  double sx, sy, sz;  // phase shift lengths (phi = sx kx + sy ky + sz kz)
   const void* in;   // state the tendency is evaluated on (ns3d.strat: b, vz)
 };
 
@@ -210,7 +212,7 @@ __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
 // conjugate)
 template <typename C, typename T>
 __device__ __forceinline__ C unshift(const RKArgs& a, C N, T kx, T ky, T kz) {
-  const C e = phase_factor<C, T>(T(a.dx), T(a.dy), T(a.dz), kx, ky, kz);
+  const C e = phase_factor<C, T>(T(a.sx), T(a.sy), T(a.sz), kx, ky, kz);
   return cmulc(N, e);
 }
 
@@ -361,7 +363,7 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
   project_state<C, T, NV, EXT>(q, N, kx, ky, kz, k2, k0);
   if (rm) N[0] = N[1] = N[2] = N[NV - 1] = mk<C>(0, 0);
   if (EXT && a.phase) {
-    const C e = phase_factor<C, T>(T(a.dx), T(a.dy), T(a.dz), kx, ky, kz);
+    const C e = phase_factor<C, T>(T(a.sx), T(a.sy), T(a.sz), kx, ky, kz);
 #pragma unroll
     for (int f = 0; f < NV; ++f) N[f] = cmulc(N[f], e);
   }

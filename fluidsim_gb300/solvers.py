@@ -21,6 +21,7 @@ precision is chosen with ``params.precision`` ("float64" or "float32").
 """
 
 import ctypes
+import random
 import signal
 from datetime import datetime, timedelta
 from math import pi
@@ -86,9 +87,61 @@ class StatePseudoSpectral:
         self.is_initialized = True
 
 
+class _PhaseShiftPairs:
+    """The (alpha, beta) shift pairs of the ``*_phaseshift_random`` schemes,
+    drawn exactly as the reference does, with the global ``random`` module
+    (so ``random.seed`` before building the simulation repeats a reference
+    run): ``get_phases_random`` (operators3d.py:1128-1146,
+    operators2d.py:618-631) and the pair rotation of
+    ``TimeSteppingPseudoSpectral._init_phaseshift_random`` /
+    ``_get_phaseshift_random`` (pseudo_spect.py:302-372).  A pair holds the
+    shifts in grid spacings per axis (x, y[, z])."""
+
+    def __init__(self, ndim, nb_pairs, nb_steps_compute_new_pair):
+        self.ndim = ndim
+        if nb_steps_compute_new_pair is None:
+            nb_steps_compute_new_pair = 2 if nb_pairs == 1 else 4 * nb_pairs
+        self.nb_pairs = nb_pairs
+        self.nb_new = nb_steps_compute_new_pair
+        self._index = 1
+        self._previous_index_pair = 0
+        self._previous_index_flip = 0
+        self._pairs = [self._draw() for _ in range(nb_pairs)]
+
+    def _draw(self):
+        alpha = tuple(random.uniform(-0.5, 0.5) for _ in range(self.ndim))
+        beta = tuple(a + 0.5 if a < 0 else a - 0.5 for a in alpha)
+        return alpha, beta
+
+    def next(self):
+        if self.nb_pairs == 1 and self.nb_new == 1:
+            alpha, beta = self._pairs[0]
+        elif self.nb_pairs == 1 and self.nb_new == 2:
+            pair = self._pairs[0]
+            alpha, beta = pair if self._index == 1 else pair[::-1]
+        else:
+            index_pair = random.randint(0, self.nb_pairs - 1)
+            pair = self._pairs[index_pair]
+            index_flip = random.randint(0, 1)
+            if (index_pair == self._previous_index_pair
+                    and index_flip == self._previous_index_flip):
+                index_flip = 0 if index_flip else 1
+            self._previous_index_pair = index_pair
+            self._previous_index_flip = index_flip
+            alpha, beta = pair if index_flip else pair[::-1]
+        if self._index == self.nb_new:
+            self._index = 1
+            new_pair = self._draw()
+            self._pairs.pop(0)
+            self._pairs.append(new_pair)
+        else:
+            self._index += 1
+        return alpha, beta
+
+
 class TimeSteppingPseudoSpectral:
-    """Pseudo-spectral time stepping (RK4, RK2, RK2_trapezoid, Euler) with the
-    reference loop semantics."""
+    """Pseudo-spectral time stepping (RK4, RK2, RK2_trapezoid, Euler and the
+    phase-shift schemes) with the reference loop semantics."""
 
     @staticmethod
     def _complete_params_with_default(params):
@@ -97,6 +150,8 @@ class TimeSteppingPseudoSpectral:
             "USE_T_END": True, "t_end": 10.0, "it_end": 10, "USE_CFL": True,
             "type_time_scheme": "RK4", "deltat0": 0.2, "deltat_max": 0.2,
             "cfl_coef": None, "max_elapsed": None})
+        params.time_stepping._set_child(
+            "phaseshift_random", attribs={"nb_pairs": 1, "nb_steps_compute_new_pair": None})
 
     def __init__(self, sim):
         self.sim = sim
@@ -111,6 +166,11 @@ class TimeSteppingPseudoSpectral:
                 f"type_time_scheme {pts.type_time_scheme!r}: GB300 runs "
                 + ", ".join(_lib.SCHEMES))
         self._scheme = _lib.SCHEMES[pts.type_time_scheme]
+        self._phase_pairs = None
+        if pts.type_time_scheme.endswith("_random"):
+            pr = pts.phaseshift_random
+            self._phase_pairs = _PhaseShiftPairs(len(sim.oper.shapeX), pr.nb_pairs,
+                                                 pr.nb_steps_compute_new_pair)
         if pts.USE_CFL:
             # base.py:249-260: default coefficient 0.4 for RK2*/Euler*, 1 for RK4
             if pts.cfl_coef is not None:
@@ -195,6 +255,12 @@ class TimeSteppingPseudoSpectral:
                 current_stream_handle()), "gbs_ns_is_dealiased")
             if ok.value:
                 flags |= _lib.GBS_STEP_DEALIASED
+        if self._phase_pairs is not None:
+            alpha, beta = self._phase_pairs.next()
+            pad = (0.0,) * (3 - len(alpha))
+            _lib.check(self.sim._lib.gbs_ns_set_phase_shifts(
+                self.sim._solver, (ctypes.c_double * 3)(*alpha, *pad),
+                (ctypes.c_double * 3)(*beta, *pad)), "gbs_ns_set_phase_shifts")
         rc = self.sim._lib.gbs_ns_step(
             self.sim._solver, self._scheme, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt),
             cfl, flags, current_stream_handle())

@@ -144,13 +144,28 @@ int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
 #define GBS_SCHEME_RK2_PHASESHIFT_EXACT 6  /* _time_step_RK2_phaseshift_exact,
                                               712-796 (allocates one more state
                                               buffer at its first step)          */
+#define GBS_SCHEME_EULER_PHASESHIFT_RANDOM 7  /* _time_step_Euler_phaseshift_random,
+                                                 421-467                          */
+#define GBS_SCHEME_RK2_PHASESHIFT_RANDOM 8    /* _time_step_RK2_phaseshift_random,
+                                                 641-710                          */
 
 /* One step of `scheme`, otherwise as gbs_ns_step_rk4 (same flags, CFL rule,
- * projection, dealiasing and NaN check).  The phase-shift schemes use the
- * phase exp(i (dx kx + dy ky + dz kz) / 2) (pseudo_spect.py:282-300) and are
- * rejected with GBS_EINVAL when a turbulence model is set. */
+ * projection, dealiasing and NaN check).  The phase-shift schemes evaluate
+ * tendencies on exp(i phi) S with phi = a_x dx kx + a_y dy ky + a_z dz kz:
+ * a = (1/2, 1/2, 1/2) for the fixed-shift schemes (pseudo_spect.py:282-300);
+ * the random ones use the pair (alpha, beta) last given to
+ * gbs_ns_set_phase_shifts, alpha for their first evaluation and beta for
+ * their second.  They are rejected with GBS_EINVAL when a turbulence model
+ * is set. */
 int gbs_ns_step(gbs_ns* solver, int scheme, void* state_spect, double* dt,
                 const double* cfl, int flags, void* stream);
+
+/* The shift pair of the random phase-shift schemes for the next steps, in
+ * grid spacings per axis (3 doubles each; z ignored in 2D): the caller draws
+ * them as TimeSteppingPseudoSpectral._get_phaseshift_random does
+ * (pseudo_spect.py:302-372) from get_phases_random (operators3d.py:
+ * 1128-1146): alpha_i uniform in (-1/2, 1/2), beta_i = alpha_i +- 1/2. */
+int gbs_ns_set_phase_shifts(gbs_ns* solver, const double* alpha, const double* beta);
 
 /* Turbulence model added to the ns3d tendencies before projection and
  * dealiasing, in every stage (fluidsim/solvers/ns3d/solver.py:246-249,

@@ -30,6 +30,7 @@ below instead of by ``SimulBase.__init__``.
 import ast
 import copy
 import importlib.util
+import random
 import sys
 import types
 from pathlib import Path
@@ -238,6 +239,12 @@ def load_reference(root):
     ops_path = fs / "operators" / "operators3d.py"
     for name in ("project_toroidal", "project_poloidal"):
         m[name] = _reference_method(ops_path, "OperatorsPseudoSpectral3D", name)
+    # the random phase pairs of the *_phaseshift_random schemes (they draw
+    # with the global `random` module, so random.seed makes them repeatable)
+    m["get_phases_random_3d"] = _reference_method(ops_path, "OperatorsPseudoSpectral3D",
+                                                  "get_phases_random")
+    m["get_phases_random_2d"] = _reference_method(
+        fs / "operators" / "operators2d.py", "OperatorsPseudoSpectral2D", "get_phases_random")
 
     # turbulence model: the reference's Smagorinsky + stress tensor, with the
     # SimulExtender plumbing of turb_model/base.py replaced by a stand-in
@@ -269,7 +276,7 @@ def _reference_method(path, class_name, name):
                 if isinstance(item, ast.FunctionDef) and item.name == name:
                     item.decorator_list = []
                     mod = ast.Module(body=[item], type_ignores=[])
-                    ns = {"np": np, "Ac": object, "Af": object}
+                    ns = {"np": np, "Ac": object, "Af": object, "uniform": random.uniform}
                     exec(compile(mod, str(path), "exec"), ns)
                     return ns[name]
     raise LookupError(f"{class_name}.{name} not found in {path}")
@@ -284,6 +291,7 @@ def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
         USE_T_END=False, t_end=10.0, it_end=10, USE_CFL=USE_CFL,
         type_time_scheme=type_time_scheme, deltat0=deltat0, deltat_max=deltat_max,
         cfl_coef=cfl_coef, max_elapsed=None,
+        phaseshift_random=_Container(nb_pairs=1, nb_steps_compute_new_pair=None),
     )
     return p
 
@@ -296,6 +304,9 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
     sim = object.__new__(Simul)
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
                          deltat_max, cfl_coef, {"beta": beta}, type_time_scheme)
+    if type_time_scheme.endswith("_random"):
+        oper = copy.copy(oper)
+        oper.get_phases_random = types.MethodType(mods["get_phases_random_2d"], oper)
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
     mods["ns2d_state"].StateNS2D._complete_info_solver(info.solver)
     sim.info = info
@@ -324,10 +335,11 @@ def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
         extra["N"] = N
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
                          deltat_max, cfl_coef, extra, type_time_scheme)
-    if projection is not None:
+    if projection is not None or type_time_scheme.endswith("_random"):
         oper = copy.copy(oper)
         for name in ("project_toroidal", "project_poloidal"):
             setattr(oper, name, types.MethodType(mods[name], oper))
+        oper.get_phases_random = types.MethodType(mods["get_phases_random_3d"], oper)
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
     State._complete_info_solver(info.solver)
     sim.info = info

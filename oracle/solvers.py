@@ -4,6 +4,8 @@ Test infrastructure only (see ``oracle/__init__.py``).  Every function cites
 the reference lines it follows; all arithmetic is float64 / complex128.
 """
 
+import random
+
 import numpy as np
 
 from .spectral import OperNumpy2D, OperNumpy3D
@@ -44,11 +46,12 @@ class _SolverBase:
     """
 
     SCHEMES = ("RK4", "RK2", "Euler", "RK2_trapezoid", "Euler_phaseshift",
-               "RK2_phaseshift", "RK2_phaseshift_exact")
+               "RK2_phaseshift", "RK2_phaseshift_exact", "Euler_phaseshift_random",
+               "RK2_phaseshift_random")
 
     def __init__(self, oper, nu_2=0.0, nu_4=0.0, nu_8=0.0, nu_m4=0.0,
                  deltat0=0.2, deltat_max=0.2, USE_CFL=False, cfl_coef=None,
-                 type_time_scheme="RK4"):
+                 type_time_scheme="RK4", nb_pairs=1, nb_steps_compute_new_pair=None):
         if type_time_scheme not in self.SCHEMES:
             raise ValueError(f"time scheme {type_time_scheme!r} not in the oracle")
         self.type_time_scheme = type_time_scheme
@@ -69,6 +72,8 @@ class _SolverBase:
         self.it = 0
         self.state_spect = np.zeros((self.nvar,) + oper.shapeK, np.complex128)
         self.state_phys = np.zeros((len(self.keys_phys),) + oper.shapeX)
+        if type_time_scheme.endswith("_random"):
+            self._init_phaseshift_random(nb_pairs, nb_steps_compute_new_pair)
 
     # ExactLinearCoefs.compute / get_updated_coefs_CLF (pseudo_spect.py:125-146)
     def _coefs(self):
@@ -145,6 +150,94 @@ class _SolverBase:
         else:
             phase = 0.5 * (o.deltax * o.KX + o.deltay * o.KY)
         return np.exp(1j * phase)
+
+    def get_phases_random(self):
+        """``operators3d.py:1128-1146`` / ``operators2d.py:618-631``: one
+        ``random.uniform(-0.5, 0.5)`` per axis (x, y, z order), beta from
+        alpha by +- 1/2; returns the coefficients (a_x, a_y[, a_z]) of
+        phase = a_x dx Kx + a_y dy Ky (+ a_z dz Kz)."""
+        alpha = tuple(random.uniform(-0.5, 0.5) for _ in self.oper.axes)
+        beta = tuple(a + 0.5 if a < 0 else a - 0.5 for a in alpha)
+        return alpha, beta
+
+    def _phase_from(self, coefs):
+        o = self.oper
+        if len(o.axes) == 3:
+            phase = (coefs[0] * o.deltax * o.Kx + coefs[1] * o.deltay * o.Ky
+                     + coefs[2] * o.deltaz * o.Kz)
+        else:
+            phase = coefs[0] * o.deltax * o.KX + coefs[1] * o.deltay * o.KY
+        return np.exp(1j * phase)
+
+    def _init_phaseshift_random(self, nb_pairs, nb_steps_compute_new_pair):
+        """``pseudo_spect.py:302-327`` (pairs kept as coefficient tuples)."""
+        if nb_steps_compute_new_pair is None:
+            nb_steps_compute_new_pair = 2 if nb_pairs == 1 else 4 * nb_pairs
+        self.nb_pairs = nb_pairs
+        self.nb_steps_compute_new_pair = nb_steps_compute_new_pair
+        self._index_phaseshift = 1
+        self._previous_index_pair = 0
+        self._previous_index_flip = 0
+        self._pairs_phaseshift = [self.get_phases_random() for _ in range(nb_pairs)]
+        self.phase_pairs_used = []
+
+    def _get_phaseshift_random(self):
+        """``pseudo_spect.py:329-372``: the (alpha, beta) coefficients of
+        this step."""
+        nb_pairs, nb_new = self.nb_pairs, self.nb_steps_compute_new_pair
+        if nb_pairs == 1 and nb_new == 1:
+            alpha, beta = self._pairs_phaseshift[0]
+        elif nb_pairs == 1 and nb_new == 2:
+            pair = self._pairs_phaseshift[0]
+            if self._index_phaseshift == 1:
+                alpha, beta = pair
+            else:
+                beta, alpha = pair
+        else:
+            index_pair = random.randint(0, nb_pairs - 1)
+            pair = self._pairs_phaseshift[index_pair]
+            index_flip = random.randint(0, 1)
+            if (index_pair == self._previous_index_pair
+                    and index_flip == self._previous_index_flip):
+                index_flip = 0 if index_flip else 1
+            self._previous_index_pair = index_pair
+            self._previous_index_flip = index_flip
+            if index_flip:
+                alpha, beta = pair
+            else:
+                beta, alpha = pair
+        if self._index_phaseshift == nb_new:
+            self._index_phaseshift = 1
+            new_pair = self.get_phases_random()
+            self._pairs_phaseshift.pop(0)
+            self._pairs_phaseshift.append(new_pair)
+        else:
+            self._index_phaseshift += 1
+        self.phase_pairs_used.append((alpha, beta))
+        return self._phase_from(alpha), self._phase_from(beta)
+
+    def time_step_Euler_phaseshift_random(self):
+        """``pseudo_spect.py:421-467``."""
+        dt = self.deltat
+        diss = self._coefs()[0]
+        S = self.state_spect
+        pa, pb = self._get_phaseshift_random()
+        Na = self.tendencies_nonlin(pa * S) / pa
+        Nb = self.tendencies_nonlin(pb * S) / pb
+        Nd = 0.5 * (Na + Nb)
+        S[:] = (S + dt * Nd) * diss
+
+    def time_step_RK2_phaseshift_random(self):
+        """``pseudo_spect.py:641-710``."""
+        dt = self.deltat
+        diss, diss2 = self._coefs()
+        pa, pb = self._get_phaseshift_random()
+        S = self.state_spect
+        N0 = self.tendencies_nonlin(pa * S) / pa
+        S1 = (S + dt * N0) * diss
+        N1s = self.tendencies_nonlin(pb * S1)
+        Nd = 0.5 * (N0 + N1s / pb)
+        S[:] = S * diss + dt * diss2 * Nd
 
     def time_step_Euler_phaseshift(self):
         """``pseudo_spect.py:374-419``."""

@@ -13,6 +13,7 @@ after 1 and 10 steps.  The oracle restatement is run beside it and must
 agree to 1e-13 before anything is written.
 """
 
+import random
 import sys
 from math import pi
 from pathlib import Path
@@ -52,6 +53,13 @@ CASES_2D = [
     dict(name="ns2d_36x32_eulerps", nx=36, ny=32, Lx=2 * pi, Ly=5.0, nu_2=2e-3,
          USE_CFL=False, deltat0=5e-3, type_time_scheme="Euler_phaseshift",
          init=dict(kmin=2.0, kmax=9.0, seed=12), steps=10),
+    dict(name="ns2d_32_eulerpsr", nx=32, ny=32, Lx=6.0, Ly=6.0, nu_2=1e-3,
+         USE_CFL=False, deltat0=5e-3, type_time_scheme="Euler_phaseshift_random",
+         phase_seed=101, init=dict(kmin=2.0, kmax=10.0, seed=13), steps=10),
+    dict(name="ns2d_40x32_rk2psr", nx=40, ny=32, Lx=2 * pi, Ly=5.0, nu_2=1e-3, beta=0.5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2_phaseshift_random", phase_seed=102,
+         init=dict(kmin=2.0, kmax=9.0, seed=14), steps=10),
 ]
 
 CASES_3D = [
@@ -83,6 +91,13 @@ CASES_3D = [
     dict(name="ns3d_eulerps_32", nx=32, ny=32, nz=32, nu_2=2e-3, USE_CFL=False,
          deltat0=2e-3, type_time_scheme="Euler_phaseshift", init="iso", seed=15,
          steps=10),
+    dict(name="ns3d_rk2psr_24x16x32_f", nx=24, ny=16, nz=32, nu_2=5e-3, f=0.5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         type_time_scheme="RK2_phaseshift_random", phase_seed=103, init="iso", seed=22,
+         steps=10),
+    dict(name="ns3d_eulerpsr_32", nx=32, ny=32, nz=32, nu_2=2e-3, USE_CFL=False,
+         deltat0=2e-3, type_time_scheme="Euler_phaseshift_random", phase_seed=104,
+         init="iso", seed=23, steps=10),
     dict(name="ns3d_toroidal_24x20x16", nx=24, ny=20, nz=16, nu_2=5e-3, f=1.0,
          USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, projection="toroidal",
          init="iso", seed=16, steps=10),
@@ -100,7 +115,30 @@ CASES_3D = [
 PROJECTION_CODES = {None: 0, "toroidal": 1, "vortical": 1, "poloidal": 2}
 
 SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
-                "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6}
+                "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
+                "RK2_phaseshift_random": 8}
+
+
+class _PhaseRNG:
+    """The random phase schemes draw with the global ``random`` module; the
+    reference solver and the oracle each get the sequence of ``random.seed``
+    (``phase_seed``), kept apart while their steps alternate."""
+
+    def __init__(self, seed):
+        self.states = {}
+        self.seed = seed
+
+    def run(self, who, fn):
+        if self.seed is None:
+            return fn()
+        if who in self.states:
+            random.setstate(self.states[who])
+        else:
+            random.seed(self.seed)
+        try:
+            return fn()
+        finally:
+            self.states[who] = random.getstate()
 
 
 def _kw(case, keys):
@@ -113,19 +151,20 @@ def run_2d(mods, case):
                         **case["init"])
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef", "type_time_scheme"])
-    sim = refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0), **kw)
+    rng = _PhaseRNG(case.get("phase_seed"))
+    sim = rng.run("ref", lambda: refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0), **kw))
     sim.state.init_from_rotfft(rot0.copy())
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
     tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
-    orc = NS2DOracle(oper, beta=case.get("beta", 0.0), **kw)
+    orc = rng.run("orc", lambda: NS2DOracle(oper, beta=case.get("beta", 0.0), **kw))
     orc.init_from_rotfft(rot0.copy())
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
                                rtol=0, atol=1e-13 * np.abs(tend0).max())
     out = dict(S_init=S_init, phys_init=phys_init, tend0=tend0, dts=[], E=[])
     for it in range(case["steps"]):
-        sim.time_stepping.one_time_step()
-        orc.one_time_step()
+        rng.run("ref", sim.time_stepping.one_time_step)
+        rng.run("orc", orc.one_time_step)
         out["dts"].append(sim.time_stepping.deltat)
         S = np.array(sim.state.state_spect)
         err = np.abs(orc.state_spect - S).max() / np.abs(S).max()
@@ -136,6 +175,8 @@ def run_2d(mods, case):
             out["S_1"] = S
     out["S_end"] = np.array(sim.state.state_spect)
     out["phys_end"] = np.array(sim.state.state_phys)
+    if case.get("phase_seed") is not None:  # (alpha, beta) of every step
+        out["phase_pairs"] = np.asarray(orc.phase_pairs_used)
     return out
 
 
@@ -151,9 +192,10 @@ def run_3d(mods, case):
                     "deltat_max", "cfl_coef", "type_time_scheme"])
     proj = dict(projection=case.get("projection"), no_vz_kz0=case.get("no_vz_kz0", False))
     strat = case.get("N") is not None
-    sim = refshim.make_ns3d(mods, oper, f=case.get("f"),
-                            smagorinsky_C=case.get("smagorinsky_C"), N=case.get("N"),
-                            **proj, **kw)
+    rng = _PhaseRNG(case.get("phase_seed"))
+    sim = rng.run("ref", lambda: refshim.make_ns3d(
+        mods, oper, f=case.get("f"), smagorinsky_C=case.get("smagorinsky_C"),
+        N=case.get("N"), **proj, **kw))
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
     if strat:  # a buoyancy field as well (set after the velocity round trip)
         b0 = isotropic_3d(nx, ny, nz, *L, seed=case["b_seed"])[0]
@@ -171,7 +213,8 @@ def run_3d(mods, case):
     if strat:
         orc = NS3DStratOracle(oper, N=case["N"], f=case.get("f"), **proj, **kw)
     else:
-        orc = NS3DOracle(oper, f=case.get("f"), turb_model=turb, **proj, **kw)
+        orc = rng.run("orc", lambda: NS3DOracle(oper, f=case.get("f"), turb_model=turb,
+                                                **proj, **kw))
     orc.init_from_vxvyvzfft(*[c.copy() for c in v0])
     if strat:
         orc.state_spect[3] = b0
@@ -181,8 +224,8 @@ def run_3d(mods, case):
                                rtol=0, atol=1e-13 * np.abs(tend0).max())
     out = dict(S_init=S_init, phys_init=phys_init, tend0=tend0, dts=[], E=[])
     for it in range(case["steps"]):
-        sim.time_stepping.one_time_step()
-        orc.one_time_step()
+        rng.run("ref", sim.time_stepping.one_time_step)
+        rng.run("orc", orc.one_time_step)
         out["dts"].append(sim.time_stepping.deltat)
         S = np.array(sim.state.state_spect)
         err = np.abs(orc.state_spect - S).max() / np.abs(S).max()
@@ -193,13 +236,15 @@ def run_3d(mods, case):
             out["S_1"] = S
     out["S_end"] = np.array(sim.state.state_spect)
     out["phys_end"] = np.array(sim.state.state_phys)
+    if case.get("phase_seed") is not None:  # (alpha, beta) of every step
+        out["phase_pairs"] = np.asarray(orc.phase_pairs_used)
     return out
 
 
 def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
             "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
-            "smagorinsky_C", "N"]
+            "smagorinsky_C", "N", "phase_seed"]
     out = {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
                                   dtype=np.float64)
            for k in keys if k in case}

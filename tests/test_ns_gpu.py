@@ -3,6 +3,8 @@
 FP64: relative L2 <= 1e-12 on every state variable after 10 steps (and on
 the first tendency); FP32: relative L2 <= 1e-5 after 10 steps.
 """
+import random
+
 import numpy as np
 import pytest
 
@@ -52,6 +54,8 @@ def make_sim(name, precision="float64"):
     ts.type_time_scheme = scheme(p)
     ts.USE_T_END = False
     ts.it_end = int(p["steps"])
+    if p.get("phase_seed") is not None:  # the random phase schemes draw with `random`
+        random.seed(int(p["phase_seed"]))
     sim = Simul(params)
     sim.state.init_statespect_from(**{k: torch.from_numpy(d["S_init"][i])
                                       for i, k in enumerate(sim.state.keys_state_spect)})
@@ -99,7 +103,8 @@ def test_ten_steps_fp64(cuda, name):
 @pytest.mark.parametrize("name", ["ns2d_256_c1", "ns3d_iso_24x16x32_f", "ns3d_tgv_32",
                                   "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f", "ns2d_32_rk2ps",
                                   "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f",
-                                  "ns3d_strat_64_f_rk2"])
+                                  "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f",
+                                  "ns2d_32_eulerpsr"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()

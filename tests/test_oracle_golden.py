@@ -1,8 +1,12 @@
 """The oracle restatement reproduces the fixtures made by the reference code.
 
 Fixtures (``tests/golden/*.npz``) come from the reference's own time-scheme
-(RK4, RK2, RK2_trapezoid, Euler) / CFL / tendency code (``oracle/refshim.py``, see ``golden/make_golden.py``).
+(RK4, RK2, RK2_trapezoid, Euler, the phase-shift schemes including the random
+ones) / CFL / tendency code (``oracle/refshim.py``, see
+``golden/make_golden.py``).
 """
+import random
+
 import numpy as np
 import pytest
 
@@ -14,6 +18,8 @@ from oracle.turb import smagorinsky_forcing
 
 def make_oracle(name):
     d, p = load(name)
+    if p.get("phase_seed") is not None:  # the random phase schemes draw with `random`
+        random.seed(int(p["phase_seed"]))
     if name.startswith("ns2d"):
         oper = OperNumpy2D(int(p["nx"]), int(p["ny"]), *lengths(p, 2))
         orc = NS2DOracle(oper, beta=p.get("beta") or 0.0, **solver_kwargs(p))
