@@ -11,11 +11,11 @@ from .fft import FFT2DGB300, FFT3DGB300, import_fft_class
 from .params import Parameters
 
 __all__ = ["FFT2DGB300", "FFT3DGB300", "import_fft_class", "Parameters",
-           "SimulNS2D", "SimulNS3D", "SimulNS3DStrat"]
+           "SimulNS2D", "SimulNS2DStrat", "SimulNS3D", "SimulNS3DStrat"]
 
 
 def __getattr__(name):
-    if name in ("SimulNS2D", "SimulNS3D", "SimulNS3DStrat"):
+    if name in ("SimulNS2D", "SimulNS2DStrat", "SimulNS3D", "SimulNS3DStrat"):
         from . import solvers
         return getattr(solvers, name)
     raise AttributeError(name)

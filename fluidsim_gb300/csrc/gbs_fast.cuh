@@ -770,15 +770,17 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
   W += bid.z * 4 * nK;
   const T kx = T(g.dkx * ix);
   auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  // ns2d.strat: two more fields, d_x b and d_y b (b: the second state field)
 #pragma unroll 1
-  for (int f = 0; f < 4; ++f) {
+  for (int f = 0; f < (g.strat ? 6 : 4); ++f) {
+    const C* Sf = f < 4 ? S : S + nK;
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int p = jt + r * P::N8;
       C x = mk<C>(0, 0);
       if (valid && (!g.pr || kept(p, P::N, g.kcy))) {
-        C w = S[(int64_t)p * g.nkx + ix];
+        C w = Sf[(int64_t)p * g.nkx + ix];
         const int kyi = kadim(p, P::N);
         const T ky = T(g.dky * kyi);
         if (PH) w = cmul(w, phase_factor<C, T>(T(g.sx), T(g.sy), T(0), kx, ky, T(0)));
@@ -788,7 +790,7 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
           const T inv = (ix == 0 && kyi == 0) ? T(0) : crcp(k2);
           cc = f == 0 ? ky * inv : -(kx * inv);
         } else {
-          cc = f == 2 ? kx : ky;
+          cc = (f == 2 || f == 4) ? kx : ky;
         }
         x = mk<C>(-cc * w.y, cc * w.x);
       }
@@ -811,12 +813,14 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 }
 
 // B: x pass, compute_Frot = -ux d_x rot - uy (d_y rot + beta).  bid = (row
-// tile, run, -).
-template <typename T, int LOGM, int L>
+// tile, run, -).  ST (ns2d.strat, strat/solver.py:27-32): 6 fields, products
+// f_rot = -ux d_x rot - uy d_y rot and f_b = -ux d_x b - uy d_y b - N^2 uy.
+template <typename T, int LOGM, int L, bool ST = false>
 __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
                                            cplx<T>* __restrict__ F, const Geo& g,
                                            const cplx<T>* __restrict__ twx,
                                            unsigned long long* vmax, uint3 bid) {
+  constexpr int NF = ST ? 6 : 4, NFO = ST ? 2 : 1;
   using C = cplx<T>;
   using P = Line<LOGM>;
   constexpr int M = P::N, M8 = P::N8, LS = M;
@@ -863,11 +867,17 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
     C* p0 = buf + ll * LS + padp<LOGM, C>(j);
     const C ux = p0[0], uy = p0[L * LS], px = p0[2 * L * LS], py = p0[3 * L * LS];
     C res;
-    if (g.beta == 0)
+    if (ST || g.beta == 0)  // (ns2d.strat has no beta term)
       res = mk<C>(-ux.x * px.x - uy.x * py.x, -ux.y * px.y - uy.y * py.y);
     else
       res = mk<C>(-ux.x * px.x - uy.x * (py.x + beta), -ux.y * px.y - uy.y * (py.y + beta));
     p0[0] = res;
+    if (ST) {
+      const C pxb = p0[4 * L * LS], pyb = p0[5 * L * LS];
+      const T n2 = T(g.N2);
+      p0[L * LS] = mk<C>(-ux.x * pxb.x - uy.x * pyb.x - n2 * uy.x,
+                         -ux.y * pxb.y - uy.y * pyb.y - n2 * uy.y);
+    }
     if (vmax && (int64_t)bid.x * L + ll < nrows) {
       mx = fmax(mx, fmax(fabs(ux.x), fabs(ux.y)));
       my = fmax(my, fmax(fabs(uy.x), fabs(uy.y)));
@@ -875,7 +885,7 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   }
   __syncthreads();
   if (vmax) block_max3(mx, my, T(0), vmax);
-  const bool act = f == 0;
+  const bool act = f < NFO;
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
@@ -885,25 +895,25 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   }
   __syncthreads();
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
-  for (int idx = threadIdx.x; idx < L * nout; idx += blockDim.x) {
-    const int k = idx % nout, ll = idx / nout;
+  for (int idx = threadIdx.x; idx < NFO * L * nout; idx += blockDim.x) {
+    const int k = idx % nout, ll = (idx / nout) % L, fo = idx / (nout * L);
     const int64_t rr = (int64_t)bid.x * L + ll;
     if (rr >= nrows) continue;
-    const C* sl = buf + ll * LS;
+    const C* sl = buf + (fo * L + ll) * LS;
     C a = sl[padp<LOGM, C>(k == M ? 0 : k)];
     C b = cconj(sl[padp<LOGM, C>(k == 0 ? 0 : M - k)]);
     const C s = cadd(a, b), d = csub(a, b);
     const C wd = cmul(twx[k], d);
     const T h = T(0.5);
-    F[rr * g.nkx + k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
+    F[fo * nK + rr * g.nkx + k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
   }
 }
 
-template <typename T, int LOGM, int L>
-__global__ void __launch_bounds__(4 * L * (1 << LOGM) / 8, 2)
+template <typename T, int LOGM, int L, bool ST = false>
+__global__ void __launch_bounds__((ST ? 6 : 4) * L * (1 << LOGM) / 8, 2)
 kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
-  kf2_x_body<T, LOGM, L>(W, F, g, twx, vmax, blockIdx);
+  kf2_x_body<T, LOGM, L, ST>(W, F, g, twx, vmax, blockIdx);
 }
 
 // C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
@@ -918,8 +928,12 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
   const int c = threadIdx.x % TX, jt = threadIdx.x / TX;
   const int ix = bid.x * TX + c;
   const bool valid = ix < g.ncx;
-  {  // run of a batched ensemble: its fields and parameters
-    const int64_t off = bid.z * (int64_t)g.ny * g.nkx;
+  // ns2d.strat: bid.y is the field (0: rot, which gets + i kx b of the state
+  // the tendency is evaluated on, strat/solver.py:185; 1: b)
+  const C* bin = (g.strat && bid.y == 0)
+                     ? static_cast<const C*>(a.in) + (int64_t)g.ny * g.nkx : nullptr;
+  {  // run of a batched ensemble (or field of ns2d.strat): its fields and parameters
+    const int64_t off = ((int64_t)bid.z * (g.strat ? 2 : 1) + bid.y) * g.ny * g.nkx;
     F += off;
     if (a.S) a.S = static_cast<const C*>(a.S) + off;
     if (a.Sout) a.Sout = static_cast<C*>(a.Sout) + off;
@@ -950,8 +964,13 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
     const bool rm = ix >= g.kcx || iabs(kyi) >= g.kcy;
     if (g.pr && rm) continue;
     const T ky = T(g.dky * kyi);
-    stage_epilogue1<C, T, EXT>(mode, a, (int64_t)iy * g.nkx + ix, cscale(v[i], inv_n),
-                          kx, ky, ix == 0 && kyi == 0, rm, q);
+    const int64_t idx = (int64_t)iy * g.nkx + ix;
+    C Nv = cscale(v[i], inv_n);
+    if (bin) {
+      const C b = bin[idx];
+      Nv = cadd(Nv, mk<C>(-kx * b.y, kx * b.x));
+    }
+    stage_epilogue1<C, T, EXT>(mode, a, idx, Nv, kx, ky, ix == 0 && kyi == 0, rm, q);
   }
 }
 

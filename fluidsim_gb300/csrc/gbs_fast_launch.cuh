@@ -290,17 +290,18 @@ int A2(const Geo& g, const void* S, void* W, const void* twy, cudaStream_t st) {
   return GBS_OK;
 }
 
-template <typename T, int LOGM>
+template <typename T, int LOGM, bool ST>
 static int B2_launch(const Geo& g, const void* W, void* F, const void* tw,
                      unsigned long long* vmax, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int L = rows_x<T, LOGM, 4>();
+  constexpr int NF = ST ? 6 : 4;
+  constexpr int L = rows_x<T, LOGM, NF>();
   constexpr int M = 1 << LOGM;
-  constexpr int TH = 4 * L * M / 8;
-  const size_t smem = sizeof(C) * (size_t)4 * L * M;
-  int rc = prep(kf2_x<T, LOGM, L>, smem);
+  constexpr int TH = NF * L * M / 8;
+  const size_t smem = sizeof(C) * (size_t)NF * L * M;
+  int rc = prep(kf2_x<T, LOGM, L, ST>, smem);
   if (rc) return rc;
-  kf2_x<T, LOGM, L><<<ceil_div(g.ny, L), TH, smem, st>>>(
+  kf2_x<T, LOGM, L, ST><<<ceil_div(g.ny, L), TH, smem, st>>>(
       static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
   GBS_CHECK_LAUNCH();
   return GBS_OK;
@@ -309,7 +310,11 @@ static int B2_launch(const Geo& g, const void* W, void* F, const void* tw,
 template <typename T>
 int B2(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
        cudaStream_t st) {
-  GBS_LOG_SWITCH(ilog2(g.M), return (B2_launch<T, LG>(g, W, F, twx, vmax, st)));
+  if (g.strat) {
+    GBS_LOG_SWITCH(ilog2(g.M), return (B2_launch<T, LG, true>(g, W, F, twx, vmax, st)));
+  } else {
+    GBS_LOG_SWITCH(ilog2(g.M), return (B2_launch<T, LG, false>(g, W, F, twx, vmax, st)));
+  }
   return GBS_OK;
 }
 
@@ -322,7 +327,7 @@ static int C2_launch(const Geo& g, const void* F, const void* tw, int mode, cons
   const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf2_fwd_y<T, LOGN, TX, PH>, smem);
   if (rc) return rc;
-  kf2_fwd_y<T, LOGN, TX, PH><<<ceil_div(g.ncx, TX), TH, smem, st>>>(
+  kf2_fwd_y<T, LOGN, TX, PH><<<dim3(ceil_div(g.ncx, TX), g.strat ? 2 : 1), TH, smem, st>>>(
       static_cast<const C*>(F), g, static_cast<const C*>(tw), mode, a, PerRun{});
   GBS_CHECK_LAUNCH();
   return GBS_OK;

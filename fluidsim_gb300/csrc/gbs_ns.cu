@@ -828,7 +828,7 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     shift_lengths(s, stages[k].phase, &a.sx, &a.sy, &a.sz);
     a.in = in;
     if (s->p.strat && stages[k].phase) {
-      set_error("phase-shift schemes are not implemented for ns3d.strat");
+      set_error("phase-shift schemes are not implemented for the strat solvers");
       return GBS_EINVAL;
     }
     rc = eval<T>(s, in, m, a, k == 0 && cfl && !cfl_apart, st, pr, stages[k].phase);
@@ -931,6 +931,13 @@ k_means(const cplx<T>* __restrict__ S, NSK q, int ndim, int strat, double inv_N2
       acc[3] += w * fh * 2 * e;
       acc[4] += w * fd * 2 * z;
       acc[5] += w * fh * 2 * z;
+      if (strat) {  // ns2d/strat/output/__init__.py:85-109: EA = (|b| / N)^2 / 2
+        const C bb = S[i + nK];
+        const double ea = 0.5 * inv_N2 * ((double)bb.x * bb.x + (double)bb.y * bb.y);
+        acc[6] += w * ea;
+        acc[7] += w * fd * 2 * ea;
+        acc[8] += w * fh * 2 * ea;
+      }
     }
   }
   __shared__ double red[kNQ][kRedThreads];
@@ -956,7 +963,7 @@ __global__ void k_sum_partials(const double* partial, int nb, double* out) {
 
 template <typename T>
 static int spatial_means(Solver* s, const void* S, double* out, cudaStream_t st) {
-  const double inv_N2 = s->p.strat ? 1.0 / (s->p.N * s->p.N) : 0.0;
+  const double inv_N2 = (s->p.strat && s->p.N != 0) ? 1.0 / (s->p.N * s->p.N) : 0.0;
   k_means<T><<<kRedBlocks, kRedThreads, 0, st>>>(static_cast<const cplx<T>*>(S),
                                                   s->q, s->p.ndim, s->p.strat, inv_N2,
                                                   s->dred);
@@ -1085,13 +1092,13 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   if ((p.ndim != 2 && p.ndim != 3) || (p.dtype != GBS_F32 && p.dtype != GBS_F64) ||
       p.nx < 2 || p.nx % 2 || p.ny < 1 || p.nz < 1 || (p.ndim == 2 && p.nz != 1) ||
       p.nx > 65536 || p.ny > 65535 || p.nz > 65536 || !(p.Lx > 0) || !(p.Ly > 0) ||
-      (p.ndim == 3 && !(p.Lz > 0)) || (p.strat && p.ndim != 3)) {
+      (p.ndim == 3 && !(p.Lz > 0))) {
     gbs::set_error("gbs_ns_create: invalid parameters (nx must be even)");
     return GBS_EINVAL;
   }
   if (p.strat && !gbs::fast::supported(p.ndim, (int)p.nx, (int)p.ny, (int)p.nz)) {
-    gbs::set_error("gbs_ns_create: ns3d.strat runs on power-of-two grids (32..1024 per "
-                   "axis, nx/2 >= 32)");
+    gbs::set_error("gbs_ns_create: ns2d.strat / ns3d.strat run on power-of-two grids "
+                   "(32..1024 per axis, nx/2 >= 32)");
     return GBS_EINVAL;
   }
   gbs_ns* h = new (std::nothrow) gbs_ns();
@@ -1099,7 +1106,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   Solver* s = &h->s;
   memset(s, 0, sizeof(*s));
   s->p = p;
-  s->nvar = p.ndim == 3 ? (p.strat ? 4 : 3) : 1;
+  s->nvar = p.ndim == 3 ? (p.strat ? 4 : 3) : (p.strat ? 2 : 1);
   gbs::NSK& q = s->q;
   q.nx = (int)p.nx;
   q.ny = (int)p.ny;
@@ -1129,8 +1136,8 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
   for (int a = 0; a < 3 && !rc; ++a) rc = gbs::twiddle_alloc(&s->tw[a], ns[a], p.dtype, 0);
   const size_t fb = s->csize * s->nK;
   // inverse-transformed fields (v, omega (+ b)) and products (v x omega (+ v b))
-  const int nW = p.ndim == 3 ? (p.strat ? 7 : 6) : 4;
-  const int nF = p.ndim == 3 ? (p.strat ? 6 : 3) : 1;
+  const int nW = p.ndim == 3 ? (p.strat ? 7 : 6) : (p.strat ? 6 : 4);
+  const int nF = p.ndim == 3 ? (p.strat ? 6 : 3) : (p.strat ? 2 : 1);
   if (!rc) {
     if (cudaMalloc(&s->W, fb * nW) != cudaSuccess ||
         cudaMalloc(&s->F, fb * nF) != cudaSuccess ||

@@ -179,6 +179,8 @@ class TimeSteppingPseudoSpectral:
                 self.CFL = 1.0 if pts.type_time_scheme.startswith("RK4") else 0.4
         self.deltat = pts.deltat0
         self.deltat_max = pts.deltat_max
+        if hasattr(sim, "deltat_cap"):  # ns2d.strat: dispersion-relation time
+            self.deltat_max = min(self.deltat_max, sim.deltat_cap())
         self._nan_check = True
         # state_spect._version right after our last step: while it is
         # unchanged the state is the dealiased output of that step
@@ -443,6 +445,70 @@ class SimulNS2D(_SimulBase):
         r = r.to(self.oper.device, self.oper.cdtype).clone()
         self.oper.dealiasing(r)
         self.state.init_statespect_from(rot_fft=r)
+
+
+class SimulNS2DStrat(SimulNS2D):
+    """``fluidsim.solvers.ns2d.strat.solver.Simul`` on GB300: state
+    (rot_fft, b_fft), tendencies ``-u.grad(rot) + d_x b`` and
+    ``-u.grad(b) - N^2 u_y`` (``ns2d/strat/solver.py:27-32,143-192``); the
+    CFL time is also capped by the dispersion-relation time 2 pi / max(N kx
+    / |k|) (``ns2d/strat/time_stepping.py:31-70,158-198``; the optional
+    group-velocity cap is not implemented).  Power-of-two grids only."""
+
+    keys_state_spect = ("rot_fft", "b_fft")
+    keys_state_phys = ("ux", "uy", "rot", "b")  # ns2d/strat/state.py:31-34
+    _means_keys = ("EK", "Z", "epsK", "epsK_hypo", "epsZ", "epsZ_hypo", "EA", "epsA",
+                   "epsA_hypo")
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        SimulNS2D._complete_params_with_default(params)
+        params._set_attribs({"N": 1.0})  # ns2d/strat/solver.py:95-99
+
+    def __init__(self, params):
+        pts = params.time_stepping
+        if getattr(pts, "cfl_coef_group", None):
+            raise NotImplementedError("the group-velocity time of ns2d.strat")
+        if params.beta:
+            raise ValueError("ns2d.strat has no beta term")
+        super().__init__(params)
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        p.strat = 1
+        p.N = float(self.params.N)
+        return p
+
+    def deltat_cap(self):
+        """``time_stepping.py:55-70`` with ``compute_dispersion_relation``
+        (``solver.py:215-225``): 2 pi / max(N KX / K_not0)."""
+        o = self.oper
+        kx = o.deltakx * np.arange(o.nx // 2 + 1)
+        ky = o.deltaky * np.fft.fftfreq(o.ny, 1.0 / o.ny)
+        KX, KY = np.meshgrid(kx, ky)
+        K2 = KX**2 + KY**2
+        K2[0, 0] = 1e-14
+        freq = (float(self.params.N) * (KX / np.sqrt(K2))).max()
+        return 2.0 * np.pi / freq
+
+    def _statephys_from_statespect(self, S):
+        """``ns2d/strat/state.py:137-151``: (ux, uy, rot, b)."""
+        rot_fft = S[0]
+        ux_fft, uy_fft = self.oper.vecfft_from_rotfft(rot_fft)
+        K = torch.stack([ux_fft, uy_fft, rot_fft, S[1]])
+        X = torch.empty((4,) + self.oper.shapeX, dtype=self.oper.rdtype, device=self.oper.device)
+        self.oper.opfft.ifft_as_arg_destroy(K, X)
+        return X
+
+    def init_from_rotbfft(self, rot_fft, b_fft):
+        """Dealiased rot and b (``ns2d/strat/init_fields.py``)."""
+        fields = []
+        for a in (rot_fft, b_fft):
+            t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.asarray(a))
+            t = t.to(self.oper.device, self.oper.cdtype).clone()
+            self.oper.dealiasing(t)
+            fields.append(t)
+        self.state.init_statespect_from(rot_fft=fields[0], b_fft=fields[1])
 
 
 class SimulNS3D(_SimulBase):

@@ -226,6 +226,13 @@ def load_reference(root):
                               fs / "solvers" / "ns3d" / "state.py")
     m["ns3d_ts"] = _module("fluidsim.solvers.ns3d.time_stepping",
                            fs / "solvers" / "ns3d" / "time_stepping.py")
+    _module("fluidsim.solvers.ns2d.strat", package=True)
+    m["ns2d_strat_solver"] = _module("fluidsim.solvers.ns2d.strat.solver",
+                                     fs / "solvers" / "ns2d" / "strat" / "solver.py")
+    m["ns2d_strat_state"] = _module("fluidsim.solvers.ns2d.strat.state",
+                                    fs / "solvers" / "ns2d" / "strat" / "state.py")
+    m["ns2d_strat_ts"] = _module("fluidsim.solvers.ns2d.strat.time_stepping",
+                                 fs / "solvers" / "ns2d" / "strat" / "time_stepping.py")
     _module("fluidsim.solvers.ns3d.strat", package=True)
     m["ns3d_strat_solver"] = _module("fluidsim.solvers.ns3d.strat.solver",
                                      fs / "solvers" / "ns3d" / "strat" / "solver.py")
@@ -298,25 +305,35 @@ def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
 
 def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, beta=0.0, USE_CFL=False, deltat0=0.2,
-              deltat_max=0.2, cfl_coef=None, type_time_scheme="RK4"):
-    """A reference ns2d ``Simul`` wired around ``oper``."""
-    Simul = mods["ns2d_solver"].Simul
+              deltat_max=0.2, cfl_coef=None, type_time_scheme="RK4", N=None):
+    """A reference ns2d ``Simul`` wired around ``oper`` (with ``N`` given:
+    the ns2d.strat ``Simul``, ``StateNS2DStrat`` and its time stepping)."""
+    strat = N is not None
+    Simul = (mods["ns2d_strat_solver"] if strat else mods["ns2d_solver"]).Simul
+    State = mods["ns2d_strat_state"].StateNS2DStrat if strat else mods["ns2d_state"].StateNS2D
     sim = object.__new__(Simul)
+    extra = {"beta": beta}
+    if strat:
+        extra["N"] = N
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
-                         deltat_max, cfl_coef, {"beta": beta}, type_time_scheme)
+                         deltat_max, cfl_coef, extra, type_time_scheme)
+    sim.params.time_stepping.cfl_coef_group = None
     if type_time_scheme.endswith("_random"):
         oper = copy.copy(oper)
         oper.get_phases_random = types.MethodType(mods["get_phases_random_2d"], oper)
     info = _Container(solver=_Container(classes=_Container(State=_Container())))
-    mods["ns2d_state"].StateNS2D._complete_info_solver(info.solver)
+    State._complete_info_solver(info.solver)
     sim.info = info
     sim.oper = oper
     sim.output = _OutputStub()
     sim.is_forcing_enabled = False
-    sim.state = mods["ns2d_state"].StateNS2D(sim)
+    sim.state = State(sim)
     sim.state.state_spect[:] = 0.0
     sim.state.state_phys[:] = 0.0
-    sim.time_stepping = mods["ts_ps"].TimeSteppingPseudoSpectral(sim)
+    if strat:
+        sim.time_stepping = mods["ns2d_strat_ts"].TimeSteppingPseudoSpectralStrat(sim)
+    else:
+        sim.time_stepping = mods["ts_ps"].TimeSteppingPseudoSpectral(sim)
     return sim
 
 

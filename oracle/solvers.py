@@ -387,6 +387,105 @@ class NS2DOracle(_SolverBase):
         }
 
 
+class NS2DStratOracle(NS2DOracle):
+    """ns2d.strat: ``fluidsim/solvers/ns2d/strat/solver.py`` (tendencies
+    101-210), ``state.py`` (keys), ``time_stepping.py`` (CFL with the
+    dispersion-relation time, 31-70, 158-198)."""
+
+    nvar = 2
+    keys_phys = ("ux", "uy", "rot", "b")  # ns2d/strat/state.py:33
+
+    def __init__(self, oper: OperNumpy2D, N=1.0, cfl_coef_group=None, **kw):
+        self.N = N
+        if cfl_coef_group:
+            raise NotImplementedError("the group-velocity time of ns2d.strat")
+        super().__init__(oper, beta=0.0, **kw)
+        # time_stepping.py:55-70 and solver.py:215-225 (compute_dispersion_relation)
+        freq_disp = (N * (oper.KX / oper.K_not0)).max()
+        self.deltat_dispersion_relation = 1.0 * (2.0 * np.pi / freq_disp)
+
+    def statephys_from_statespect(self):
+        super().statephys_from_statespect()
+        self.state_phys[3] = self.oper.ifft(self.state_spect[1])
+
+    def init_from_rotbfft(self, rot_fft, b_fft):
+        rot_fft = np.array(rot_fft, dtype=np.complex128)
+        b_fft = np.array(b_fft, dtype=np.complex128)
+        self.oper.dealiasing(rot_fft)
+        self.oper.dealiasing(b_fft)
+        self.state_spect[0] = rot_fft
+        self.state_spect[1] = b_fft
+        self.statephys_from_statespect()
+
+    def tendencies_nonlin(self, state_spect=None):
+        """``ns2d/strat/solver.py:143-192`` and
+        ``tendencies_nonlin_ns2dstrat`` 27-32."""
+        oper = self.oper
+        if state_spect is None:
+            rot_fft, b_fft = self.state_spect[0], self.state_spect[1]
+            ux, uy = self.state_phys[0], self.state_phys[1]
+        else:
+            rot_fft, b_fft = state_spect[0], state_spect[1]
+            ux_fft, uy_fft = oper.vecfft_from_rotfft(rot_fft)
+            ux = oper.ifft(ux_fft)
+            uy = oper.ifft(uy_fft)
+        px_rot_fft, py_rot_fft = oper.gradfft_from_fft(rot_fft)
+        px_b_fft, py_b_fft = oper.gradfft_from_fft(b_fft)
+        px_rot, py_rot = oper.ifft(px_rot_fft), oper.ifft(py_rot_fft)
+        px_b, py_b = oper.ifft(px_b_fft), oper.ifft(py_b_fft)
+        f_rot = -ux * px_rot - uy * py_rot
+        f_b = -ux * px_b - uy * py_b - self.N**2 * uy
+        F = np.empty_like(self.state_spect)
+        F[1] = oper.fft(f_b)
+        F[0] = oper.fft(f_rot)
+        F[0] += px_b_fft
+        oper.dealiasing(F[0])
+        oper.dealiasing(F[1])
+        return F
+
+    def one_time_step_computation(self):
+        """``pseudo_spect.py:236-243`` (dealiasing of every variable)."""
+        self.time_step()
+        self.oper.dealiasing(self.state_spect[0])
+        self.oper.dealiasing(self.state_spect[1])
+        self.statephys_from_statespect()
+        if np.isnan(np.sum(self.state_spect[0])):
+            raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")
+
+    def compute_time_increment_CLF(self):
+        """``time_stepping.py:158-198`` (``_compute_time_increment_CFL_uxuyb``,
+        no group-velocity term, no forcing)."""
+        ux, uy = self.state_phys[0], self.state_phys[1]
+        freq_CFL = abs(ux).max() / self.oper.deltax + abs(uy).max() / self.oper.deltay
+        deltat_CFL = self.CFL / freq_CFL if freq_CFL > 0 else self.deltat_max
+        maybe_new_dt = min(deltat_CFL, self.deltat_dispersion_relation, self.deltat_max)
+        normalize_diff = abs(self.deltat - maybe_new_dt) / maybe_new_dt
+        if normalize_diff > 0.02:
+            self.deltat = maybe_new_dt
+
+    # ns2d/strat/output/__init__.py:85-109 (compute_energies_fft)
+    def energyA_fft(self):
+        if self.N == 0:
+            return np.zeros(self.oper.shapeK)
+        return ((np.abs(self.state_spect[1]) / self.N) ** 2) / 2
+
+    def compute_energy(self):
+        return self.oper.sum_wavenumbers(self.energy_fft() + self.energyA_fft())
+
+    def spatial_means(self):
+        """``ns2d/strat/output/spatial_means.py:23-55`` (no forcing)."""
+        f_d, f_d_hypo = compute_freq_diss(self.oper, self.nu_2, self.nu_4,
+                                          self.nu_8, self.nu_m4)
+        ek, ea, z = self.energy_fft(), self.energyA_fft(), self.enstrophy_fft()
+        s = self.oper.sum_wavenumbers
+        return {
+            "E": s(ek + ea), "EK": s(ek), "EA": s(ea), "Z": s(z),
+            "epsK": s(f_d * 2.0 * ek), "epsK_hypo": s(f_d_hypo * 2.0 * ek),
+            "epsA": s(f_d * 2.0 * ea), "epsA_hypo": s(f_d_hypo * 2.0 * ea),
+            "epsZ": s(f_d * 2.0 * z), "epsZ_hypo": s(f_d_hypo * 2.0 * z),
+        }
+
+
 class NS3DOracle(_SolverBase):
     """ns3d: ``fluidsim/solvers/ns3d/solver.py``, ``time_stepping.py``."""
 

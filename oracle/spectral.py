@@ -309,6 +309,7 @@ class OperNumpy2D:
         self.K8 = self.K4**2
         self.K2_not0 = np.copy(self.K2)
         self.K2_not0[0, 0] = 1e-14
+        self.K_not0 = np.sqrt(self.K2_not0)  # fluidfft's K_not0 (|k|, 1e-7 at k = 0)
         self.inv_K_square_nozero = 1.0 / self.K2_not0
         self.inv_K_square_nozero[0, 0] = 0.0
         self.kcut = (

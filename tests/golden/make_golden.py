@@ -25,7 +25,7 @@ sys.path.insert(0, str(HERE.parent.parent))
 
 from oracle import refshim  # noqa: E402
 from oracle.spectral import OperNumpy2D, OperNumpy3D  # noqa: E402
-from oracle.solvers import NS2DOracle, NS3DOracle, NS3DStratOracle  # noqa: E402
+from oracle.solvers import NS2DOracle, NS2DStratOracle, NS3DOracle, NS3DStratOracle  # noqa: E402
 from oracle.turb import smagorinsky_forcing  # noqa: E402
 from fluidsim_gb300.init_fields import (  # noqa: E402
     isotropic_3d, noise_rot_2d, taylor_green_3d)
@@ -60,6 +60,14 @@ CASES_2D = [
          USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
          type_time_scheme="RK2_phaseshift_random", phase_seed=102,
          init=dict(kmin=2.0, kmax=9.0, seed=14), steps=10),
+    dict(name="ns2d_strat_64x32", nx=64, ny=32, Lx=2 * pi, Ly=pi, nu_2=1e-3, N=1.5,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         init=dict(kmin=2.0, kmax=8.0, seed=15), b_init=dict(kmin=2.0, kmax=6.0, seed=16),
+         steps=10),
+    dict(name="ns2d_strat_64_rk2", nx=64, ny=64, Lx=6.0, Ly=6.0, nu_8=1e-9, N=3.0,
+         USE_CFL=False, deltat0=5e-3, type_time_scheme="RK2",
+         init=dict(kmin=2.0, kmax=10.0, seed=17), b_init=dict(kmin=3.0, kmax=9.0, seed=18),
+         steps=10),
 ]
 
 CASES_3D = [
@@ -152,13 +160,29 @@ def run_2d(mods, case):
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef", "type_time_scheme"])
     rng = _PhaseRNG(case.get("phase_seed"))
-    sim = rng.run("ref", lambda: refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0), **kw))
-    sim.state.init_from_rotfft(rot0.copy())
+    strat = case.get("N") is not None
+    sim = rng.run("ref", lambda: refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0),
+                                                    N=case.get("N"), **kw))
+    if strat:  # rot and b, dealiased, then the phys/spect round trip
+        b0 = noise_rot_2d(case["nx"], case["ny"], case["Lx"], case["Ly"], **case["b_init"])
+        r, b = rot0.copy(), b0.copy()
+        oper.dealiasing(r)
+        oper.dealiasing(b)
+        sim.state.state_spect.set_var("rot_fft", r)
+        sim.state.state_spect.set_var("b_fft", b)
+        sim.state.statephys_from_statespect()
+    else:
+        sim.state.init_from_rotfft(rot0.copy())
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
     tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
-    orc = rng.run("orc", lambda: NS2DOracle(oper, beta=case.get("beta", 0.0), **kw))
-    orc.init_from_rotfft(rot0.copy())
+    if strat:
+        orc = NS2DStratOracle(oper, N=case["N"], **kw)
+        orc.init_from_rotbfft(rot0.copy(), b0.copy())
+    else:
+        orc = rng.run("orc", lambda: NS2DOracle(oper, beta=case.get("beta", 0.0), **kw))
+        orc.init_from_rotfft(rot0.copy())
+    assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
                                rtol=0, atol=1e-13 * np.abs(tend0).max())
     out = dict(S_init=S_init, phys_init=phys_init, tend0=tend0, dts=[], E=[])

@@ -18,11 +18,14 @@ TOL_F32 = 1e-5
 
 def make_sim(name, precision="float64"):
     import torch
-    from fluidsim_gb300.solvers import SimulNS2D, SimulNS3D, SimulNS3DStrat
+    from fluidsim_gb300.solvers import SimulNS2D, SimulNS2DStrat, SimulNS3D, SimulNS3DStrat
     d, p = load(name)
     ndim = 2 if name.startswith("ns2d") else 3
-    Simul = SimulNS2D if ndim == 2 else (SimulNS3DStrat if p.get("N") is not None
-                                         else SimulNS3D)
+    strat = p.get("N") is not None
+    if ndim == 2:
+        Simul = SimulNS2DStrat if strat else SimulNS2D
+    else:
+        Simul = SimulNS3DStrat if strat else SimulNS3D
     params = Simul.create_default_params()
     if p.get("N") is not None:
         params.N = p["N"]
@@ -104,7 +107,7 @@ def test_ten_steps_fp64(cuda, name):
                                   "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f", "ns2d_32_rk2ps",
                                   "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f",
                                   "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f",
-                                  "ns2d_32_eulerpsr"])
+                                  "ns2d_32_eulerpsr", "ns2d_strat_64_rk2"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()
@@ -113,7 +116,7 @@ def test_ten_steps_fp32(cuda, name):
 
 
 @pytest.mark.parametrize("name", ["ns2d_48x40_beta", "ns3d_iso_24x16x32_f",
-                                  "ns3d_strat_64x32x32"])
+                                  "ns3d_strat_64x32x32", "ns2d_strat_64x32"])
 def test_spatial_means_match_oracle(cuda, name):
     from test_oracle_golden import make_oracle
     sim, d, _ = make_sim(name)

@@ -12,7 +12,7 @@ import pytest
 
 from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, solver_kwargs
 from oracle.spectral import OperNumpy2D, OperNumpy3D
-from oracle.solvers import NS2DOracle, NS3DOracle, NS3DStratOracle
+from oracle.solvers import NS2DOracle, NS2DStratOracle, NS3DOracle, NS3DStratOracle
 from oracle.turb import smagorinsky_forcing
 
 
@@ -22,7 +22,10 @@ def make_oracle(name):
         random.seed(int(p["phase_seed"]))
     if name.startswith("ns2d"):
         oper = OperNumpy2D(int(p["nx"]), int(p["ny"]), *lengths(p, 2))
-        orc = NS2DOracle(oper, beta=p.get("beta") or 0.0, **solver_kwargs(p))
+        if p.get("N") is not None:
+            orc = NS2DStratOracle(oper, N=p["N"], **solver_kwargs(p))
+        else:
+            orc = NS2DOracle(oper, beta=p.get("beta") or 0.0, **solver_kwargs(p))
     else:
         oper = OperNumpy3D(int(p["nx"]), int(p["ny"]), int(p["nz"]), *lengths(p, 3))
         turb = None
@@ -78,7 +81,13 @@ def test_reference_tendency_conserves_energy(name):
     orc, d, p = make_oracle(name)
     S, F = d["S_init"], d["tend0"]
     T = np.real(np.conj(F) * S)
-    if p.get("N") is not None:  # ns3d/strat/test_solver.py:34-58: b weighted by 1/N^2
+    if p.get("N") is not None and name.startswith("ns2d"):
+        # ns2d/strat/solver.py:212-240 (check_energy_conservation): kinetic
+        # energy from the vorticity (1 / k^2, 0 at k = 0) plus b / N^2
+        inv_k2 = orc.oper.inv_K_square_nozero
+        T = 0.5 * inv_k2 * T[0] + T[1] / (2 * p["N"] ** 2)
+        T = T[None]
+    elif p.get("N") is not None:  # ns3d/strat/test_solver.py:34-58: b weighted by 1/N^2
         T[3] /= p["N"] ** 2
     T = T.sum(axis=0)
     ratio = orc.oper.sum_wavenumbers(T) / orc.oper.sum_wavenumbers(np.abs(T))
