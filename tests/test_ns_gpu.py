@@ -152,6 +152,22 @@ def test_strat_tendency_conserves_energy_gpu(cuda):
     assert abs(ratio) < 1e-14
 
 
+def test_strat2d_tendency_conserves_energy_gpu(cuda):
+    """``ns2d/strat/solver.py:212-240`` (check_energy_conservation) on the
+    GPU path: kinetic (from the vorticity) plus potential energy transfer."""
+    sim, d, p = make_sim("ns2d_strat_64x32")
+    S = sim.state.state_spect
+    F = sim.tendencies_nonlin(S)
+    T = (F.conj() * S).real
+    k2 = sim.oper.K2.clone()
+    k2[0, 0] = 1.0
+    TK = 0.5 * T[0] / k2
+    TK[0, 0] = 0.0
+    T = TK + T[1] / (2 * p["N"] ** 2)
+    ratio = sim.oper.sum_wavenumbers(T) / sim.oper.sum_wavenumbers(T.abs())
+    assert abs(ratio) < 1e-14
+
+
 def test_nan_raises_value_error(cuda):
     sim, d, _ = make_sim("ns2d_32_cfl")
     sim.params.time_stepping.USE_CFL = False
