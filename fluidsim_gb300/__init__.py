@@ -11,11 +11,12 @@ from .fft import FFT2DGB300, FFT3DGB300, import_fft_class
 from .params import Parameters
 
 __all__ = ["FFT2DGB300", "FFT3DGB300", "import_fft_class", "Parameters",
-           "SimulNS2D", "SimulNS2DStrat", "SimulNS3D", "SimulNS3DStrat"]
+           "SimulNS2D", "SimulNS2DStrat", "SimulNS2DBouss", "SimulNS3D", "SimulNS3DStrat",
+           "SimulNS3DBouss"]
 
 
 def __getattr__(name):
-    if name in ("SimulNS2D", "SimulNS2DStrat", "SimulNS3D", "SimulNS3DStrat"):
+    if name in __all__[4:]:
         from . import solvers
         return getattr(solvers, name)
     raise AttributeError(name)

@@ -55,7 +55,7 @@ class NSParams(ctypes.Structure):
         ("kcut_x", ctypes.c_int64), ("kcut_y", ctypes.c_int64),
         ("kcut_z", ctypes.c_int64),
         ("dtype", ctypes.c_int),
-        ("strat", ctypes.c_int), ("N", ctypes.c_double),
+        ("strat", ctypes.c_int), ("N", ctypes.c_double), ("bouss", ctypes.c_int),
     ]
 
 

@@ -1184,7 +1184,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
     g.k2_hypo0 = q.k2_hypo0;
     g.has_f = q.has_f;
     g.strat = p.strat ? 1 : 0;
-    g.N2 = p.N * p.N;
+    g.N2 = p.bouss ? 0.0 : p.N * p.N;
   }
   if (!rc) {
     // tmp / tmp1 start at zero so that modes never written stay zero

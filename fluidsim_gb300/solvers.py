@@ -482,6 +482,8 @@ class SimulNS2DStrat(SimulNS2D):
     def deltat_cap(self):
         """``time_stepping.py:55-70`` with ``compute_dispersion_relation``
         (``solver.py:215-225``): 2 pi / max(N KX / K_not0)."""
+        if not float(self.params.N):
+            return np.inf
         o = self.oper
         kx = o.deltakx * np.arange(o.nx // 2 + 1)
         ky = o.deltaky * np.fft.fftfreq(o.ny, 1.0 / o.ny)
@@ -509,6 +511,29 @@ class SimulNS2DStrat(SimulNS2D):
             self.oper.dealiasing(t)
             fields.append(t)
         self.state.init_statespect_from(rot_fft=fields[0], b_fft=fields[1])
+
+
+class SimulNS2DBouss(SimulNS2DStrat):
+    """``fluidsim.solvers.ns2d.bouss.solver.Simul`` on GB300: Boussinesq
+    with the buoyancy along y, tendencies ``-u.grad(rot) + d_x b`` and
+    ``-u.grad(b)`` (``ns2d/bouss/solver.py:22-27,60-160``): the ns2d.strat
+    equations with N = 0, the plain ns2d time stepping and energy."""
+
+    _means_keys = SimulNS2DStrat._means_keys
+
+    @staticmethod
+    def _complete_params_with_default(params):
+        SimulNS2D._complete_params_with_default(params)
+
+    def __init__(self, params):
+        params._set_attribs({"N": 0.0})
+        super().__init__(params)
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        p.N = 0.0
+        p.bouss = 1
+        return p
 
 
 class SimulNS3D(_SimulBase):
@@ -620,3 +645,15 @@ class SimulNS3DStrat(SimulNS3D):
         X = self.state.state_phys
         self.oper.opfft.fft_as_arg(X.contiguous(), self.state.state_spect)
         self.state._phys = None
+
+
+class SimulNS3DBouss(SimulNS3DStrat):
+    """``fluidsim.solvers.ns3d.bouss.solver.Simul`` on GB300: the ns3d.strat
+    tendencies without the -N^2 v_z term (``ns3d/bouss/solver.py:48-160``);
+    params.N (default 1) only weights the potential energy of the outputs,
+    as in the reference, whose bouss solver keeps the strat output."""
+
+    def _ns_params(self):
+        p = super()._ns_params()
+        p.bouss = 1
+        return p

@@ -98,9 +98,15 @@ typedef struct gbs_ns_params {
   int has_f;    /* ns3d: 1 when params.f is not None                   */
   int64_t kcut_x, kcut_y, kcut_z;
   int dtype;
-  int strat;    /* ns3d.strat (fluidsim/solvers/ns3d/strat/solver.py): state
-                   (vx, vy, vz, b), power-of-two grids only              */
-  double N;     /* ns3d.strat: Brunt-Vaisala frequency (params.N)        */
+  int strat;    /* buoyancy solvers, power-of-two grids only: ns3d.strat
+                   (fluidsim/solvers/ns3d/strat/solver.py), state
+                   (vx, vy, vz, b); ns2d.strat (ns2d/strat/solver.py),
+                   state (rot, b)                                        */
+  double N;     /* Brunt-Vaisala frequency (params.N): the -N^2 v_z (u_y)
+                   term of the b tendency and EA = |b|^2 / (2 N^2)       */
+  int bouss;    /* with strat: ns3d.bouss / ns2d.bouss (ns3d/bouss/
+                   solver.py, ns2d/bouss/solver.py), the same tendencies
+                   without the -N^2 v_z term (N then only sets EA)       */
 } gbs_ns_params;
 
 int gbs_ns_create(const gbs_ns_params* params, gbs_ns** solver);

@@ -233,11 +233,19 @@ def load_reference(root):
                                     fs / "solvers" / "ns2d" / "strat" / "state.py")
     m["ns2d_strat_ts"] = _module("fluidsim.solvers.ns2d.strat.time_stepping",
                                  fs / "solvers" / "ns2d" / "strat" / "time_stepping.py")
+    _module("fluidsim.solvers.ns2d.bouss", package=True)
+    m["ns2d_bouss_solver"] = _module("fluidsim.solvers.ns2d.bouss.solver",
+                                     fs / "solvers" / "ns2d" / "bouss" / "solver.py")
+    m["ns2d_bouss_state"] = _module("fluidsim.solvers.ns2d.bouss.state",
+                                    fs / "solvers" / "ns2d" / "bouss" / "state.py")
     _module("fluidsim.solvers.ns3d.strat", package=True)
     m["ns3d_strat_solver"] = _module("fluidsim.solvers.ns3d.strat.solver",
                                      fs / "solvers" / "ns3d" / "strat" / "solver.py")
     m["ns3d_strat_state"] = _module("fluidsim.solvers.ns3d.strat.state",
                                     fs / "solvers" / "ns3d" / "strat" / "state.py")
+    _module("fluidsim.solvers.ns3d.bouss", package=True)
+    m["ns3d_bouss_solver"] = _module("fluidsim.solvers.ns3d.bouss.solver",
+                                     fs / "solvers" / "ns3d" / "bouss" / "solver.py")
 
     # the reference's toroidal / poloidal projectors (methods of its
     # OperatorsPseudoSpectral3D, whose module needs fluidfft): their function
@@ -305,12 +313,19 @@ def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
 
 def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, beta=0.0, USE_CFL=False, deltat0=0.2,
-              deltat_max=0.2, cfl_coef=None, type_time_scheme="RK4", N=None):
+              deltat_max=0.2, cfl_coef=None, type_time_scheme="RK4", N=None,
+              bouss=False):
     """A reference ns2d ``Simul`` wired around ``oper`` (with ``N`` given:
-    the ns2d.strat ``Simul``, ``StateNS2DStrat`` and its time stepping)."""
+    the ns2d.strat ``Simul``, ``StateNS2DStrat`` and its time stepping; with
+    ``bouss``: the ns2d.bouss ``Simul`` and ``StateNS2DBouss``)."""
     strat = N is not None
-    Simul = (mods["ns2d_strat_solver"] if strat else mods["ns2d_solver"]).Simul
-    State = mods["ns2d_strat_state"].StateNS2DStrat if strat else mods["ns2d_state"].StateNS2D
+    if bouss:
+        Simul = mods["ns2d_bouss_solver"].Simul
+        State = mods["ns2d_bouss_state"].StateNS2DBouss
+    else:
+        Simul = (mods["ns2d_strat_solver"] if strat else mods["ns2d_solver"]).Simul
+        State = (mods["ns2d_strat_state"].StateNS2DStrat if strat
+                 else mods["ns2d_state"].StateNS2D)
     sim = object.__new__(Simul)
     extra = {"beta": beta}
     if strat:
@@ -340,11 +355,13 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
               cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4",
-              projection=None, no_vz_kz0=False, N=None):
+              projection=None, no_vz_kz0=False, N=None, bouss=False):
     """A reference ns3d ``Simul`` wired around ``oper`` (with ``N`` given:
-    the ns3d.strat ``Simul`` and ``StateNS3DStrat``)."""
+    the ns3d.strat ``Simul`` and ``StateNS3DStrat``; with ``bouss`` as well:
+    the ns3d.bouss ``Simul``, whose tendencies do not use N)."""
     strat = N is not None
-    Simul = (mods["ns3d_strat_solver"] if strat else mods["ns3d_solver"]).Simul
+    Simul = (mods["ns3d_bouss_solver"] if bouss else
+             mods["ns3d_strat_solver"] if strat else mods["ns3d_solver"]).Simul
     State = mods["ns3d_strat_state"].StateNS3DStrat if strat else mods["ns3d_state"].StateNS3D
     sim = object.__new__(Simul)
     extra = {"f": f, "no_vz_kz0": no_vz_kz0, "projection": projection}

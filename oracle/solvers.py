@@ -400,9 +400,11 @@ class NS2DStratOracle(NS2DOracle):
         if cfl_coef_group:
             raise NotImplementedError("the group-velocity time of ns2d.strat")
         super().__init__(oper, beta=0.0, **kw)
-        # time_stepping.py:55-70 and solver.py:215-225 (compute_dispersion_relation)
+        # time_stepping.py:55-70 and solver.py:215-225 (compute_dispersion_relation);
+        # N = 0 (ns2d.bouss: the plain ns2d time stepping) caps nothing
         freq_disp = (N * (oper.KX / oper.K_not0)).max()
-        self.deltat_dispersion_relation = 1.0 * (2.0 * np.pi / freq_disp)
+        self.deltat_dispersion_relation = (1.0 * (2.0 * np.pi / freq_disp) if freq_disp > 0
+                                           else np.inf)
 
     def statephys_from_statespect(self):
         super().statephys_from_statespect()
@@ -598,8 +600,12 @@ class NS3DStratOracle(NS3DOracle):
     nvar = 4
     keys_phys = ("vx", "vy", "vz", "b")  # ns3d/strat/state.py:18-24
 
-    def __init__(self, oper: OperNumpy3D, N=1.0, **kw):
+    def __init__(self, oper: OperNumpy3D, N=1.0, bouss=False, **kw):
+        """bouss: ns3d.bouss (``ns3d/bouss/solver.py:48-160``), the same
+        tendencies without the -N^2 vz term (its output still weights EA by
+        the strat class's params.N)."""
         self.N = N
+        self.bouss = bouss
         super().__init__(oper, **kw)
 
     def init_from_vxvyvzfft(self, vx_fft, vy_fft, vz_fft):
@@ -628,7 +634,10 @@ class NS3DStratOracle(NS3DOracle):
         F[2] = oper.fft(vx * oy - vy * ox)
         F[2] += b_fft
         div_vb_fft = oper.div_vb_fft_from_vb(vx, vy, vz, b)
-        F[3] = -div_vb_fft - self.N**2 * vz_fft  # compute_fb_fft, solver.py:19-23
+        if self.bouss:  # ns3d/bouss/solver.py:150-152
+            F[3] = -div_vb_fft
+        else:
+            F[3] = -div_vb_fft - self.N**2 * vz_fft  # compute_fb_fft, solver.py:19-23
         self.project_state_spect(F)
         oper.dealiasing(F)
         return F

@@ -64,6 +64,10 @@ CASES_2D = [
          USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
          init=dict(kmin=2.0, kmax=8.0, seed=15), b_init=dict(kmin=2.0, kmax=6.0, seed=16),
          steps=10),
+    dict(name="ns2d_bouss_64x32", nx=64, ny=32, Lx=2 * pi, Ly=pi, nu_2=1e-3, bouss=True,
+         USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None,
+         init=dict(kmin=2.0, kmax=8.0, seed=19), b_init=dict(kmin=2.0, kmax=6.0, seed=20),
+         steps=10),
     dict(name="ns2d_strat_64_rk2", nx=64, ny=64, Lx=6.0, Ly=6.0, nu_8=1e-9, N=3.0,
          USE_CFL=False, deltat0=5e-3, type_time_scheme="RK2",
          init=dict(kmin=2.0, kmax=10.0, seed=17), b_init=dict(kmin=3.0, kmax=9.0, seed=18),
@@ -115,6 +119,9 @@ CASES_3D = [
     dict(name="ns3d_strat_64x32x32", nx=64, ny=32, nz=32, Lx=2 * pi, Ly=pi, Lz=pi,
          nu_2=2e-3, N=2.0, USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=0.5,
          init="iso", seed=18, b_seed=19, steps=10),
+    dict(name="ns3d_bouss_32x32x64", nx=64, ny=32, nz=32, Lx=2 * pi, Ly=pi, Lz=pi,
+         nu_2=2e-3, N=1.0, bouss=True, USE_CFL=True, deltat0=0.2, deltat_max=0.2,
+         cfl_coef=0.5, init="iso", seed=24, b_seed=25, steps=10),
     dict(name="ns3d_strat_64_f_rk2", nx=64, ny=64, nz=64, nu_2=1e-3, N=4.0, f=0.5,
          USE_CFL=True, deltat0=0.2, deltat_max=0.2, cfl_coef=None, type_time_scheme="RK2",
          init="iso", seed=20, b_seed=21, steps=10),
@@ -160,9 +167,10 @@ def run_2d(mods, case):
     kw = _kw(case, ["nu_2", "nu_4", "nu_8", "nu_m4", "USE_CFL", "deltat0",
                     "deltat_max", "cfl_coef", "type_time_scheme"])
     rng = _PhaseRNG(case.get("phase_seed"))
-    strat = case.get("N") is not None
+    bouss = bool(case.get("bouss"))
+    strat = case.get("N") is not None or bouss
     sim = rng.run("ref", lambda: refshim.make_ns2d(mods, oper, beta=case.get("beta", 0.0),
-                                                    N=case.get("N"), **kw))
+                                                    N=case.get("N"), bouss=bouss, **kw))
     if strat:  # rot and b, dealiased, then the phys/spect round trip
         b0 = noise_rot_2d(case["nx"], case["ny"], case["Lx"], case["Ly"], **case["b_init"])
         r, b = rot0.copy(), b0.copy()
@@ -176,8 +184,8 @@ def run_2d(mods, case):
     S_init = np.array(sim.state.state_spect)
     phys_init = np.array(sim.state.state_phys)
     tend0 = np.array(sim.tendencies_nonlin(state_spect=sim.state.state_spect))
-    if strat:
-        orc = NS2DStratOracle(oper, N=case["N"], **kw)
+    if strat:  # (ns2d.bouss: the strat equations with N = 0)
+        orc = NS2DStratOracle(oper, N=case.get("N") or 0.0, **kw)
         orc.init_from_rotbfft(rot0.copy(), b0.copy())
     else:
         orc = rng.run("orc", lambda: NS2DOracle(oper, beta=case.get("beta", 0.0), **kw))
@@ -219,7 +227,7 @@ def run_3d(mods, case):
     rng = _PhaseRNG(case.get("phase_seed"))
     sim = rng.run("ref", lambda: refshim.make_ns3d(
         mods, oper, f=case.get("f"), smagorinsky_C=case.get("smagorinsky_C"),
-        N=case.get("N"), **proj, **kw))
+        N=case.get("N"), bouss=bool(case.get("bouss")), **proj, **kw))
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
     if strat:  # a buoyancy field as well (set after the velocity round trip)
         b0 = isotropic_3d(nx, ny, nz, *L, seed=case["b_seed"])[0]
@@ -235,7 +243,8 @@ def run_3d(mods, case):
         def turb(o, vx, vy, vz):
             return smagorinsky_forcing(o, vx, vy, vz, C=C)
     if strat:
-        orc = NS3DStratOracle(oper, N=case["N"], f=case.get("f"), **proj, **kw)
+        orc = NS3DStratOracle(oper, N=case["N"], f=case.get("f"), bouss=bool(case.get("bouss")),
+                              **proj, **kw)
     else:
         orc = rng.run("orc", lambda: NS3DOracle(oper, f=case.get("f"), turb_model=turb,
                                                 **proj, **kw))
@@ -268,7 +277,7 @@ def run_3d(mods, case):
 def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
             "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
-            "smagorinsky_C", "N", "phase_seed"]
+            "smagorinsky_C", "N", "phase_seed", "bouss"]
     out = {("p_" + k): np.asarray(case[k] if case.get(k) is not None else np.nan,
                                   dtype=np.float64)
            for k in keys if k in case}

@@ -7,12 +7,13 @@ import numpy as np
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES_2D = ["ns2d_32_cfl", "ns2d_48x40_beta", "ns2d_256_c1", "ns2d_32_euler", "ns2d_40x32_rk2",
             "ns2d_32_rk2ps", "ns2d_36x32_eulerps", "ns2d_32_eulerpsr", "ns2d_40x32_rk2psr",
-            "ns2d_strat_64x32", "ns2d_strat_64_rk2"]
+            "ns2d_strat_64x32", "ns2d_strat_64_rk2", "ns2d_bouss_64x32"]
 CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20x24x16",
             "ns3d_rk2_20x15x10", "ns3d_heun_24x16x32_f", "ns3d_euler_tgv_32",
             "ns3d_rk2ps_20x15x10", "ns3d_rk2psx_16x24x32_f", "ns3d_eulerps_32",
             "ns3d_toroidal_24x20x16", "ns3d_poloidal_32_novz", "ns3d_strat_64x32x32",
-            "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f", "ns3d_eulerpsr_32"]
+            "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f", "ns3d_eulerpsr_32",
+            "ns3d_bouss_32x32x64"]
 PROJECTIONS = {0: None, 1: "toroidal", 2: "poloidal"}
 SCHEME_NAMES = {0: "RK4", 1: "Euler", 2: "RK2", 3: "RK2_trapezoid", 4: "Euler_phaseshift",
                 5: "RK2_phaseshift", 6: "RK2_phaseshift_exact", 7: "Euler_phaseshift_random",

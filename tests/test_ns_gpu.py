@@ -18,14 +18,15 @@ TOL_F32 = 1e-5
 
 def make_sim(name, precision="float64"):
     import torch
-    from fluidsim_gb300.solvers import SimulNS2D, SimulNS2DStrat, SimulNS3D, SimulNS3DStrat
+    from fluidsim_gb300.solvers import (SimulNS2D, SimulNS2DBouss, SimulNS2DStrat, SimulNS3D,
+                                        SimulNS3DBouss, SimulNS3DStrat)
     d, p = load(name)
     ndim = 2 if name.startswith("ns2d") else 3
     strat = p.get("N") is not None
     if ndim == 2:
-        Simul = SimulNS2DStrat if strat else SimulNS2D
+        Simul = SimulNS2DBouss if p.get("bouss") else (SimulNS2DStrat if strat else SimulNS2D)
     else:
-        Simul = SimulNS3DStrat if strat else SimulNS3D
+        Simul = SimulNS3DBouss if p.get("bouss") else (SimulNS3DStrat if strat else SimulNS3D)
     params = Simul.create_default_params()
     if p.get("N") is not None:
         params.N = p["N"]

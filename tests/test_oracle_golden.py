@@ -22,8 +22,8 @@ def make_oracle(name):
         random.seed(int(p["phase_seed"]))
     if name.startswith("ns2d"):
         oper = OperNumpy2D(int(p["nx"]), int(p["ny"]), *lengths(p, 2))
-        if p.get("N") is not None:
-            orc = NS2DStratOracle(oper, N=p["N"], **solver_kwargs(p))
+        if p.get("N") is not None or p.get("bouss"):
+            orc = NS2DStratOracle(oper, N=p.get("N") or 0.0, **solver_kwargs(p))
         else:
             orc = NS2DOracle(oper, beta=p.get("beta") or 0.0, **solver_kwargs(p))
     else:
@@ -35,8 +35,8 @@ def make_oracle(name):
             def turb(o, vx, vy, vz):
                 return smagorinsky_forcing(o, vx, vy, vz, C=C)
         if p.get("N") is not None:
-            orc = NS3DStratOracle(oper, N=p["N"], f=p.get("f"), **projection_kwargs(p),
-                                  **solver_kwargs(p))
+            orc = NS3DStratOracle(oper, N=p["N"], f=p.get("f"), bouss=bool(p.get("bouss")),
+                                  **projection_kwargs(p), **solver_kwargs(p))
         else:
             orc = NS3DOracle(oper, f=p.get("f"), turb_model=turb, **projection_kwargs(p),
                              **solver_kwargs(p))
@@ -81,6 +81,10 @@ def test_reference_tendency_conserves_energy(name):
     orc, d, p = make_oracle(name)
     S, F = d["S_init"], d["tend0"]
     T = np.real(np.conj(F) * S)
+    if p.get("bouss"):
+        # the bouss equations exchange kinetic energy with b (the buoyancy
+        # force does work) and have no N^2 term to close a quadratic budget
+        pytest.skip("bouss: no conserved quadratic energy")
     if p.get("N") is not None and name.startswith("ns2d"):
         # ns2d/strat/solver.py:212-240 (check_energy_conservation): kinetic
         # energy from the vorticity (1 / k^2, 0 at k = 0) plus b / N^2
