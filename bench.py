@@ -192,6 +192,29 @@ def ncu_traffic(kind, n):
     return None
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the
+    platform string)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part", "hardware"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(n, v0, reps=1):
     """Oracle (float64, scipy.fft on all cores): one tendency evaluation."""
     from oracle.solvers import NS3DOracle
@@ -206,6 +229,7 @@ def cpu_sample(n, v0, reps=1):
         orc.tendencies_nonlin(S)
     dt = (time.perf_counter() - t0) / reps
     return {"value": 1.0 / (4 * dt), "unit": "steps/s", "cores": WORKERS, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": (f"{reps} tendencies_nonlin evaluation(s) of the float64 oracle at "
                        f"{n}^3 (9 FFTs + curl, v x omega, projection, dealiasing), "
                        f"{dt:.2f} s each, x4 for one RK4 step (elementwise RK updates "
@@ -400,6 +424,12 @@ def main():
                 "kernel_ms": {k: v["ms"] / max(v["launches"], 1) for k, v in kinds.items()},
                 "kernel_share": {k: v["ms"] / sum(x["ms"] for x in kinds.values())
                                  for k, v in kinds.items()}}
+    # whole pruned step: the algorithmic bytes of its 20 launches against
+    # the peak at the measured step rate
+    step_bytes = 4 * sum(fpl.values()) * field_bytes
+    step_gbs = step_bytes * steps_per_s / world / 1e9
+    roofline["step"] = {"alg_bytes_per_step": step_bytes, "achieved": step_gbs,
+                        "frac": step_gbs / peak, "unit": "GB/s"}
 
     # end to end: host state in pinned memory, copied in and out every step
     S = sim.state.state_spect
