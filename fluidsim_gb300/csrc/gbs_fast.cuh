@@ -89,20 +89,22 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
-// Block coordinates of the CTA d places after this one in launch order (x
-// fastest); false for d <= 0 or past the end of the grid.  CTAs start about
-// in this order, so with d = the number of CTAs resident on the GPU the CTA
-// named starts about when this one ends: fetching its inputs into L2 now
-// overlaps their DRAM latency with this CTA's transforms.
-__device__ __forceinline__ bool cta_ahead(int d, int& bx, int& by, int& bz) {
-  if (d <= 0) return false;
-  const int64_t gx = gridDim.x, gy = gridDim.y;
-  const int64_t lin = (blockIdx.z * gy + blockIdx.y) * gx + blockIdx.x + d;
-  if (lin >= gx * gy * gridDim.z) return false;
-  bx = (int)(lin % gx);
-  by = (int)((lin / gx) % gy);
-  bz = (int)(lin / (gx * gy));
-  return true;
+// Block coordinates of the CTA dy grid rows (dy * gridDim.x CTAs) after this
+// one in launch order (x fastest); false for dy <= 0 or past the end of the
+// grid.  CTAs start about in this order, so with dy * gridDim.x about the
+// number of CTAs resident on the GPU the CTA named starts about when this
+// one ends: fetching its inputs into L2 now overlaps their DRAM latency with
+// this CTA's transforms.  (Whole rows: no division by the grid size.)
+__device__ __forceinline__ bool cta_ahead(int dy, int& bx, int& by, int& bz) {
+  if (dy <= 0) return false;
+  bx = blockIdx.x;
+  by = blockIdx.y + dy;
+  bz = blockIdx.z;
+  if (by >= (int)gridDim.y) {  // dy < gridDim.y is checked on the host
+    by -= gridDim.y;
+    ++bz;
+  }
+  return bz < (int)gridDim.z;
 }
 
 // exp(-2 pi i r / 16), r = 0..8: the x-pass pre/post-processing twiddle of
@@ -225,7 +227,7 @@ struct ColArgs {
   int ncols;
   int kc_in, kc_out;
   int64_t es, os, fs;
-  int pf;  // L2 prefetch distance in CTAs (0: none); set by the launcher
+  int pf;  // L2 prefetch distance in grid rows (0: none); set by the launcher
 };
 
 template <typename T, int LOGN, int TX, int DIR>

@@ -99,10 +99,12 @@ static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, i
   if (rc) return rc;
   static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR>, TH, smem);
   ColArgs ap = a;
-  // only for row-strided columns (y passes): with plane strides (z passes)
-  // the next wave's tiles span every plane
-  ap.pf = a.es * (int64_t)sizeof(C) <= 65536 ? pf : 0;
   dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
+  // in grid rows (a resident wave of CTAs, rounded up); only for
+  // row-strided columns (y passes): with plane strides (z passes) the next
+  // wave's tiles span every plane
+  const int dy = (int)((pf + grid.x - 1) / grid.x);
+  ap.pf = (a.es * (int64_t)sizeof(C) <= 65536 && dy < (int)grid.y) ? dy : 0;
   kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
                                                  static_cast<C*>(out), ap,
                                                  static_cast<const C*>(tw), T(scale));
