@@ -63,6 +63,33 @@ __device__ __forceinline__ int swz(int q) {
   return q ^ ((q >> LG) & (E - 1));
 }
 
+// swz(b | K) from sb = swz(b), for b and K with no bit in common (b per
+// thread, K a compile-time constant of an unrolled loop): the swizzle is an
+// XOR with the bits of q above LG, so it splits over disjoint operands,
+// swz(b | K) = sb ^ swz(K), and the bits of swz(K) at or above E meet no bit
+// of sb (b and K are disjoint there, the XOR only reaches bits below E): one
+// XOR with a constant below E plus an immediate offset, instead of forming q
+// and its swizzle again for every access.
+template <typename C>
+__device__ __forceinline__ int swz_join(int sb, int K) {
+  constexpr int E = 128 / sizeof(C);
+  const int sK = swz<C>(K);
+  return (sb ^ (sK & (E - 1))) + (sK & ~(E - 1));
+}
+
+// Shared-memory view of the line(s) one thread works on: position p of its
+// line at buf[swz(p * TX + c)] (a tile of TX columns; rows: TX = 1, c = 0,
+// buf the row's slot, whose offset is a multiple of E).  base(b) / at(sb, K)
+// address position b | K (b and K disjoint) through swz_join.
+template <typename C, int TX>
+struct SwzView {
+  C* buf;
+  int c;
+  __device__ __forceinline__ C& operator()(int p) const { return buf[swz<C>(p * TX + c)]; }
+  __device__ __forceinline__ int base(int b) const { return swz<C>(b * TX + c); }
+  __device__ __forceinline__ C& at(int sb, int K) const { return buf[swz_join<C>(sb, K * TX)]; }
+};
+
 __device__ __forceinline__ bool kept(int p, int n, int kc) {
   return p < kc || p > n - kc;
 }
@@ -168,18 +195,20 @@ __device__ __forceinline__ void stage_twiddles(const C* __restrict__ tw, int k, 
 // WARP: every line lies inside one warp (rows with N/8 <= 32 threads and
 // the line index above jt), so the exchanges only need __syncwarp().
 template <int DIR, int LOGN, bool WARP = false, typename C, typename Acc>
-__device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
+__device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& acc,
                                     const C* __restrict__ tw, int tws) {
   using P = Line<LOGN>;
   constexpr int N = P::N, N8 = P::N8;
   if (active) dft8<DIR>(v);
+  // every exchange position below is (per-thread part) | (constant part)
+  const int sj = acc.base(jt);
 #pragma unroll
   for (int s = 1; s < P::NST; ++s) {
     const int Ns = 1 << (3 * (s - 1));  // radix-8 stage s-1 wrote with this Ns
     if (active) {
-      const int d = ((jt / Ns) * Ns << 3) + (jt % Ns);
+      const int sd = acc.base(((jt / Ns) * Ns << 3) + (jt % Ns));
 #pragma unroll
-      for (int r = 0; r < 8; ++r) acc(d + r * Ns) = v[r];
+      for (int r = 0; r < 8; ++r) acc.at(sd, r * Ns) = v[r];
     }
     if (WARP) __syncwarp(); else __syncthreads();
     const int Nsn = Ns << 3;
@@ -191,7 +220,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
         stage_twiddles<DIR, 8>(tw, bm * tm, w);
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          C x = acc(jt + r * N8);
+          C x = acc.at(sj, r * N8);
           if (r) x = cmul(x, w[r]);
           v[r] = x;
         }
@@ -207,7 +236,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, Acc acc,
           stage_twiddles<DIR, RL>(tw, bm * tm, w);
 #pragma unroll
           for (int r = 0; r < RL; ++r) {
-            C x = acc(b + r * (N / RL));
+            C x = acc.at(sj, g * N8 + r * (N / RL));
             if (r) x = cmul(x, w[r]);
             v[g * RL + r] = x;
           }
@@ -256,7 +285,7 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
     const int p = jt + r * P::N8;
     v[r] = (valid && kept(p, P::N, a.kc_in)) ? in[base + p * a.es] : mk<C>(0, 0);
   }
-  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  const SwzView<C, TX> acc{buf, c};
   run<DIR, LOGN>(v, jt, true, acc, tw, 1);
   if (!valid) return;
 #pragma unroll
@@ -289,11 +318,11 @@ kf_row_r2c(const T* __restrict__ x, cplx<T>* __restrict__ out, int64_t nrows,
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = valid ? xc[jt + r * M8] : mk<C>(0, 0);
   C* slot = buf + l * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
+  const SwzView<C, 1> acc{slot, 0};
   constexpr bool WARP = Line<LOGM>::N8 <= 32;
   run<-1, LOGM, WARP>(v, jt, true, acc, twx, 2);
 #pragma unroll
-  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   if (WARP) __syncwarp(); else __syncthreads();
   if (!valid) return;
   // X[k] and X[M - k] -> spectrum k = jt + r M/8 (and k = M for jt = 0),
@@ -342,7 +371,7 @@ kf_row_c2r(const cplx<T>* __restrict__ in, T* __restrict__ x, int64_t nrows,
     v[r] = Z;
   }
   C* slot = buf + l * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
+  const SwzView<C, 1> acc{slot, 0};
   run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
   if (!valid) return;
   C* xc = reinterpret_cast<C*>(x) + row * M;
@@ -417,7 +446,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const int64_t nK = plane * g.nz;
   const int64_t base = (int64_t)iy * g.nkx + ix;
   const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
-  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  const SwzView<C, TX> acc{buf, c};
   // job j: source field, whether it is multiplied by i kz
   //   0: Ty   1: Tx (-> vx, oz)   2: Tz   3: Dy (-> ox)   4: Dx (-> oy)   5: b
   auto src_of = [](int j) { return j == 0 || j == 3 ? 1 : (j == 1 || j == 4 ? 0 : (j == 2 ? 2 : 3)); };
@@ -539,7 +568,7 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const int64_t row = (int64_t)blockIdx.x * L + l;
   const bool valid = row < nrows;
   C* slot = buf + (f * L + l) * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
+  const SwzView<C, 1> acc{slot, 0};
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
   const C t0 = twx[jt];
@@ -562,16 +591,16 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
   run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
 #pragma unroll
-  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   __syncthreads();
   x_products<T, L, M, ST>(buf, nrows, vmax);
   const bool act = f < (ST ? 6 : 3);
 #pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(acc.base(jt), r * M8) : mk<C>(0, 0);
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+    for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   }
   __syncthreads();
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
@@ -646,11 +675,11 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
       __syncthreads();  // the slot becomes the exchange buffer
     }
     C* slot = buf + (ST && f > 3 ? 3 : f) * N * TX;
-    auto acc = [&](int p) -> C& { return slot[swz<C>(p * TX + c)]; };
+    const SwzView<C, TX> acc{slot, c};
     run<-1, LOGN>(v, jt, true, acc, twz, 1);
     if (!ST || f < 3) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = v[i];
+      for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * N8) = v[i];
     } else {
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
@@ -662,7 +691,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
       }
       if (f == 5) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * N8) = dv[i];
+        for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * N8) = dv[i];
       }
     }
   }
@@ -771,7 +800,7 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
   S += bid.z * nK;  // run of a batched ensemble
   W += bid.z * 4 * nK;
   const T kx = T(g.dkx * ix);
-  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  const SwzView<C, TX> acc{buf, c};
   // ns2d.strat: two more fields, d_x b and d_y b (b: the second state field)
 #pragma unroll 1
   for (int f = 0; f < (g.strat ? 6 : 4); ++f) {
@@ -837,7 +866,7 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   W += bid.y * 4 * nK;  // run of a batched ensemble
   F += bid.y * nK;
   C* slot = buf + (f * L + l) * LS;
-  auto acc = [&](int p) -> C& { return slot[padp<LOGM, C>(p)]; };
+  const SwzView<C, 1> acc{slot, 0};
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
   C v[8];
   const C t0 = twx[jt];
@@ -860,7 +889,7 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   }
   run<+1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, true, acc, twx, 2);
 #pragma unroll
-  for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+  for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   __syncthreads();
   T mx = 0, my = 0;
   const T beta = T(g.beta);
@@ -889,11 +918,11 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   if (vmax) block_max3(mx, my, T(0), vmax);
   const bool act = f < NFO;
 #pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = act ? acc(jt + r * M8) : mk<C>(0, 0);
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(acc.base(jt), r * M8) : mk<C>(0, 0);
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc(jt + P::outm(i) * M8) = v[i];
+    for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   }
   __syncthreads();
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
@@ -953,7 +982,7 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
 #pragma unroll
   for (int r = 0; r < 8; ++r)
     v[r] = valid ? F[(int64_t)(jt + r * P::N8) * g.nkx + ix] : mk<C>(0, 0);
-  auto acc = [&](int p) -> C& { return buf[swz<C>(p * TX + c)]; };
+  const SwzView<C, TX> acc{buf, c};
   run<-1, LOGN>(v, jt, true, acc, twy, 1);
   if (!valid) return;
   const T kx = T(g.dkx * ix);
