@@ -597,6 +597,8 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   const bool act = f < (ST ? 6 : 3);
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(acc.base(jt), r * M8) : mk<C>(0, 0);
+  // the line's first exchange overwrites positions other threads still read
+  if (Line<LOGM>::N8 <= 32) __syncwarp(); else __syncthreads();
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
@@ -618,6 +620,84 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const C wd = cmul(r < 8 ? twx_at(twx, t0, jt, r, M8) : twx[M], d);
       Fo[k] = mk<C>(h * (s.x + wd.y), h * (s.y - wd.x));
     }
+  }
+}
+
+// B, rows in pairs: rows 2 q and 2 q + 1 of a field travel as the real and
+// imaginary parts of one complex line of N = nx points.  With A0, A1 their
+// spectra extended by Hermitian symmetry (imaginary parts of k = 0 and
+// k = N/2 dropped, as a C2R transform does), Z = A0 + i A1 transforms back to
+// z = a0 + i a1; x_products works componentwise, so it forms the products of
+// both rows at once; and the forward transform Z of p0 + i p1 splits into
+//   P0[k] = (Z[k] + conj Z[N-k]) / 2,   P1[k] = (Z[k] - conj Z[N-k]) / 2i.
+// No pre- or post-processing twiddles (the half-length real transforms of
+// kf3_x spend about as many instructions on those as on a radix-8 stage).
+// LP row pairs per CTA; N/8 threads per line.
+template <typename T, int LOGN, int LP, bool ST>
+__global__ void __launch_bounds__((ST ? 7 : 6) * LP * (1 << LOGN) / 8,
+                                  min_blocks((ST ? 7 : 6) * LP * (1 << LOGN) / 8))
+kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
+       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  constexpr int N = P::N, N8 = P::N8, H = N / 2;
+  constexpr bool WARP = N8 <= 32;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % N8;
+  const int lp = (threadIdx.x / N8) % LP;
+  const int f = threadIdx.x / (N8 * LP);
+  const int64_t nrows = (int64_t)g.nz * g.ny;
+  const int64_t nK = nrows * g.nkx;
+  const int64_t row0 = ((int64_t)blockIdx.x * LP + lp) * 2;
+  const bool v0 = row0 < nrows, v1 = row0 + 1 < nrows;
+  const SwzView<C, 1> acc{buf + (f * LP + lp) * N, 0};
+  const int kcx = g.pr ? g.kcx : g.nkx + 1;
+  C v[8];
+  {
+    const C* r0 = W + f * nK + row0 * g.nkx;
+    const C* r1 = r0 + g.nkx;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      // k = jt + r N/8: k < N/2 for r < 4 (stored), else N - k (mirrored)
+      const int idx = r < 4 ? jt + r * N8 : (8 - r) * N8 - jt;
+      const bool in = idx < kcx;
+      C a0 = (v0 && in) ? r0[idx] : mk<C>(0, 0);
+      C a1 = (v1 && in) ? r1[idx] : mk<C>(0, 0);
+      if ((r == 0 || r == 4) && jt == 0) { a0.y = 0; a1.y = 0; }
+      v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
+    }
+  }
+  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1);
+  const int sj = acc.base(jt);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+  __syncthreads();
+  x_products<T, LP, N, ST>(buf, (nrows + 1) / 2, vmax);
+  const bool act = f < (ST ? 6 : 3);
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
+  // the line's first exchange overwrites positions other threads still read
+  if (WARP) __syncwarp(); else __syncthreads();
+  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1);
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+  }
+  __syncthreads();
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  if (!act) return;
+  C* F0 = F + f * nK + row0 * g.nkx;
+  C* F1 = F0 + g.nkx;
+  const T h = T(0.5);
+#pragma unroll
+  for (int r = 0; r <= 4; ++r) {
+    const int k = r < 4 ? jt + r * N8 : H;
+    if ((r == 4 && jt != 0) || k >= nout) continue;
+    // Z[k]: this thread's own register when the last stage is radix 8
+    const C z = (P::REM == 0 && r < 4) ? v[r] : acc(k);
+    const C m = acc((N - k) & (N - 1));
+    if (v0) F0[k] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
+    if (v1) F1[k] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
   }
 }
 
@@ -919,6 +999,8 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   const bool act = f < NFO;
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(acc.base(jt), r * M8) : mk<C>(0, 0);
+  // the line's first exchange overwrites positions other threads still read
+  if (Line<LOGM>::N8 <= 32) __syncwarp(); else __syncthreads();
   run<-1, LOGM, (Line<LOGM>::N8 <= 32)>(v, jt, act, acc, twx, 2);
   if (act) {
 #pragma unroll
