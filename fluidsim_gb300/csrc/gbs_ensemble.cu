@@ -445,6 +445,7 @@ int gbs_ens2d_create(int64_t nx, int64_t ny, double Lx, double Ly, int64_t nruns
   g.beta = beta;
   g.inv_n = 1.0 / ((double)nx * ny);
   g.k2_hypo0 = g.dkx * g.dkx;
+  gbs::fast::geo_f32(g);
   e->txA = 8;
   e->Lb = 2;
   e->txC = 8;

@@ -394,7 +394,39 @@ struct Geo {
   int proj, no_vz_kz0;   // ns3d projection of the tendencies and the state
   double N2;             // ns3d.strat: Brunt-Vaisala frequency squared
   int strat;             // ns3d.strat: 4 state fields (vx, vy, vz, b)
+  // float copies for the FP32 kernels (geo_f32)
+  float fdkx, fdky, fdkz, fnu2, fnu4, fnu8, fnum4, fk2_hypo0, fbeta, fN2, ff;
 };
+
+// Fill the float copies of a Geo's double parameters (host, after setting
+// them; the per-run overrides of an ensemble set their own on the device).
+inline void geo_f32(Geo& g) {
+  g.fdkx = (float)g.dkx;
+  g.fdky = (float)g.dky;
+  g.fdkz = (float)g.dkz;
+  g.fnu2 = (float)g.nu2;
+  g.fnu4 = (float)g.nu4;
+  g.fnu8 = (float)g.nu8;
+  g.fnum4 = (float)g.num4;
+  g.fk2_hypo0 = (float)g.k2_hypo0;
+  g.fbeta = (float)g.beta;
+  g.fN2 = (float)g.N2;
+  g.ff = (float)g.f;
+}
+
+// Wavenumber k dk in the kernels' type: FP64 forms the product in double,
+// FP32 multiplies dk rounded to float by the exact integer k (one rounding
+// more, and no FP64 instruction per mode).
+template <typename T>
+__device__ __forceinline__ T wavenum(double dk, float fdk, int k) {
+  if constexpr (sizeof(T) == 8) return dk * k;
+  else return fdk * (float)k;
+}
+template <typename T>
+__device__ __forceinline__ T par(double d, float f) {
+  if constexpr (sizeof(T) == 8) return d;
+  else return f;
+}
 
 // Per-run parameters of a batched ensemble (null pointers: single run).
 struct PerRun {
@@ -410,6 +442,11 @@ __device__ __forceinline__ Phys phys_of(const Geo& g) {
   q.nu8 = g.nu8;
   q.num4 = g.num4;
   q.k2_hypo0 = g.k2_hypo0;
+  q.fnu2 = g.fnu2;
+  q.fnu4 = g.fnu4;
+  q.fnu8 = g.fnu8;
+  q.fnum4 = g.fnum4;
+  q.fk2_hypo0 = g.fk2_hypo0;
   q.proj = g.proj;
   q.no_vz_kz0 = g.no_vz_kz0;
   return q;
@@ -445,7 +482,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
   const int64_t plane = (int64_t)g.ny * g.nkx;
   const int64_t nK = plane * g.nz;
   const int64_t base = (int64_t)iy * g.nkx + ix;
-  const T kx = T(g.dkx * ix), ky = T(g.dky * kadim(iy, g.ny));
+  const T kx = wavenum<T>(g.dkx, g.fdkx, ix), ky = wavenum<T>(g.dky, g.fdky, kadim(iy, g.ny));
   const SwzView<C, TX> acc{buf, c};
   // job j: source field, whether it is multiplied by i kz
   //   0: Ty   1: Tx (-> vx, oz)   2: Tz   3: Dy (-> ox)   4: Dx (-> oy)   5: b
@@ -475,12 +512,12 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
       const int p = jt + r * P::N8;
       C x = v[r];
       if (dz) {
-        const T kz = T(g.dkz * kadim(p, P::N));
+        const T kz = wavenum<T>(g.dkz, g.fdkz, kadim(p, P::N));
         x = mk<C>(-kz * x.y, kz * x.x);
       }
       if (PH)
         x = cmul(x, phase_factor<C, T>(T(g.sx), T(g.sy), T(g.sz), kx, ky,
-                                       T(g.dkz * kadim(p, P::N))));
+                                       wavenum<T>(g.dkz, g.fdkz, kadim(p, P::N))));
       v[r] = x;
     }
     run<+1, LOGN>(v, jt, true, acc, twz, 1);
@@ -504,7 +541,7 @@ kf3_inv_z(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 #pragma unroll
     for (int i = 0; i < 8; ++i) Wo[base + (jt + P::outm(i) * P::N8) * plane] = v[i];
     if (j == 1) {  // oz = i kx Ty - i ky Tx (+ f: the k = 0 mode of the column kx = ky = 0)
-      const T fz = (g.has_f && ix == 0 && iy == 0) ? T(g.f) : T(0);
+      const T fz = (g.has_f && ix == 0 && iy == 0) ? par<T>(g.f, g.ff) : T(0);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const C h = hold[i * TH + threadIdx.x];  // Ty
@@ -763,9 +800,9 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
     } else {
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const T kj = f == 3 ? T(g.dkx * ix)
-                            : (f == 4 ? T(g.dky * kadim(iy, g.ny))
-                                      : T(g.dkz * kadim(jt + P::outm(i) * N8, N)));
+        const T kj = f == 3 ? wavenum<T>(g.dkx, g.fdkx, ix)
+                            : (f == 4 ? wavenum<T>(g.dky, g.fdky, kadim(iy, g.ny))
+                                      : wavenum<T>(g.dkz, g.fdkz, kadim(jt + P::outm(i) * N8, N)));
         const C t = mk<C>(-kj * v[i].y, kj * v[i].x);
         dv[i] = f == 3 ? t : cadd(dv[i], t);
       }
@@ -778,7 +815,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
   __syncthreads();
   if (!valid) return;
   const int kyi = kadim(iy, g.ny);
-  const T kx = T(g.dkx * ix), ky = T(g.dky * kyi);
+  const T kx = wavenum<T>(g.dkx, g.fdkx, ix), ky = wavenum<T>(g.dky, g.fdky, kyi);
   const T inv_n = T(g.inv_n);
   const Phys q = phys_of(g);
   if constexpr (!ST && !EXT) {
@@ -814,7 +851,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
         const bool rm = (ix >= g.kcx) || (iabs(kyi) >= g.kcy) || (iabs(kzi) >= g.kcz);
         if (g.pr && rm) continue;  // stays zero in S, tmp and tmp1
         const int64_t i = base + iz * plane;
-        const T kz = T(g.dkz * kzi);
+        const T kz = wavenum<T>(g.dkz, g.fdkz, kzi);
         C N3[3];
 #pragma unroll
         for (int ff = 0; ff < 3; ++ff) N3[ff] = cscale(buf[ff * N * TX + swz<C>(iz * TX + c)], inv_n);
@@ -837,7 +874,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
     const bool rm = (ix >= g.kcx) || (iabs(kyi) >= g.kcy) || (iabs(kzi) >= g.kcz);
     if (g.pr && rm) continue;  // stays zero in S, tmp and tmp1
     const int64_t i = base + iz * plane;
-    const T kz = T(g.dkz * kzi);
+    const T kz = wavenum<T>(g.dkz, g.fdkz, kzi);
     constexpr int NV = ST ? 4 : 3;
     C N3[NV];
 #pragma unroll
@@ -846,7 +883,7 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
       const C* in = static_cast<const C*>(a.in);
       const C vz = in[i + 2 * nK], b = in[i + 3 * nK];
       N3[2] = cadd(N3[2], b);
-      const T n2 = T(g.N2);
+      const T n2 = par<T>(g.N2, g.fN2);
       N3[NV - 1] = mk<C>(-N3[NV - 1].x - n2 * vz.x, -N3[NV - 1].y - n2 * vz.y);
     }
     if (a.add) {
@@ -879,7 +916,7 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
   const int64_t nK = (int64_t)g.ny * g.nkx;
   S += bid.z * nK;  // run of a batched ensemble
   W += bid.z * 4 * nK;
-  const T kx = T(g.dkx * ix);
+  const T kx = wavenum<T>(g.dkx, g.fdkx, ix);
   const SwzView<C, TX> acc{buf, c};
   // ns2d.strat: two more fields, d_x b and d_y b (b: the second state field)
 #pragma unroll 1
@@ -893,7 +930,7 @@ __device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
       if (valid && (!g.pr || kept(p, P::N, g.kcy))) {
         C w = Sf[(int64_t)p * g.nkx + ix];
         const int kyi = kadim(p, P::N);
-        const T ky = T(g.dky * kyi);
+        const T ky = wavenum<T>(g.dky, g.fdky, kyi);
         if (PH) w = cmul(w, phase_factor<C, T>(T(g.sx), T(g.sy), T(0), kx, ky, T(0)));
         T cc;
         if (f == 0 || f == 1) {
@@ -972,7 +1009,7 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   for (int i = 0; i < 8; ++i) acc.at(acc.base(jt), P::outm(i) * M8) = v[i];
   __syncthreads();
   T mx = 0, my = 0;
-  const T beta = T(g.beta);
+  const T beta = par<T>(g.beta, g.fbeta);
   for (int idx = threadIdx.x; idx < L * M; idx += blockDim.x) {
     const int ll = idx / M, j = idx % M;
     C* p0 = buf + ll * LS + padp<LOGM, C>(j);
@@ -985,7 +1022,7 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
     p0[0] = res;
     if (ST) {
       const C pxb = p0[4 * L * LS], pyb = p0[5 * L * LS];
-      const T n2 = T(g.N2);
+      const T n2 = par<T>(g.N2, g.fN2);
       p0[L * LS] = mk<C>(-ux.x * pxb.x - uy.x * pyb.x - n2 * uy.x,
                          -ux.y * pxb.y - uy.y * pyb.y - n2 * uy.y);
     }
@@ -1058,6 +1095,9 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
       a.dt = pr.dt[bid.z];
       g.nu2 = pr.nu2[bid.z];
       g.nu8 = pr.nu8[bid.z];
+      a.fdt = (float)a.dt;
+      g.fnu2 = (float)g.nu2;
+      g.fnu8 = (float)g.nu8;
     }
   }
   C v[8];
@@ -1067,7 +1107,7 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
   const SwzView<C, TX> acc{buf, c};
   run<-1, LOGN>(v, jt, true, acc, twy, 1);
   if (!valid) return;
-  const T kx = T(g.dkx * ix);
+  const T kx = wavenum<T>(g.dkx, g.fdkx, ix);
   const T inv_n = T(g.inv_n);
   const Phys q = phys_of(g);
 #pragma unroll
@@ -1076,7 +1116,7 @@ __device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Ge
     const int kyi = kadim(iy, P::N);
     const bool rm = ix >= g.kcx || iabs(kyi) >= g.kcy;
     if (g.pr && rm) continue;
-    const T ky = T(g.dky * kyi);
+    const T ky = wavenum<T>(g.dky, g.fdky, kyi);
     const int64_t idx = (int64_t)iy * g.nkx + ix;
     C Nv = cscale(v[i], inv_n);
     if (bin) {

@@ -59,6 +59,11 @@ __device__ __forceinline__ Phys phys(const NSK& q) {
   p.nu8 = q.nu8;
   p.num4 = q.num4;
   p.k2_hypo0 = q.k2_hypo0;
+  p.fnu2 = (float)q.nu2;
+  p.fnu4 = (float)q.nu4;
+  p.fnu8 = (float)q.nu8;
+  p.fnum4 = (float)q.num4;
+  p.fk2_hypo0 = (float)q.k2_hypo0;
   p.proj = q.proj;
   p.no_vz_kz0 = q.no_vz_kz0;
   return p;
@@ -839,6 +844,7 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
       *dt = cfl_rule(*dt, cfl_tmp(s, s->hbuf), cfl[0], cfl[1]);
     }
     a.dt = *dt;
+    a.fdt = (float)*dt;
     rc = turb_stage<T>(s, in, a, st);
     if (rc) return rc;
     rc = finish<T>(s, m, a, st, pr);
@@ -1185,6 +1191,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
     g.has_f = q.has_f;
     g.strat = p.strat ? 1 : 0;
     g.N2 = p.bouss ? 0.0 : p.N * p.N;
+    gbs::fast::geo_f32(g);
   }
   if (!rc) {
     // tmp / tmp1 start at zero so that modes never written stay zero

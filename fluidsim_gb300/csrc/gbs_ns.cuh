@@ -58,6 +58,7 @@ struct RKArgs {
   void* tmp1;     // _state_spect_tmp1
   void* tend;     // output for kTend
   double dt;
+  float fdt;  // dt rounded to float (the FP32 kernels read this one)
   int* nan_flag;
   const void* add;  // optional forcing (nvar spectral fields) added to the
                     // tendency before projection and dealiasing
@@ -71,13 +72,36 @@ struct RKArgs {
 struct Phys {
   double nu2, nu4, nu8, num4;
   double k2_hypo0;  // K2 at (0, .., 1): the value f_d_hypo[0, .., 0] copies
+  float fnu2, fnu4, fnu8, fnum4, fk2_hypo0;  // the same rounded to float
   int proj;         // ns3d projection: GBS_PROJ_PERPK / _TOROIDAL / _POLOIDAL
   int no_vz_kz0;    // ns3d: vz(kz = 0) = 0 after the projection
 };
 
+// FP32 kernels read float copies of the double parameters made on the host
+// (or once per thread), so that no FP64 instruction runs per mode: GB300
+// executes FP64 at 2 operations per clock per SM against 128 for FP32.
+template <typename T>
+__device__ __forceinline__ T dt_of(const RKArgs& a) {
+  if constexpr (sizeof(T) == 8) return a.dt;
+  else return a.fdt;
+}
+
 // fluidsim/base/solvers/pseudo_spect.py:166-191
 template <typename T>
 __device__ __forceinline__ T freq_lin(const Phys& q, T k2, bool k0) {
+  if constexpr (sizeof(T) == 4) {  // the same operations on the float copies
+    float fd = q.fnu2 > 0.f ? q.fnu2 * k2 : 0.f;
+    if (q.fnu4 > 0.f) fd += q.fnu4 * (k2 * k2);
+    if (q.fnu8 > 0.f) {
+      const float k4 = k2 * k2;
+      fd += q.fnu8 * (k4 * k4);
+    }
+    if (q.fnum4 != 0.f) {
+      const float k2n0 = k0 ? q.fk2_hypo0 : k2;
+      fd += q.fnum4 / (k2n0 * k2n0);
+    }
+    return fd;
+  }
   T fd = q.nu2 > 0 ? T(q.nu2) * k2 : T(0);
   if (q.nu4 > 0) fd += T(q.nu4) * (k2 * k2);
   if (q.nu8 > 0) {
@@ -104,7 +128,7 @@ __device__ __forceinline__ float dexp(float x) { return expf(x); }
 // kernels instantiate an RK4-only variant, which keeps their epilogue lean).
 template <typename C, typename T, bool EXT>
 __device__ __forceinline__ C final_value(int mode, const RKArgs& a, int64_t i, C N, T sigma) {
-  const T dt = T(a.dt);
+  const T dt = dt_of<T>(a);
   if (!EXT || mode == kRK3) {
     const C t = static_cast<const C*>(a.tmp)[i];
     const T c6 = dt / T(6);
@@ -164,7 +188,7 @@ __device__ __forceinline__ void rk4_stage_values(int mode, T dt, T sigma, C N, C
 template <typename C, typename T, bool EXT>
 __device__ __forceinline__ void rk_update(int mode, const RKArgs& a, int64_t i,
                                          C N, T sigma) {
-  const T dt = T(a.dt);
+  const T dt = dt_of<T>(a);
   C* tmp = static_cast<C*>(a.tmp);
   C* tmp1 = static_cast<C*>(a.tmp1);
   if (!EXT && mode > kRK2) return;
@@ -300,7 +324,7 @@ __device__ __forceinline__ void stage_epilogue_rk4(int mode, const RKArgs& a, in
 #pragma unroll
     for (int f = 0; f < NV; ++f) o[i + f * nK] = N[f];
   } else if (mode == kRK3) {
-    const T c6 = T(a.dt) / T(6);
+    const T c6 = dt_of<T>(a) / T(6);
     C Sn[NV];
 #pragma unroll
     for (int f = 0; f < NV; ++f) Sn[f] = mk<C>(T0[f].x + c6 * N[f].x, T0[f].y + c6 * N[f].y);
@@ -317,7 +341,7 @@ __device__ __forceinline__ void stage_epilogue_rk4(int mode, const RKArgs& a, in
 #pragma unroll
     for (int f = 0; f < NV; ++f) {
       C o, o1;
-      rk4_stage_values<C, T>(mode, T(a.dt), sig, N[f], S0[f], T0[f], o, o1);
+      rk4_stage_values<C, T>(mode, dt_of<T>(a), sig, N[f], S0[f], T0[f], o, o1);
       tmp[i + f * nK] = o;
       tmp1[i + f * nK] = o1;
     }
@@ -340,7 +364,7 @@ __device__ __forceinline__ void stage_epilogue3(int mode, const RKArgs& a, int64
       for (int f = 0; f < NV; ++f) o[i + f * nK] = N[f];
     } else if (mode == kRK3) {
       const C* tmp = static_cast<const C*>(a.tmp);
-      const T c6 = T(a.dt) / T(6);
+      const T c6 = dt_of<T>(a) / T(6);
       C Sn[NV];
 #pragma unroll
       for (int f = 0; f < NV; ++f) {
