@@ -158,11 +158,11 @@ kmix_x(const __grid_constant__ MixArgs m) {
   float2* F = static_cast<float2*>(G.F);
   const float2* tw = static_cast<const float2*>(G.twx);
   switch (G.logm) {
-    case 5: kf2_x_body<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
-    case 6: kf2_x_body<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
-    case 7: kf2_x_body<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
-    case 8: kf2_x_body<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
-    default: kf2_x_body<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 5: kf2_x_any<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 6: kf2_x_any<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 7: kf2_x_any<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
+    case 8: kf2_x_any<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
+    default: kf2_x_any<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
   }
 }
 

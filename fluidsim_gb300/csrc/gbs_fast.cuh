@@ -1059,11 +1059,120 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
   }
 }
 
+// B with rows in pairs (as kf3_xp): rows 2 q, 2 q + 1 of a field are the
+// real and imaginary parts of one N = nx point complex line; LP pairs per
+// CTA, N/8 threads per line, the same threads and shared memory as
+// kf2_x_body with L = 2 LP rows.
+template <typename T, int LOGN, int LP, bool ST = false>
+__device__ __forceinline__ void kf2_xp_body(const cplx<T>* __restrict__ W,
+                                            cplx<T>* __restrict__ F, const Geo& g,
+                                            const cplx<T>* __restrict__ twx,
+                                            unsigned long long* vmax, uint3 bid) {
+  constexpr int NF = ST ? 6 : 4, NFO = ST ? 2 : 1;
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  constexpr int N = P::N, N8 = P::N8, H = N / 2;
+  constexpr bool WARP = N8 <= 32;
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % N8;
+  const int lp = (threadIdx.x / N8) % LP;
+  const int f = threadIdx.x / (N8 * LP);
+  const int64_t nrows = g.ny;
+  const int64_t nK = nrows * g.nkx;
+  const int64_t row0 = ((int64_t)bid.x * LP + lp) * 2;
+  const bool v0 = row0 < nrows, v1 = row0 + 1 < nrows;
+  W += bid.y * 4 * nK;  // run of a batched ensemble
+  F += bid.y * nK;
+  const SwzView<C, 1> acc{buf + (f * LP + lp) * N, 0};
+  const int kcx = g.pr ? g.kcx : g.nkx + 1;
+  C v[8];
+  {
+    const C* r0 = W + f * nK + row0 * g.nkx;
+    const C* r1 = r0 + g.nkx;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int idx = r < 4 ? jt + r * N8 : (8 - r) * N8 - jt;
+      const bool in = idx < kcx;
+      C a0 = (v0 && in) ? r0[idx] : mk<C>(0, 0);
+      C a1 = (v1 && in) ? r1[idx] : mk<C>(0, 0);
+      if ((r == 0 || r == 4) && jt == 0) { a0.y = 0; a1.y = 0; }
+      v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
+    }
+  }
+  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1);
+  const int sj = acc.base(jt);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+  __syncthreads();
+  T mx = 0, my = 0;
+  const T beta = par<T>(g.beta, g.fbeta);
+  const int64_t npairs = (nrows + 1) / 2;
+  for (int idx = threadIdx.x; idx < LP * N; idx += blockDim.x) {
+    const int ll = idx / N, j = idx % N;
+    C* p0 = buf + ll * N + swz<C>(j);
+    const C ux = p0[0], uy = p0[LP * N], px = p0[2 * LP * N], py = p0[3 * LP * N];
+    C res;
+    if (ST || g.beta == 0)  // (ns2d.strat has no beta term)
+      res = mk<C>(-ux.x * px.x - uy.x * py.x, -ux.y * px.y - uy.y * py.y);
+    else
+      res = mk<C>(-ux.x * px.x - uy.x * (py.x + beta), -ux.y * px.y - uy.y * (py.y + beta));
+    p0[0] = res;
+    if (ST) {
+      const C pxb = p0[4 * LP * N], pyb = p0[5 * LP * N];
+      const T n2 = par<T>(g.N2, g.fN2);
+      p0[LP * N] = mk<C>(-ux.x * pxb.x - uy.x * pyb.x - n2 * uy.x,
+                         -ux.y * pxb.y - uy.y * pyb.y - n2 * uy.y);
+    }
+    if (vmax && (int64_t)bid.x * LP + ll < npairs) {
+      mx = fmax(mx, fmax(fabs(ux.x), fabs(ux.y)));
+      my = fmax(my, fmax(fabs(uy.x), fabs(uy.y)));
+    }
+  }
+  __syncthreads();
+  if (vmax) block_max3(mx, my, T(0), vmax);
+  const bool act = f < NFO;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
+  // the line's first exchange overwrites positions other threads still read
+  if (WARP) __syncwarp(); else __syncthreads();
+  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1);
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+  }
+  __syncthreads();
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  const T h = T(0.5);
+  for (int idx = threadIdx.x; idx < NFO * LP * nout; idx += blockDim.x) {
+    const int k = idx % nout, ll = (idx / nout) % LP, fo = idx / (nout * LP);
+    const int64_t r0 = ((int64_t)bid.x * LP + ll) * 2;
+    if (r0 >= nrows) continue;
+    const C* sl = buf + (fo * LP + ll) * N;
+    const C z = sl[swz<C>(k)];
+    const C m = sl[swz<C>((N - k) & (N - 1))];
+    C* Fo = F + fo * nK + r0 * g.nkx + k;
+    Fo[0] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
+    if (r0 + 1 < nrows) Fo[g.nkx] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
+  }
+}
+
+// The ns2d x pass for L rows per CTA: in pairs when L is even (FP32).
+template <typename T, int LOGM, int L, bool ST = false>
+__device__ __forceinline__ void kf2_x_any(const cplx<T>* __restrict__ W,
+                                          cplx<T>* __restrict__ F, const Geo& g,
+                                          const cplx<T>* __restrict__ twx,
+                                          unsigned long long* vmax, uint3 bid) {
+  if constexpr (sizeof(T) == 4 && L % 2 == 0)
+    kf2_xp_body<T, LOGM + 1, L / 2, ST>(W, F, g, twx, vmax, bid);
+  else
+    kf2_x_body<T, LOGM, L, ST>(W, F, g, twx, vmax, bid);
+}
+
 template <typename T, int LOGM, int L, bool ST = false>
 __global__ void __launch_bounds__((ST ? 6 : 4) * L * (1 << LOGM) / 8, 2)
 kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
-  kf2_x_body<T, LOGM, L, ST>(W, F, g, twx, vmax, blockIdx);
+  kf2_x_any<T, LOGM, L, ST>(W, F, g, twx, vmax, blockIdx);
 }
 
 // C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
