@@ -188,15 +188,26 @@ __device__ __forceinline__ void stage_twiddles(const C* __restrict__ tw, int k, 
   }
 }
 
+// Barrier over the threads that share a line's slot: the warp (WARP: lines
+// inside one warp), the named barrier `bar` > 0 of the line's NT threads
+// (whole, contiguous warps: lines do not wait for each other), or the CTA.
+template <bool WARP, int NT>
+__device__ __forceinline__ void line_sync(int bar) {
+  if (WARP) __syncwarp();
+  else if (bar > 0) asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(NT) : "memory");
+  else __syncthreads();
+}
+
 // Stockham FFT of one line whose stage-0 inputs v[r] = x[jt + r N/8] are in
 // registers; `acc(p)` addresses position p of this line in shared memory.
-// Every thread of the CTA must call it (it contains barriers); `active`
-// threads compute, the others only take part in the barriers.
-// WARP: every line lies inside one warp (rows with N/8 <= 32 threads and
-// the line index above jt), so the exchanges only need __syncwarp().
+// Every thread that shares its barriers must call it; `active` threads
+// compute, the others only take part in the barriers.  Barriers: the CTA's
+// (bar = 0), or per line (WARP: every line lies inside one warp, rows with
+// N/8 <= 32 threads and the line index above jt; bar > 0: the named barrier
+// of the line's N/8 threads), and then only the line's threads call it.
 template <int DIR, int LOGN, bool WARP = false, typename C, typename Acc>
 __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& acc,
-                                    const C* __restrict__ tw, int tws) {
+                                    const C* __restrict__ tw, int tws, int bar = 0) {
   using P = Line<LOGN>;
   constexpr int N = P::N, N8 = P::N8;
   if (active) dft8<DIR>(v);
@@ -210,7 +221,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& a
 #pragma unroll
       for (int r = 0; r < 8; ++r) acc.at(sd, r * Ns) = v[r];
     }
-    if (WARP) __syncwarp(); else __syncthreads();
+    line_sync<WARP, N8>(bar);
     const int Nsn = Ns << 3;
     if (active) {
       if (s < P::S8) {
@@ -244,7 +255,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& a
         }
       }
     }
-    if (WARP) __syncwarp(); else __syncthreads();
+    line_sync<WARP, N8>(bar);
   }
 }
 
@@ -704,25 +715,30 @@ kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
     }
   }
-  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1);
+  // lines of two or more warps synchronise on their own named barrier
+  const int bar = WARP ? 0 : 1 + f * LP + lp;
+  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1, bar);
   const int sj = acc.base(jt);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
   __syncthreads();
   x_products<T, LP, N, ST>(buf, (nrows + 1) / 2, vmax);
+  // from here on each product line is read and written by its own threads;
+  // idle lines leave unless they share a warp's barriers with a product line
   const bool act = f < (ST ? 6 : 3);
+  if (!act && !WARP) return;
 #pragma unroll
   for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
   // the line's first exchange overwrites positions other threads still read
-  if (WARP) __syncwarp(); else __syncthreads();
-  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1);
+  line_sync<WARP, N8>(bar);
+  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1, bar);
   if (act) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
   }
-  __syncthreads();
-  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  line_sync<WARP, N8>(bar);
   if (!act) return;
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
   C* F0 = F + f * nK + row0 * g.nkx;
   C* F1 = F0 + g.nkx;
   const T h = T(0.5);
@@ -1099,7 +1115,8 @@ __device__ __forceinline__ void kf2_xp_body(const cplx<T>* __restrict__ W,
       v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
     }
   }
-  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1);
+  const int bar = WARP ? 0 : 1 + f * LP + lp;  // as in kf3_xp
+  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1, bar);
   const int sj = acc.base(jt);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
@@ -1130,15 +1147,18 @@ __device__ __forceinline__ void kf2_xp_body(const cplx<T>* __restrict__ W,
   }
   __syncthreads();
   if (vmax) block_max3(mx, my, T(0), vmax);
+  // product lines; idle lines skip this unless they share a warp's barriers
   const bool act = f < NFO;
+  if (act || WARP) {
 #pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
-  // the line's first exchange overwrites positions other threads still read
-  if (WARP) __syncwarp(); else __syncthreads();
-  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1);
-  if (act) {
+    for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
+    // the line's first exchange overwrites positions other threads still read
+    line_sync<WARP, N8>(bar);
+    run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1, bar);
+    if (act) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+      for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
+    }
   }
   __syncthreads();
   const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
