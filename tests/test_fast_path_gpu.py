@@ -90,6 +90,16 @@ def test_ns3d_fast_fp32_nx512_error(cuda):
     assert abs(sim.time_stepping.deltat - orc.deltat) <= 1e-5 * orc.deltat
 
 
+def test_ns3d_fast_fp32_nx1024_error(cuda):
+    """nx = 1024 in FP32: rows in pairs on 1024-point lines of four warps
+    (named barriers of 128 threads), CFL maxima included."""
+    sim, orc = run_3d((32, 32, 1024), "float32", 4, USE_CFL=True, cfl_coef=0.5,
+                      L=(2 * pi,) * 3)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
+    assert abs(sim.time_stepping.deltat - orc.deltat) <= 1e-5 * orc.deltat
+
+
 def test_ns3d_strat_fast_fp32_nx512_error(cuda):
     """ns3d.strat with nx = 512 in FP32 (the 7-field 16 x 16 x pass)."""
     import torch
@@ -167,6 +177,39 @@ def test_ns2d_fast_fp64_matches_oracle(cuda, shape, beta, cfl, scheme):
     orc.init_from_rotfft(rot)
     orc.run(it_end=5)
     assert rel(sim.state.state_spect.cpu().numpy(), orc.state_spect) < 1e-12
+
+
+@pytest.mark.parametrize("shape,beta,cfl", [
+    ((64, 256), 2.0, True),     # 6 rows per CTA: 3 pairs of 256-point lines
+    ((128, 512), 0.0, False),   # 3 rows per CTA: half-length real transforms
+    ((32, 1024), 1.0, True),    # 1 row per CTA
+    ((64, 64), 0.5, True)])     # 24 rows per CTA: 12 pairs of 64-point lines
+def test_ns2d_fast_fp32_matches_oracle(cuda, shape, beta, cfl):
+    """The ns2d FP32 x pass with and without rows in pairs."""
+    from fluidsim_gb300.init_fields import noise_rot_2d
+    from fluidsim_gb300.solvers import SimulNS2D
+    from oracle.solvers import NS2DOracle
+    from oracle.spectral import OperNumpy2D
+    ny, nx = shape
+    L = (2 * pi, 2 * pi * ny / nx)
+    p = SimulNS2D.create_default_params()
+    p.precision = "float32"
+    p.oper.nx, p.oper.ny = nx, ny
+    p.oper.Lx, p.oper.Ly = L
+    p.nu_2, p.beta = 1e-3, beta
+    ts = p.time_stepping
+    ts.USE_CFL, ts.cfl_coef, ts.deltat0 = cfl, 0.5, 2e-3
+    ts.USE_T_END, ts.it_end = False, 5
+    sim = SimulNS2D(p)
+    rot = noise_rot_2d(nx, ny, *L, kmin=3, kmax=10, seed=6)
+    sim.init_from_rotfft(rot)
+    sim.time_stepping.start()
+    orc = NS2DOracle(OperNumpy2D(nx, ny, *L), beta=beta, nu_2=1e-3, USE_CFL=cfl,
+                     cfl_coef=0.5, deltat0=2e-3)
+    orc.init_from_rotfft(rot)
+    orc.run(it_end=5)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
 
 
 @pytest.mark.parametrize("precision,shape", [("float32", (64, 64, 64)),
