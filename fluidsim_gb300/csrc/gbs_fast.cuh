@@ -282,12 +282,20 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
   const bool valid = col < a.ncols;
   const int64_t base = blockIdx.z * a.fs + blockIdx.y * a.os + col;
   int bx, by, bz;
-  if ((c == 0 || c == TX - 1) && cta_ahead(a.pf, bx, by, bz) && bx * TX + c < a.ncols) {
-    const int64_t bp = bz * a.fs + by * a.os + bx * TX + c;
+  if (cta_ahead(a.pf, bx, by, bz)) {
+    // the TX lanes of each jt share its 8 rows: lane c fetches rows c, c + TX,
+    // .., both ends of the row's segment of the tile (a segment may straddle
+    // two 128-byte lines); the first column of a CTA in the grid is valid
+    const int64_t bp = bz * a.fs + by * a.os + bx * TX;
+    const int last = (a.ncols - bx * TX < TX ? a.ncols - bx * TX : TX) - 1;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = c; r < 8; r += TX) {
       const int p = jt + r * P::N8;
-      if (kept(p, P::N, a.kc_in)) prefetch_l2(in + bp + p * a.es);
+      if (kept(p, P::N, a.kc_in)) {
+        const cplx<T>* q = in + bp + p * a.es;
+        prefetch_l2(q);
+        prefetch_l2(q + last);
+      }
     }
   }
   C v[8];
