@@ -991,21 +991,21 @@ static int64_t spectrum_bins(const Solver* s) {
   return (int64_t)floor(kmax / dk + 0.5) + 1;
 }
 
-// flag = 1 if a removed mode of any field is not +0 (bitwise)
+// flag = 1 if a removed mode of any field is not +0 (bitwise).  One CTA per
+// kx row (iy, iz): a row whose ky or kz is cut is removed whole, the others
+// from kx = kcut_x on; no index division.
 template <typename T>
 __global__ void k_removed_nonzero(const cplx<T>* __restrict__ S, NSK q, int nvar,
                                   int* __restrict__ flag) {
+  const int iz = blockIdx.x, iy = blockIdx.y;  // nz on x: it may exceed 65535
   const int64_t nK = (int64_t)q.nz * q.ny * q.nkx;
+  const int kz = q.nz > 1 ? kadim(iz, q.nz) : 0;
+  const int ix0 = removed(q, 0, kadim(iy, q.ny), kz) ? 0 : q.kcx;
+  const cplx<T>* row = S + ((int64_t)iz * q.ny + iy) * q.nkx;
   bool nz = false;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nK;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int ix = (int)(i % q.nkx);
-    const int64_t r = i / q.nkx;
-    const int iy = (int)(r % q.ny), iz = (int)(r / q.ny);
-    const int kz = q.nz > 1 ? kadim(iz, q.nz) : 0;
-    if (!removed(q, ix, kadim(iy, q.ny), kz)) continue;
+  for (int ix = ix0 + threadIdx.x; ix < q.nkx; ix += blockDim.x) {
     for (int f = 0; f < nvar; ++f) {
-      const cplx<T> v = S[i + f * nK];
+      const cplx<T> v = row[ix + f * nK];
       nz = nz || v.x != T(0) || v.y != T(0) || signbit(v.x) || signbit(v.y);
     }
   }
@@ -1418,10 +1418,10 @@ int gbs_ns_is_dealiased(gbs_ns* h, const void* S, int* out, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   GBS_CUDA_TRY(cudaMemsetAsync(s->dflag, 0, sizeof(int), st));
   if (s->p.dtype == GBS_F64)
-    gbs::k_removed_nonzero<double><<<gbs::kRedBlocks * 4, gbs::kRedThreads, 0, st>>>(
+    gbs::k_removed_nonzero<double><<<dim3(s->q.nz, s->q.ny), 128, 0, st>>>(
         static_cast<const double2*>(S), s->q, s->nvar, s->dflag);
   else
-    gbs::k_removed_nonzero<float><<<gbs::kRedBlocks * 4, gbs::kRedThreads, 0, st>>>(
+    gbs::k_removed_nonzero<float><<<dim3(s->q.nz, s->q.ny), 128, 0, st>>>(
         static_cast<const float2*>(S), s->q, s->nvar, s->dflag);
   GBS_CHECK_LAUNCH();
   ++s->launches;
