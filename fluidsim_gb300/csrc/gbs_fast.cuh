@@ -205,16 +205,24 @@ __device__ __forceinline__ void line_sync(int bar) {
 // (bar = 0), or per line (WARP: every line lies inside one warp, rows with
 // N/8 <= 32 threads and the line index above jt; bar > 0: the named barrier
 // of the line's N/8 threads), and then only the line's threads call it.
-template <int DIR, int LOGN, bool WARP = false, typename C, typename Acc>
-__device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& acc,
+// ALT > 0: the exchanges alternate between the slot and the one ALT
+// elements after it, so an exchange needs one barrier (between its writes
+// and its reads; the next exchange writes the other slot, and the one
+// after it comes after the next barrier); the caller must then not reuse
+// either slot before a barrier of its own.
+template <int DIR, int LOGN, bool WARP = false, int ALT = 0, typename C, typename Acc>
+__device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& acc_a,
                                     const C* __restrict__ tw, int tws, int bar = 0) {
   using P = Line<LOGN>;
   constexpr int N = P::N, N8 = P::N8;
+  Acc acc_b = acc_a;
+  acc_b.buf += ALT;
   if (active) dft8<DIR>(v);
   // every exchange position below is (per-thread part) | (constant part)
-  const int sj = acc.base(jt);
+  const int sj = acc_a.base(jt);
 #pragma unroll
   for (int s = 1; s < P::NST; ++s) {
+    const Acc& acc = (ALT > 0 && (s & 1) == 0) ? acc_b : acc_a;
     const int Ns = 1 << (3 * (s - 1));  // radix-8 stage s-1 wrote with this Ns
     if (active) {
       const int sd = acc.base(((jt / Ns) * Ns << 3) + (jt % Ns));
@@ -255,7 +263,7 @@ __device__ __forceinline__ void run(C (&v)[8], int jt, bool active, const Acc& a
         }
       }
     }
-    line_sync<WARP, N8>(bar);
+    if (ALT == 0) line_sync<WARP, N8>(bar);
   }
 }
 
@@ -305,7 +313,7 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
     v[r] = (valid && kept(p, P::N, a.kc_in)) ? in[base + p * a.es] : mk<C>(0, 0);
   }
   const SwzView<C, TX> acc{buf, c};
-  run<DIR, LOGN>(v, jt, true, acc, tw, 1);
+  run<DIR, LOGN, false, P::N * TX>(v, jt, true, acc, tw, 1);  // two exchange slots
   if (!valid) return;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {

@@ -94,7 +94,7 @@ static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, i
   using C = cplx<T>;
   constexpr int TX = tx_cols<T, LOGN>();
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = sizeof(C) * (size_t)(1 << LOGN) * TX;
+  const size_t smem = 2 * sizeof(C) * (size_t)(1 << LOGN) * TX;  // two exchange slots
   int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
   if (rc) return rc;
   static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR>, TH, smem);
