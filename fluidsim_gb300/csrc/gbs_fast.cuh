@@ -687,6 +687,11 @@ kf3_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
 }
 
+// Paired x passes with three-stage lines (N = 128 .. 512) give each line a
+// second exchange slot (after all first slots).
+template <int LOGN>
+__host__ __device__ constexpr bool xp_alt() { return Line<LOGN>::NST == 3; }
+
 // B, rows in pairs: rows 2 q and 2 q + 1 of a field travel as the real and
 // imaginary parts of one complex line of N = nx points.  With A0, A1 their
 // spectra extended by Hermitian symmetry (imaginary parts of k = 0 and
@@ -731,9 +736,12 @@ kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
       v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
     }
   }
-  // lines of two or more warps synchronise on their own named barrier
+  // lines of two or more warps synchronise on their own named barrier; with
+  // three stages the two exchanges use the line's slot and a second one
+  // (ALT), and the last one (in the second slot) leaves the first free
   const int bar = WARP ? 0 : 1 + f * LP + lp;
-  run<+1, LOGN, WARP>(v, jt, true, acc, twx, 1, bar);
+  constexpr int ALT = xp_alt<LOGN>() ? (ST ? 7 : 6) * LP * N : 0;
+  run<+1, LOGN, WARP, ALT>(v, jt, true, acc, twx, 1, bar);
   const int sj = acc.base(jt);
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];
@@ -747,7 +755,7 @@ kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   for (int r = 0; r < 8; ++r) v[r] = act ? acc.at(sj, r * N8) : mk<C>(0, 0);
   // the line's first exchange overwrites positions other threads still read
   line_sync<WARP, N8>(bar);
-  run<-1, LOGN, WARP>(v, jt, act, acc, twx, 1, bar);
+  run<-1, LOGN, WARP, ALT>(v, jt, act, acc, twx, 1, bar);
   if (act) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc.at(sj, P::outm(i) * N8) = v[i];

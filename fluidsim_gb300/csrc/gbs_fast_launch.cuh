@@ -224,7 +224,7 @@ static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
   constexpr int NF = ST ? 7 : 6;
   constexpr int LP = GBS_X_THREADS / NF / N8 > 0 ? GBS_X_THREADS / NF / N8 : 1;
   constexpr int TH = NF * LP * N8;
-  const size_t smem = sizeof(C) * (size_t)NF * LP * N;
+  const size_t smem = sizeof(C) * (size_t)NF * LP * N * (xp_alt<LOGN>() ? 2 : 1);
   int rc = prep(kf3_xp<T, LOGN, LP, ST>, smem);
   if (rc) return rc;
   const int64_t npairs = ((int64_t)g.nz * g.ny + 1) / 2;
