@@ -12,9 +12,10 @@ so no explicit L2 flush is needed between steps.
 
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
 (the spec path has no data-path exchange); value = steps of all ranks
-divided by the slowest rank's time.  The reference arm times the CPU
-restatement of the reference algorithm (float64, scipy.fft on all host
-cores) on a bounded sample of the same workload.
+divided by the slowest rank's time.  The reference arm times whole RK4
+steps of the CPU restatement of the reference algorithm (float64, scipy.fft
+and slab-parallel numpy on all host cores) on the same workload, honouring
+--steps and --warmup.
 """
 
 import argparse
@@ -57,10 +58,34 @@ def fields_per_launch(nx, ny, nz, coef=2.0 / 3):
             "fwd_z_rk": 3 * fx * fy + rk_state * fx * fy * fz}
 
 
+def fp64_flops_per_step(nx, ny, nz, coef=2.0 / 3):
+    """Floating-point operations of the FFT butterflies of one pruned RK4
+    step (4 tendency evaluations), counting 5 n log2 n per complex n-point
+    line and 2.5 n log2 n per real line, over the lines each pass actually
+    transforms given the 2/3 truncation: per evaluation 5 inverse and 3
+    forward z transforms on the kept (kx, ky) columns, 6 inverse and 3
+    forward y transforms on the kept kx columns, 6 C2R and 3 R2C x rows."""
+    from math import log2
+    from fluidsim_gb300.init_fields import cubic_dealias_cutoff
+    kx = min(cubic_dealias_cutoff(nx, 2 * pi, coef), nx // 2 + 1)
+    ky = min(2 * cubic_dealias_cutoff(ny, 2 * pi, coef) - 1, ny)
+    z_lines, y_lines, x_lines = kx * ky, kx * nz, ny * nz
+    per_eval = ((5 + 3) * z_lines * 5 * nz * log2(nz)
+                + (6 + 3) * y_lines * 5 * ny * log2(ny)
+                + (6 + 3) * x_lines * 2.5 * nx * log2(nx))
+    return 4 * per_eval
+
+
+def fp64_peak_tflops(sm_mhz, sms=152):
+    """FP64 FMA peak: 2 FP64 FMA (4 flops) per clock per SM."""
+    return sms * 4 * sm_mhz * 1e6 / 1e12
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 100; 20 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=512)
@@ -101,6 +126,30 @@ def cfl_dt(vmax, n, cfl=0.5, dtmax=0.2):
     dx = 2 * pi / n
     tmp = sum(v / dx for v in vmax)
     return min(cfl / tmp, dtmax) if tmp > 0 else dtmax
+
+
+def initial_dt(v0, n):
+    """The workload's fixed dt: the CFL rule (coefficient 0.5) applied once
+    to the initial field, with max|v_i| taken in float64 on the host, so both
+    arms step with the same dt."""
+    import scipy.fft as sfft
+    nz, ny = v0.shape[1], v0.shape[2]
+    shape = (nz, ny, n)
+    vmax = []
+    for c in range(3):
+        x = sfft.irfftn(v0[c], s=shape, workers=os.cpu_count()) * (n * ny * nz)
+        vmax.append(float(max(abs(x.min()), abs(x.max()))))
+    return cfl_dt(vmax, n)
+
+
+def workload_config(n, ny, nz, dt, world):
+    size = f"{n}^3" if n == ny == nz else f"{n}x{ny}x{nz}"
+    return {"workload": f"ns3d decaying isotropic turbulence {size}", "nx": n,
+            "ny": ny, "nz": nz, "L": "2pi", "nu_2": 5e-4, "dt": dt,
+            "scheme": "RK4 exact integrating factor", "dealiasing": "2/3 cubic",
+            "initial": "seeded solenoidal random phases, E(k)~k^4 exp(-2(k/4)^2), E=0.5",
+            "l2_flush": "none needed: working set ~10 GB >> 129 MB L2",
+            "parallelism": f"replicas x{world}"}
 
 
 def make_sim(n, precision, v0):
@@ -215,44 +264,67 @@ def cpu_model():
     return platform.processor() or platform.machine()
 
 
-def cpu_sample(n, v0, reps=1):
-    """Oracle (float64, scipy.fft on all cores): one tendency evaluation."""
+def oracle_sim(n, v0, dt):
+    """The float64 CPU oracle set up on the workload (untimed)."""
     from oracle.solvers import NS3DOracle
-    from oracle.spectral import WORKERS, OperNumpy3D
-    orc = NS3DOracle(OperNumpy3D(n, n, n), nu_2=5e-4)
+    from oracle.spectral import OperNumpy3D
+    orc = NS3DOracle(OperNumpy3D(n, n, n), nu_2=5e-4, deltat0=dt, USE_CFL=False)
     orc.state_spect[:] = v0
-    S = orc.state_spect.copy()
-    small = NS3DOracle(OperNumpy3D(32, 32, 32))
-    small.tendencies_nonlin(small.state_spect.copy())  # warm the code paths
+    orc.statephys_from_statespect()
+    orc._coefs()  # exp(-dt sigma) tables, computed once per dt
+    return orc
+
+
+def cpu_sample(n, v0, dt, steps=1):
+    """Oracle (float64, scipy.fft and slab-parallel numpy on all host cores):
+    ``steps`` whole RK4 steps (4 tendency evaluations, the stage updates,
+    projection, dealiasing, the inverse transforms of the state, NaN check)."""
+    from oracle.spectral import WORKERS
+    orc = oracle_sim(n, v0, dt)
     t0 = time.perf_counter()
-    for _ in range(reps):
-        orc.tendencies_nonlin(S)
-    dt = (time.perf_counter() - t0) / reps
-    return {"value": 1.0 / (4 * dt), "unit": "steps/s", "cores": WORKERS, "kind": "port",
+    for _ in range(steps):
+        orc.one_time_step()
+    el = time.perf_counter() - t0
+    return {"value": steps / el, "unit": "steps/s", "cores": WORKERS, "kind": "port",
             "cpu_model": cpu_model(),
-            "sample": (f"{reps} tendencies_nonlin evaluation(s) of the float64 oracle at "
-                       f"{n}^3 (9 FFTs + curl, v x omega, projection, dealiasing), "
-                       f"{dt:.2f} s each, x4 for one RK4 step (elementwise RK updates "
-                       "not counted)")}
+            "sample": (f"{steps} whole RK4 step(s) of the float64 oracle at {n}^3 "
+                       f"(one_time_step: 4 tendency evaluations, stage updates, "
+                       f"projection, dealiasing, state_phys, NaN check), "
+                       f"{el / steps:.2f} s each")}
 
 
 def run_reference(args):
+    """Reference arm: the CPU restatement of the reference's algorithm,
+    whole RK4 steps on the same workload, ``--warmup`` untimed then exactly
+    ``--steps`` timed (the method of fluidsim/util/console/util.py:329-390:
+    fixed dt, it_end steps, outputs off)."""
     rank, _, world = dist_env()
     if rank != 0:
         return
+    from oracle.spectral import WORKERS
     n = args.n
+    steps = args.steps if args.steps is not None else 20
     v0 = initial_state(n)
-    reps = max(1, min(args.steps, 3))
-    base = cpu_sample(n, v0, reps=reps)
-    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "steps/s",
-            "n_gpus": args.gpus, "steps": reps, "warmup": 1,
-            "ms_per_step": 1000.0 / base["value"], "higher_is_better": True,
+    dt = initial_dt(v0, n)
+    orc = oracle_sim(n, v0, dt)
+    for _ in range(args.warmup):
+        orc.one_time_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.one_time_step()
+    el = time.perf_counter() - t0
+    value = steps / el
+    base = {"value": value, "unit": "steps/s", "cores": WORKERS, "kind": "port",
+            "cpu_model": cpu_model(),
+            "sample": (f"{steps} timed whole RK4 steps after {args.warmup} warm-up steps "
+                       f"of the float64 oracle at {n}^3, {el / steps:.2f} s each")}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * el / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"ns3d decaying isotropic turbulence {n}^3", "nx": n,
-                       "nu_2": 5e-4, "scheme": "RK4 exact integrating factor",
-                       "dealiasing": "2/3 cubic"},
+            "config": workload_config(n, n, n, dt, world),
             "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -339,20 +411,24 @@ def fft_throughput(n, reps=20):
     out = {"r2c_ms": r2c_ms, "c2r_ms": c2r_ms,
            "r2c_hbm_gbs": alg / r2c_ms / 1e6, "c2r_hbm_gbs": alg / c2r_ms / 1e6,
            "alg_bytes_per_transform": alg}
-    # comparison only: cuFFT through torch (not part of the product)
+    # comparison only: cuFFT through torch (not part of the product); both
+    # directions warmed up (plan creation) before either is timed
     for _ in range(3):
         torch.fft.rfftn(x)
+        torch.fft.irfftn(k, s=x.shape)
     torch.cuda.synchronize()
     ev[0].record()
     for _ in range(reps):
         torch.fft.rfftn(x)
     ev[1].record()
+    torch.cuda.synchronize()
+    ev[2].record()
     for _ in range(reps):
         torch.fft.irfftn(k, s=x.shape)
-    ev[2].record()
+    ev[3].record()
     torch.cuda.synchronize()
     out["cufft_compare"] = {"rfftn_ms": ev[0].elapsed_time(ev[1]) / reps,
-                            "irfftn_ms": ev[1].elapsed_time(ev[2]) / reps}
+                            "irfftn_ms": ev[2].elapsed_time(ev[3]) / reps}
     return out
 
 
@@ -374,9 +450,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     n = args.n
+    steps = args.steps if args.steps is not None else 100
     v0 = initial_state(n, args.ny, args.nz)
+    dt = initial_dt(v0, n)
     sim = make_sim(n, "float32", v0)
-    dt = cfl_dt(sim.max_velocity(), n)
     sim.time_stepping.deltat = dt
     lib = sim._lib
     ts = sim.time_stepping
@@ -393,7 +470,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
         start.record()
-        for _ in range(args.steps):
+        for _ in range(steps):
             ts.one_time_step()
         stop.record()
         torch.cuda.synchronize()
@@ -405,7 +482,7 @@ def main():
     launches = ctypes.c_int64()
     _lib.check(lib.gbs_ns_timing_report(sim._solver, ms, cnt, 5, ctypes.byref(launches)))
     _lib.check(lib.gbs_ns_timing(sim._solver, 0))
-    steps_per_s, elapsed_ms = replica_rate(elapsed_ms, args.steps, world, dist, "cuda")
+    steps_per_s, elapsed_ms = replica_rate(elapsed_ms, steps, world, dist, "cuda")
 
     # roofline of the dominant kernel (largest share of the timed region)
     field_bytes = v0.shape[1] * v0.shape[2] * (n // 2 + 1) * 8  # complex64
@@ -436,22 +513,18 @@ def main():
     host_in = torch.empty(S.shape, dtype=S.dtype, pin_memory=True)
     host_in.copy_(S)
     host_out = torch.empty_like(host_in, pin_memory=True)
-    e_steps = max(3, args.steps // 2)
+    e_steps = max(3, steps // 2)
     e2e_serial = e2e_run(ts, S, host_in, host_out, e_steps, world, dist, pipelined=False)
     e2e_run(ts, S, host_in, host_out, 2, world, dist, pipelined=True)  # warm-up
     e2e_rate = e2e_run(ts, S, host_in, host_out, e_steps, world, dist, pipelined=True)
     state_bytes = S.numel() * S.element_size()
 
     line = {"metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "steps": steps, "warmup": args.warmup,
+            "ms_per_step": elapsed_ms / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"ns3d decaying isotropic turbulence {n}^3", "nx": n,
-                       "ny": n, "nz": n, "L": "2pi", "nu_2": 5e-4, "dt": dt,
-                       "scheme": "RK4 exact integrating factor", "dealiasing": "2/3 cubic",
-                       "precision": "fp32 FFT/products, fp64 twiddles and reductions",
-                       "l2_flush": "none needed: working set ~10 GB >> 129 MB L2",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(n, v0.shape[2], v0.shape[1], dt, world),
+            "precision": "fp32 FFT/products, fp64 twiddles and reductions",
             "gpu_launches": int(launches.value - launches0.value),
             "roofline": roofline,
             "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
@@ -486,12 +559,21 @@ def main():
         torch.cuda.synchronize()
         fp64_rate = 9 / (f0.elapsed_time(f1) / 1000.0)
         s64 = sim64.state.state_spect.cpu().numpy()
-        line["fp64"] = {"steps_per_s": fp64_rate, "ms_per_step": 1000.0 / fp64_rate}
+        flops = fp64_flops_per_step(n, v0.shape[2], v0.shape[1])
+        sm_mhz = line["clocks"].get("sm_mhz") or 2070.0
+        peak64 = fp64_peak_tflops(sm_mhz)
+        line["fp64"] = {"steps_per_s": fp64_rate, "ms_per_step": 1000.0 / fp64_rate,
+                        "roofline": {"bound": "fp64", "flops_per_step": flops,
+                                     "achieved": flops * fp64_rate / 1e12, "unit": "TFLOP/s",
+                                     "peak": peak64, "frac": flops * fp64_rate / 1e12 / peak64,
+                                     "peak_source": (f"derived: 152 SMs x 2 FP64 FMA/clk x 2 "
+                                                     f"flops x {sm_mhz:.0f} MHz (median SM "
+                                                     "clock of the timed FP32 region)")}}
         line["fp32_over_fp64_speedup"] = steps_per_s / world / fp64_rate
         line["fp32_vs_fp64_rel_l2_10_steps"] = rel_l2(s32.astype(np.complex128), s64)
 
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(n, v0)
+        line["cpu_baseline"] = cpu_sample(n, v0, dt)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

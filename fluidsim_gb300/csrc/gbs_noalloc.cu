@@ -11,14 +11,28 @@
 // workspace in one file-scope device array of kScratchBytes (32 MiB), which
 // every GPU that loads the library holds until the process exits.
 //
-// The device address of that array is looked up once per device with
-// cudaGetSymbolAddress (the array's name in host code is only a host-side
-// stand-in, not a device address); the first call on a device does this
-// set-up, so that first call should come before any stream capture.  All
-// calls share the array and it keeps the contents of the last call, so calls
-// whose GPU work overlaps (two streams, or two threads) race on it.  Nothing
-// in the array has to start at zero: every call regenerates the twiddles and
-// the first pass writes the whole workspace before the next pass reads it.
+// The device address of that array is looked up with cudaGetSymbolAddress
+// (the array's name in host code is only a host-side stand-in, not a device
+// address) once per device and CUDA context: the first call on a device does
+// this set-up, so that first call should come before any stream capture.
+// The cache is keyed on the context's unique id, so a call made after
+// cudaDeviceReset (which rebuilds the primary context and the array) looks
+// the address up again instead of reusing a stale one.
+//
+// Under lazy module loading (CUDA_MODULE_LOADING=LAZY, the CUDA default)
+// the array itself is only allocated by that first look-up.  A caller whose
+// pool will later take all device memory must therefore make one call (any
+// small transform) on each device before the pool reserves its memory, or
+// run with CUDA_MODULE_LOADING=EAGER; after that, no call needs device
+// memory beyond what it was given.
+//
+// All calls share the array and it keeps the contents of the last call, so
+// calls whose GPU work overlaps (two streams, or two threads) race on it.
+// Nothing in the array has to start at zero: every call regenerates the
+// twiddles and the first pass writes the whole workspace before the next
+// pass reads it.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "gbs_internal.cuh"
@@ -41,9 +55,48 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 static std::mutex g_scratch_mu;
 static unsigned char* g_scratch_ptr[kMaxDevices];
+static unsigned long long g_scratch_ctx[kMaxDevices];  // context id of the entry
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current CUDA context (0 if none is
+// current yet), through driver entry points obtained from the runtime.
+static int current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    GBS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                  cudaEnableDefault, &q1));
+    GBS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                                  cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess ||
+        !f1 || !f2) {
+      set_error("gbs_fft_c2r_noalloc: driver entry points cuCtxGetCurrent / "
+                "cuCtxGetId unavailable");
+      return GBS_ECUDA;
+    }
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) {
+    set_error("gbs_fft_c2r_noalloc: cuCtxGetCurrent failed");
+    return GBS_ECUDA;
+  }
+  *id = 0;
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS) {
+    set_error("gbs_fft_c2r_noalloc: cuCtxGetId failed");
+    return GBS_ECUDA;
+  }
+  return GBS_OK;
+}
 
 // Device address of the scratch array on the current device (set-up on the
-// first call per device).
+// first call per device and context).
 static int scratch_address(unsigned char** out) {
   int dev = 0;
   GBS_CUDA_TRY(cudaGetDevice(&dev));
@@ -51,16 +104,25 @@ static int scratch_address(unsigned char** out) {
     set_error("gbs_fft_c2r_noalloc: device ordinal %d out of range", dev);
     return GBS_EINVAL;
   }
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || ctx == 0 || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
+    // initialises the device's primary context if this thread has none yet
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       set_error("gbs_fft_c2r_noalloc: cudaGetSymbolAddress failed: %s",
                 cudaGetErrorString(e));
       return GBS_ECUDA;
     }
+    if (ctx == 0) {
+      rc = current_context_id(&ctx);
+      if (rc) return rc;
+    }
     g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return GBS_OK;

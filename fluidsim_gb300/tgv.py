@@ -1,15 +1,13 @@
-"""Taylor-Green vortex: FP64 GPU vs the FP64 CPU oracle, FP32 vs FP64 on GPU.
+"""Taylor-Green vortex runs on the GPU: FP64 and FP32 to t_end.
 
 Configuration: 256^3 periodic box L = 2 pi, u = sin x cos y cos z,
 v = -cos x sin y cos z, w = 0 (``doc/test_cases/Taylor_Green_vortices/
 run_simul.py:40-54``), nu = 1/1600, RK4 with exact integrating factor, CFL
 0.5, 2/3 dealiasing, run to t = 10.
 
-* ``oracle_steps`` first steps: FP64 GPU state against the FP64 CPU oracle
-  (relative L2 per velocity component), same time steps;
-* FP64 and FP32 GPU runs to ``t_end``: dissipation rate
-  eps(t) = sum 2 nu k^2 E(k) (FP64 reductions) every ``every`` steps, and
-  the FP32 state's relative L2 against FP64 at the end.
+FP64 and FP32 GPU runs to ``t_end``: dissipation rate
+eps(t) = sum 2 nu k^2 E(k) (FP64 reductions) every ``every`` steps, and the
+FP32 state's relative L2 against FP64 at the end.
 
 ``python -m fluidsim_gb300.tgv`` prints one JSON line.
 """
@@ -60,44 +58,15 @@ def run_curve(sim, t_end, every):
     return np.array(curve), wall
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--t-end", type=float, default=10.0)
-    ap.add_argument("--oracle-steps", type=int, default=20)
-    ap.add_argument("--every", type=int, default=10)
-    a = ap.parse_args()
-    n = a.n
-    out = {"config": {"workload": f"Taylor-Green vortex {n}^3", "nu": 1 / 1600, "cfl": 0.5,
-                      "t_end": a.t_end}}
-
-    # 1. FP64 GPU vs FP64 CPU oracle over the first steps
-    from oracle.solvers import NS3DOracle
-    from oracle.spectral import OperNumpy3D
-    sim = make(n, "float64")
-    orc = NS3DOracle(OperNumpy3D(n, n, n), nu_2=1 / 1600, USE_CFL=True, cfl_coef=0.5,
-                     deltat0=0.2, deltat_max=0.2)
-    v0 = taylor_green_3d(n, n, n)
-    orc.init_from_vxvyvzfft(*v0)
-    t0 = time.perf_counter()
-    for _ in range(a.oracle_steps):
-        orc.one_time_step()
-    cpu_s = (time.perf_counter() - t0) / a.oracle_steps
-    for _ in range(a.oracle_steps):
-        sim.time_stepping.one_time_step()
-    out["fp64_vs_oracle"] = {"steps": a.oracle_steps,
-                             "rel_l2": rel_l2(sim.state.state_spect.cpu().numpy(),
-                                              orc.state_spect),
-                             "dt_gpu": sim.time_stepping.deltat, "dt_oracle": orc.deltat,
-                             "oracle_s_per_step": cpu_s}
-    del sim, orc
-
-    # 2. FP64 and FP32 GPU runs to t_end with the dissipation curve
+def compare_precisions(n, t_end, every):
+    """FP64 and FP32 runs to ``t_end``: their eps(t) curves and the FP32
+    state's relative L2 against FP64 at the end."""
+    out = {}
     curves = {}
     finals = {}
     for prec in ("float64", "float32"):
         sim = make(n, prec)
-        curve, wall = run_curve(sim, a.t_end, a.every)
+        curve, wall = run_curve(sim, t_end, every)
         curves[prec] = curve
         finals[prec] = sim.state.state_spect.cpu().numpy().astype(np.complex128)
         out[prec] = {"steps": sim.time_stepping.it, "wall_s": wall,
@@ -115,6 +84,18 @@ def main():
     }
     out["eps_curve_fp64"] = c64[:, [0, 2]].round(8).tolist()
     out["eps_curve_fp32"] = c32[:, [0, 2]].round(8).tolist()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--t-end", type=float, default=10.0)
+    ap.add_argument("--every", type=int, default=10)
+    a = ap.parse_args()
+    out = {"config": {"workload": f"Taylor-Green vortex {a.n}^3", "nu": 1 / 1600, "cfl": 0.5,
+                      "t_end": a.t_end}}
+    out.update(compare_precisions(a.n, a.t_end, a.every))
     print(json.dumps(out))
 
 

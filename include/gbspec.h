@@ -72,10 +72,14 @@ int gbs_fft_c2r(gbs_fft_plan* plan, void* k, void* x, int may_destroy,
  * a plan of this shape; k is preserved.  Twiddles and workspace live in one
  * static 32 MiB device array that every GPU loading the library holds until
  * exit; shapes needing more (3*align256 twiddle tables + batch * nK
- * complex) are rejected with GBS_EINVAL.  The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture.  All calls share the array: calls whose
- * GPU work overlaps race. */
+ * complex) are rejected with GBS_EINVAL.  The first call on a device (and
+ * the first after a cudaDeviceReset) looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  Under lazy module loading (the CUDA default) that first call is
+ * also where the driver allocates the 32 MiB array: make one small call on
+ * each device before a pool takes all device memory, or set
+ * CUDA_MODULE_LOADING=EAGER.  All calls share the array: calls whose GPU
+ * work overlaps race. */
 int gbs_fft_c2r_noalloc(int ndim, const int64_t* shapeX, int dtype, int batch,
                         const void* k, void* x, void* stream);
 

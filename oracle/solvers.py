@@ -8,7 +8,7 @@ import random
 
 import numpy as np
 
-from .spectral import OperNumpy2D, OperNumpy3D
+from .spectral import OperNumpy2D, OperNumpy3D, slab_map
 
 
 def max_abs(arr):
@@ -96,21 +96,41 @@ class _SolverBase:
             self.deltat = maybe_new_dt
 
     def time_step_RK4(self):
-        """``pseudo_spect.py:798-984`` line for line."""
+        """``pseudo_spect.py:798-984`` line for line (each expression run over
+        slabs of the first spatial axis on all host cores)."""
         dt = self.deltat
         diss, diss2 = self._coefs()
         S = self.state_spect
+        tmp = np.empty_like(S)
+        tmp1 = np.empty_like(S)
+        nslab = S.shape[1]
         N0 = self.tendencies_nonlin()
-        tmp = (S + dt / 6 * N0) * diss
-        tmp1 = (S + dt / 2 * N0) * diss2
+
+        def stage1(sl):
+            s = (slice(None), sl)
+            tmp[s] = (S[s] + dt / 6 * N0[s]) * diss[sl]
+            tmp1[s] = (S[s] + dt / 2 * N0[s]) * diss2[sl]
+        slab_map(stage1, nslab)
         N1 = self.tendencies_nonlin(tmp1)
-        tmp += dt / 3 * diss2 * N1
-        tmp1 = S * diss2 + dt / 2 * N1
+
+        def stage2(sl):
+            s = (slice(None), sl)
+            tmp[s] += dt / 3 * diss2[sl] * N1[s]
+            tmp1[s] = S[s] * diss2[sl] + dt / 2 * N1[s]
+        slab_map(stage2, nslab)
         N2 = self.tendencies_nonlin(tmp1)
-        tmp += dt / 3 * diss2 * N2
-        tmp1 = S * diss + dt * diss2 * N2
+
+        def stage3(sl):
+            s = (slice(None), sl)
+            tmp[s] += dt / 3 * diss2[sl] * N2[s]
+            tmp1[s] = S[s] * diss[sl] + dt * diss2[sl] * N2[s]
+        slab_map(stage3, nslab)
         N3 = self.tendencies_nonlin(tmp1)
-        S[:] = tmp + dt / 6 * N3
+
+        def stage4(sl):
+            s = (slice(None), sl)
+            S[s] = tmp[s] + dt / 6 * N3[s]
+        slab_map(stage4, nslab)
 
     def time_step_Euler(self):
         """``pseudo_spect.py:245-280`` (``step_Euler_inplace``, 51-60)."""
@@ -547,9 +567,13 @@ class NS3DOracle(_SolverBase):
         else:
             vx, vy, vz = oper.ifft(vx_fft), oper.ifft(vy_fft), oper.ifft(vz_fft)
         # fluidfft vector_product(v, omega) = v x omega
-        fx = vy * oz - vz * oy
-        fy = vz * ox - vx * oz
-        fz = vx * oy - vy * ox
+        fx, fy, fz = np.empty((3,) + vx.shape)
+
+        def product(sl):
+            fx[sl] = vy[sl] * oz[sl] - vz[sl] * oy[sl]
+            fy[sl] = vz[sl] * ox[sl] - vx[sl] * oz[sl]
+            fz[sl] = vx[sl] * oy[sl] - vy[sl] * ox[sl]
+        slab_map(product, vx.shape[0])
         F = np.empty_like(self.state_spect)
         F[0] = oper.fft(fx)
         F[1] = oper.fft(fy)

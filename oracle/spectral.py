@@ -25,12 +25,37 @@ tests pin:
 """
 
 import os
+from concurrent.futures import ThreadPoolExecutor
 from math import pi
 
 import numpy as np
 import scipy.fft as sfft
 
 WORKERS = os.cpu_count() or 1
+_POOL = None
+
+
+def slabs(n, parts=None):
+    """Split ``range(n)`` into at most ``parts`` (default: all host cores)
+    contiguous slices."""
+    parts = max(1, min(n, parts or WORKERS))
+    b = [n * i // parts for i in range(parts + 1)]
+    return [slice(b[i], b[i + 1]) for i in range(parts)]
+
+
+def slab_map(fn, n):
+    """Run ``fn(sl)`` over slabs ``sl`` of a leading axis of length ``n`` on
+    all host cores (numpy ufuncs release the GIL).  Each element gets the same
+    operations as one whole-array expression, so results do not depend on the
+    number of slabs."""
+    global _POOL
+    if WORKERS == 1 or n < 2:
+        fn(slice(None))
+        return
+    if _POOL is None:
+        _POOL = ThreadPoolExecutor(WORKERS)
+    for _ in _POOL.map(fn, slabs(n)):
+        pass
 
 
 def kadim_from_ik(ik, n):
@@ -148,10 +173,20 @@ class OperNumpy3D:
 
     # -- transforms -----------------------------------------------------------
     def fft(self, fieldX):
-        return _rfftn(fieldX) / self.npoints
+        out = _rfftn(fieldX)
+
+        def norm(sl):
+            out[sl] /= self.npoints
+        slab_map(norm, out.shape[0])
+        return out
 
     def ifft(self, fieldK):
-        return _irfftn(fieldK, self.shapeX) * self.npoints
+        out = _irfftn(fieldK, self.shapeX)
+
+        def norm(sl):
+            out[sl] *= self.npoints
+        slab_map(norm, out.shape[0])
+        return out
 
     def fft_as_arg(self, fieldX, fieldK):
         fieldK[...] = self.fft(fieldX)
@@ -177,10 +212,16 @@ class OperNumpy3D:
 
     # -- spectral operators ---------------------------------------------------
     def rotfft_from_vecfft(self, vx, vy, vz):
-        Kx, Ky, Kz = self.Kx, self.Ky, self.Kz
-        return (1j * (Ky * vz - Kz * vy),
-                1j * (Kz * vx - Kx * vz),
-                1j * (Kx * vy - Ky * vx))
+        out = np.empty((3,) + np.shape(vx), np.complex128)
+
+        def curl(sl):
+            Kx, Ky, Kz = self.Kx[sl], self.Ky[sl], self.Kz[sl]
+            x, y, z = vx[sl], vy[sl], vz[sl]
+            out[0][sl] = 1j * (Ky * z - Kz * y)
+            out[1][sl] = 1j * (Kz * x - Kx * z)
+            out[2][sl] = 1j * (Kx * y - Ky * x)
+        slab_map(curl, out.shape[1])
+        return out[0], out[1], out[2]
 
     def rotfft_from_vecfft_outin(self, vx, vy, vz, rx, ry, rz):
         ox, oy, oz = self.rotfft_from_vecfft(vx, vy, vz)
@@ -197,10 +238,14 @@ class OperNumpy3D:
 
     def project_perpk3d(self, vx, vy, vz):
         """In place ``v -= k (k.v)/|k|^2``; the k=0 mode is unchanged."""
-        tmp = (self.Kx * vx + self.Ky * vy + self.Kz * vz) * self.inv_K_square_nozero
-        vx -= self.Kx * tmp
-        vy -= self.Ky * tmp
-        vz -= self.Kz * tmp
+        def proj(sl):
+            Kx, Ky, Kz = self.Kx[sl], self.Ky[sl], self.Kz[sl]
+            x, y, z = vx[sl], vy[sl], vz[sl]
+            tmp = (Kx * x + Ky * y + Kz * z) * self.inv_K_square_nozero[sl]
+            x -= Kx * tmp
+            y -= Ky * tmp
+            z -= Kz * tmp
+        slab_map(proj, np.shape(vx)[0])
 
     def div_vb_fft_from_vb(self, vx, vy, vz, b):
         """Spectral divergence of v b for physical fields (fluidfft's
@@ -239,7 +284,11 @@ class OperNumpy3D:
 
     def dealiasing_variable(self, arr):
         if self._has_to_dealiase:
-            arr[self.where_dealiased.astype(bool)] = 0.0
+            mask = self.where_dealiased.astype(bool)
+
+            def zero(sl):
+                arr[sl][mask[sl]] = 0.0
+            slab_map(zero, arr.shape[0])
 
     def dealiasing(self, *args):
         for thing in args:

@@ -2,7 +2,7 @@
 
 Usage (needs the fluidsim 0.8.3 sources; writes ``tests/golden/*.npz``)::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <fluidsim source root> [case ...]
 
 Each case builds a reference ns2d / ns3d ``Simul`` with ``oracle.refshim``
 (the reference's ``TimeSteppingPseudoSpectral`` RK4, CFL logic,
@@ -307,4 +307,6 @@ def main(ref_root, only=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <fluidsim source root> [case ...]")
+    main(sys.argv[1], sys.argv[2:])

@@ -67,3 +67,50 @@ def test_noalloc_rejects_oversize(cuda):
                                  ctypes.c_void_p(dummy.data_ptr()), _stream())
     assert rc == -22
     assert b"static maximum" in lib.gbs_last_error()
+
+
+def test_noalloc_after_warmup_with_device_memory_taken(cuda):
+    """The caller this entry point is for: after one warm-up call (which,
+    under lazy module loading, is where the driver allocates the static
+    array), a pool takes nearly all free device memory, and later calls must
+    still succeed.  Less than the 32 MiB array stays free, so a call that
+    needed to allocate it, or anything else as large, would fail."""
+    import torch
+    lib = cuda
+    shape, dtype, batch = (32, 24, 16), 1, 1
+    nk = shape[:-1] + (shape[-1] // 2 + 1,)
+    c_shape = (ctypes.c_int64 * 3)(*shape)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    K = torch.randn((batch,) + nk, dtype=torch.complex128, device="cuda", generator=g)
+    out = torch.empty((batch,) + shape, dtype=torch.float64, device="cuda")
+    ref = torch.empty_like(out)
+    plan = ctypes.c_void_p()
+    assert lib.gbs_fft_plan_create(3, c_shape, dtype, batch, ctypes.byref(plan)) == 0
+    try:
+        assert lib.gbs_fft_c2r(plan, ctypes.c_void_p(K.data_ptr()),
+                               ctypes.c_void_p(ref.data_ptr()), 0, _stream()) == 0
+    finally:
+        lib.gbs_fft_plan_destroy(plan)
+    rc = lib.gbs_fft_c2r_noalloc(3, c_shape, dtype, batch, ctypes.c_void_p(K.data_ptr()),
+                                 ctypes.c_void_p(out.data_ptr()), _stream())
+    assert rc == 0, lib.gbs_last_error()  # warm-up
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    keep = 24 << 20  # less than the 32 MiB static array
+    take = (free - keep) // (2 << 20) * (2 << 20)
+    pool = torch.empty(take, dtype=torch.uint8, device="cuda") if take > 0 else None
+    try:
+        assert torch.cuda.mem_get_info()[0] < (32 << 20)
+        for _ in range(2):
+            out.fill_(float("nan"))
+            rc = lib.gbs_fft_c2r_noalloc(3, c_shape, dtype, batch,
+                                         ctypes.c_void_p(K.data_ptr()),
+                                         ctypes.c_void_p(out.data_ptr()), _stream())
+            assert rc == 0, lib.gbs_last_error()
+            torch.cuda.synchronize()
+            err = (out - ref).abs().max().item() / ref.abs().max().item()
+            assert err <= TOL[dtype], err
+    finally:
+        del pool
+        torch.cuda.empty_cache()
