@@ -6,7 +6,9 @@ import scipy.fft as sfft
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(16, 16), (40, 48), (15, 20), (256, 256), (8, 12, 10), (10, 15, 20),
-          (32, 32, 32), (64, 48, 40), (128, 128, 128), (4, 6, 2), (1, 8, 8)]
+          (32, 32, 32), (64, 48, 40), (128, 128, 128), (4, 6, 2), (1, 8, 8),
+          # the 512-point column and row kernels of the 512^3 benchmark step
+          (512, 512), (512, 512, 16), (16, 16, 512), (512, 512, 512)]
 TOL = {"float64": 1e-13, "float32": 3e-6}
 
 
