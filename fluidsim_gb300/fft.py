@@ -238,18 +238,29 @@ class FFT3DGB300(_FFTGB300):
     ndim = 3
 
 
+# fluidfft method name -> plugin module (the `fluidfft.plugins` entry points
+# that pyproject.toml declares)
+PLUGIN_MODULES = {
+    "fft2d.with_gb300": "fluidsim_gb300.plugins.fft2d_with_gb300",
+    "fft3d.with_gb300": "fluidsim_gb300.plugins.fft3d_with_gb300",
+}
+
+
 def import_fft_class(name, dim=None):
-    """Resolve a ``params.oper.type_fft`` string to an FFT class."""
-    table = {
-        "fft2d.with_gb300": FFT2DGB300, "fluidfft.fft2d.with_gb300": FFT2DGB300,
-        "fft3d.with_gb300": FFT3DGB300, "fluidfft.fft3d.with_gb300": FFT3DGB300,
-    }
+    """Resolve a ``params.oper.type_fft`` string to an FFT class, as
+    fluidfft's ``import_fft_class`` does for a plugin: strip a leading
+    ``fluidfft.``, import the module the method's entry point names and
+    return its ``FFTclass``.  ``"default"``/``"sequential"``/``"gb300"``
+    select this plugin's class of dimension ``dim``."""
+    import importlib
     if name in (None, "default", "sequential", "gb300", "with_gb300"):
         if dim is None:
             raise ValueError("dim is required for the default FFT class")
-        return FFT2DGB300 if dim == 2 else FFT3DGB300
+        name = "fft2d.with_gb300" if dim == 2 else "fft3d.with_gb300"
+    method = name[len("fluidfft."):] if name.startswith("fluidfft.") else name
     try:
-        return table[name]
+        module = PLUGIN_MODULES[method]
     except KeyError:
         raise ValueError(f"unknown FFT class {name!r} (this plugin provides "
-                         f"{sorted(table)})") from None
+                         f"{sorted(PLUGIN_MODULES)})") from None
+    return importlib.import_module(module).FFTclass
