@@ -35,6 +35,7 @@ EXPORTED = (
     "gbs_ens2d_mixed_create", "gbs_ens2d_mixed_destroy", "gbs_ens2d_mixed_step",
     "gbs_ens2d_mixed_set_tuning",
     "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection", "gbs_ns_set_phase_shifts",
+    "gbs_spectra_sizes", "gbs_spectra",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
            "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
@@ -94,6 +95,10 @@ def _declare(lib):
         "gbs_ns_spatial_means": (ctypes.c_int, [P, P, DP, P]),
         "gbs_ns_spectrum_size": (ctypes.c_int, [P, I64P]),
         "gbs_ns_spectrum": (ctypes.c_int, [P, P, P, P]),
+        "gbs_spectra_sizes": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.POINTER(ctypes.c_double),
+                                             I64P]),
+        "gbs_spectra": (ctypes.c_int, [ctypes.c_int, I64P, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int, P, P, P, P, P, P, P]),
         "gbs_ns_is_dealiased": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_int), P]),
         "gbs_ns_timing": (ctypes.c_int, [P, ctypes.c_int]),
         "gbs_ns_timing_report": (ctypes.c_int, [P, DP, I64P, ctypes.c_int, I64P]),

@@ -108,19 +108,42 @@ class _OperBase:
     # (x non-negative) is summed with the Hermitian weights (x modes other
     # than 0 and nx/2 count twice) and divided by the bin width; a mode goes
     # to bin round(|k| / dk).
-    def _hermitian_weights(self):
-        nkx = self.nx // 2 + 1
-        w = torch.full((nkx,), 2.0, dtype=torch.float64, device=self.device)
-        w[0] = 1.0
-        if self.nx % 2 == 0:
-            w[-1] = 1.0
-        return w
+    def _deltak(self):
+        return (self.deltakx, self.deltaky, getattr(self, "deltakz", 1.0))[: self.ndim]
 
-    def _bin_sum(self, values, index, nbins):
-        out = torch.zeros(nbins, dtype=torch.float64, device=self.device)
-        index = index.clamp(max=nbins - 1).reshape(-1)
-        out.index_add_(0, index, values.reshape(-1))
-        return out
+    def _spectra(self, energy_fft, kx=False, ky=False, kz=False, shell=False, kzkh=False):
+        """FP64 spectra of ``energy_fft`` (real, shapeK) by the ``gbs_spectra``
+        kernel; returns the requested outputs, in (kx, ky, kz, shell, kzkh)
+        order, as float64 device tensors."""
+        import ctypes
+
+        from . import _lib
+        from .fft import current_stream_handle
+        e = energy_fft if isinstance(energy_fft, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(energy_fft))
+        e = e.to(self.device)
+        if e.dtype not in (torch.float32, torch.float64):
+            e = e.to(torch.float64)
+        e = e.contiguous()
+        if tuple(e.shape) != tuple(self.shapeK):
+            raise ValueError(f"energy array of shape {tuple(e.shape)}, expected {self.shapeK}")
+        lib = self.opfft._lib
+        shape = (ctypes.c_int64 * self.ndim)(*self.shapeX)
+        dk = (ctypes.c_double * self.ndim)(*self._deltak())
+        sizes = (ctypes.c_int64 * 5)()
+        _lib.check(lib.gbs_spectra_sizes(self.ndim, shape, dk, sizes), "spectra")
+        want = (kx, ky, kz, shell, kzkh)
+        lens = (sizes[0], sizes[1], sizes[2], sizes[3], sizes[2] * sizes[4])
+        outs = [torch.empty(n, dtype=torch.float64, device=self.device) if w else None
+                for w, n in zip(want, lens)]
+        ptrs = [ctypes.c_void_p(o.data_ptr()) if o is not None else None for o in outs]
+        dtype = _lib.GBS_F64 if e.dtype == torch.float64 else _lib.GBS_F32
+        with torch.cuda.device(self.device):
+            _lib.check(lib.gbs_spectra(self.ndim, shape, dk, dtype, ctypes.c_void_p(e.data_ptr()),
+                                       *ptrs, current_stream_handle()), "spectra")
+        if kzkh:
+            outs[4] = outs[4].reshape(int(sizes[2]), int(sizes[4]))
+        return [o for o in outs if o is not None]
 
     def create_arrayX_random(self, min_val=None, max_val=None, shape="loc"):
         """Uniform random real array (``min_val`` 0, ``max_val`` 1 by default)."""
@@ -221,22 +244,17 @@ class OperatorsPseudoSpectral2D(_OperBase):
         fy_fft.sub_(self.KY * tmp)
 
     def compute_1dspectra(self, energy_fft):
-        """(E(kx), E(ky)) of an energy array: sums over the other axis,
-        divided by the bin width."""
-        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, :]
-        skx = e.sum(0) / self.deltakx
-        iky = torch.from_numpy(np.abs(_kadim(self.ny))).to(self.device)
-        sky = self._bin_sum(e.sum(1), iky, self.ny // 2 + 1) / self.deltaky
-        return skx, sky
+        """(E(kx), E(ky)) of an energy array: Hermitian-weighted sums over the
+        other axis, |ky| binned, divided by the bin width (FP64)."""
+        return tuple(self._spectra(energy_fft, kx=True, ky=True))
 
     def compute_2dspectrum(self, energy_fft):
-        """Shell-summed spectrum, bins round(|k| / dk), dk = min(dkx, dky)."""
-        dk = min(self.deltakx, self.deltaky)
-        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, :]
-        kk = torch.sqrt(self.KX.to(torch.float64) ** 2 + self.KY.to(torch.float64) ** 2)
-        idx = torch.floor(kk / dk + 0.5).to(torch.int64)
-        nb = int(max(self.nx, self.ny) // 2 + 1)
-        return self._bin_sum(e, idx, nb) / dk
+        """Shell-summed spectrum, bins floor(|k| / dk + 0.5), dk = min(dkx, dky)."""
+        return self._spectra(energy_fft, shell=True)[0]
+
+    # names fluidsim's ns2d outputs bind (fluidsim/base/output/spectra.py:373-374)
+    spectra1D_from_fft = compute_1dspectra
+    spectrum2D_from_fft = compute_2dspectrum
 
     def produce_str_describing_oper(self):
         return f"{self.nx}x{self.ny}"
@@ -367,40 +385,19 @@ class OperatorsPseudoSpectral3D(_OperBase):
         return out
 
     def compute_1dspectra(self, energy_fft):
-        """(E(kx), E(ky), E(kz)) of an energy array: sums over the other
-        axes, |k| binned along y and z, divided by the bin width."""
-        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
-        skx = e.sum((0, 1)) / self.deltakx
-        iky = torch.from_numpy(np.abs(_kadim(self.ny))).to(self.device)
-        ikz = torch.from_numpy(np.abs(_kadim(self.nz))).to(self.device)
-        sky = self._bin_sum(e.sum((0, 2)), iky, self.ny // 2 + 1) / self.deltaky
-        skz = self._bin_sum(e.sum((1, 2)), ikz, self.nz // 2 + 1) / self.deltakz
-        return skx, sky, skz
+        """(E(kx), E(ky), E(kz)) of an energy array: Hermitian-weighted sums
+        over the other axes, |ky| and |kz| binned, divided by the bin width."""
+        return tuple(self._spectra(energy_fft, kx=True, ky=True, kz=True))
 
     def compute_3dspectrum(self, energy_fft):
-        """Shell-summed spectrum, bins round(|k| / dk), dk = min(dkx, dky, dkz)."""
-        dk = min(self.deltakx, self.deltaky, self.deltakz)
-        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
-        k = torch.sqrt(self.Kx.to(torch.float64) ** 2 + self.Ky.to(torch.float64) ** 2
-                       + self.Kz.to(torch.float64) ** 2)
-        idx = torch.floor(k / dk + 0.5).to(torch.int64)
-        nb = int(max(self.nx, self.ny, self.nz) // 2 + 1)
-        return self._bin_sum(e, idx, nb) / dk
+        """Shell-summed spectrum, bins floor(|k| / dk + 0.5), dk = min(dkx, dky, dkz)."""
+        return self._spectra(energy_fft, shell=True)[0]
 
     def compute_spectrum_kzkh(self, energy_fft):
-        """2D spectrum over (|kz|, kh), kh = sqrt(kx^2 + ky^2), bins
-        round(|kz| / dkz) and round(kh / dkh), dkh = min(dkx, dky)."""
-        dkh = min(self.deltakx, self.deltaky)
-        e = energy_fft.to(torch.float64) * self._hermitian_weights()[None, None, :]
-        kh = torch.sqrt(self.Kx.to(torch.float64) ** 2 + self.Ky.to(torch.float64) ** 2)
-        ih = torch.floor(kh / dkh + 0.5).to(torch.int64)
-        nh = int(max(self.nx, self.ny) // 2 + 1)
-        ih = ih.clamp(max=nh - 1)
-        iz = torch.from_numpy(np.abs(_kadim(self.nz))).to(self.device)[:, None, None]
-        nz = self.nz // 2 + 1
-        flat = (iz * nh + ih).expand(self.shapeK)
-        out = self._bin_sum(e, flat, nz * nh).reshape(nz, nh)
-        return out / (self.deltakz * dkh)
+        """2D spectrum over (|kz|, kh), kh = sqrt(kx^2 + ky^2): rows |kz_adim|,
+        columns floor(kh / dkh + 0.5), dkh = min(dkx, dky), divided by
+        dkz dkh."""
+        return self._spectra(energy_fft, kzkh=True)[0]
 
     def project_perpk3d(self, vx_fft, vy_fft, vz_fft):
         tmp = (self.Kx * vx_fft + self.Ky * vy_fft + self.Kz * vz_fft) * self.inv_K_square_nozero

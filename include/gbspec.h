@@ -333,6 +333,27 @@ int gbs_ns_spectrum_size(gbs_ns* solver, int64_t* nk);
 int gbs_ns_spectrum(gbs_ns* solver, const void* state_spect, double* spectrum,
                     void* stream);
 
+/* FP64 spectra of a real spectral energy density `energy` (shape (nz, ny,
+ * nx/2+1), 2D: (ny, nx/2+1); dtype GBS_F32 or GBS_F64), replacing the
+ * operator methods compute_1dspectra / compute_3dspectrum /
+ * compute_spectrum_kzkh (3D) and spectra1D_from_fft / spectrum2D_from_fft
+ * (2D) that fluidsim's spectra outputs call
+ * (fluidsim/solvers/ns3d/output/spectra.py:15-100,
+ * fluidsim/solvers/ns2d/output/spectra.py:16-27, bound at
+ * fluidsim/base/output/spectra.py:373-374; the methods live in fluidfft).
+ * Hermitian weights (1 for kx = 0 and the Nyquist column, else 2), each
+ * output divided by its bin width: skx[nx/2+1] per kx; sky[ny/2+1] and
+ * skz[nz/2+1] binned by |k_adim|; shell[n3] binned by floor(|k|/dk + 0.5),
+ * dk = min(deltak); kzkh[(nz/2+1) * nkh] by |kz_adim| and
+ * floor(kh/dkh + 0.5), dkh = min(dkx, dky).  deltak = (dkx, dky[, dkz]).
+ * Any output may be NULL (skz and kzkh must be in 2D); device pointers.
+ * gbs_spectra_sizes writes (nx/2+1, ny/2+1, nz/2+1 or 0, n3, nkh or 0). */
+int gbs_spectra_sizes(int ndim, const int64_t* shapeX, const double* deltak,
+                      int64_t* sizes);
+int gbs_spectra(int ndim, const int64_t* shapeX, const double* deltak, int dtype,
+                const void* energy, double* skx, double* sky, double* skz,
+                double* shell, double* kzkh, void* stream);
+
 /* ns3d projection of the tendencies and of the state after each step
  * (Simul.project_state_spect, fluidsim/solvers/ns3d/solver.py:147-175,
  * 255-263): params.projection None / "toroidal" ("vortical") / "poloidal"

@@ -315,18 +315,45 @@ class OperNumpy3D:
     def mean_space(self, arr):
         return float(np.mean(arr))
 
-    def compute_3dspectrum(self, energy_fft):
-        """Shell spectrum; bins ``round(|k|/deltak_min)`` (own definition)."""
-        dk = min(self.deltakx, self.deltaky, self.deltakz)
-        kmod = np.sqrt(self.K2)
-        ik = np.floor(kmod / dk + 0.5).astype(np.int64)
-        nk = int(ik.max()) + 1
-        w = np.full(self.shapeK[2], 2.0)
+    # -- spectra ------------------------------------------------------------
+    # fluidfft's compute_1dspectra / compute_3dspectrum / compute_spectrum_kzkh
+    # (called by fluidsim/solvers/ns3d/output/spectra.py:15-100) are not in
+    # the reference; restated from their definitions: Hermitian weights over
+    # the half spectrum, sums binned by |k_adim| (1D), floor(|k|/dk + 0.5)
+    # (shells, dk = min of the deltak) and floor(kh/dkh + 0.5) (kh columns,
+    # dkh = min(dkx, dky)), each divided by its bin width.
+    def hermitian_weights(self):
+        w = np.full(self.shapeK[-1], 2.0)
         w[0] = 1.0
         if self.nx % 2 == 0:
             w[-1] = 1.0
-        e = np.bincount(ik.ravel(), weights=(energy_fft * w).ravel(), minlength=nk)
-        return dk * np.arange(nk), e / dk
+        return w
+
+    def compute_1dspectra(self, energy_fft):
+        e = np.asarray(energy_fft, dtype=np.float64) * self.hermitian_weights()
+        skx = e.sum(axis=(0, 1)) / self.deltakx
+        iky = np.abs(k_adim_seq(self.ny))
+        ikz = np.abs(k_adim_seq(self.nz))
+        sky = np.bincount(iky, weights=e.sum(axis=(0, 2)), minlength=self.ny // 2 + 1)
+        skz = np.bincount(ikz, weights=e.sum(axis=(1, 2)), minlength=self.nz // 2 + 1)
+        return skx, sky / self.deltaky, skz / self.deltakz
+
+    def compute_3dspectrum(self, energy_fft):
+        dk = min(self.deltakx, self.deltaky, self.deltakz)
+        ik = np.floor(np.sqrt(self.K2) / dk + 0.5).astype(np.int64)
+        e = np.asarray(energy_fft, dtype=np.float64) * self.hermitian_weights()
+        return np.bincount(ik.ravel(), weights=e.ravel(), minlength=int(ik.max()) + 1) / dk
+
+    def compute_spectrum_kzkh(self, energy_fft):
+        dkh = min(self.deltakx, self.deltaky)
+        kh = np.sqrt(self.Kx**2 + self.Ky**2)
+        ih = np.floor(kh / dkh + 0.5).astype(np.int64)
+        nkh = int(ih.max()) + 1
+        nzb = self.nz // 2 + 1
+        iz = np.broadcast_to(np.abs(k_adim_seq(self.nz))[:, None, None], self.shapeK)
+        e = np.asarray(energy_fft, dtype=np.float64) * self.hermitian_weights()
+        flat = np.bincount((iz * nkh + ih).ravel(), weights=e.ravel(), minlength=nzb * nkh)
+        return flat.reshape(nzb, nkh) / (self.deltakz * dkh)
 
 
 class OperNumpy2D:
@@ -453,3 +480,27 @@ class OperNumpy2D:
 
     def mean_space(self, arr):
         return float(np.mean(arr))
+
+    # fluidfft's spectra1D_from_fft / spectrum2D_from_fft (bound at
+    # fluidsim/base/output/spectra.py:373-374), restated as in the 3D case
+    def hermitian_weights(self):
+        w = np.full(self.shapeK[-1], 2.0)
+        w[0] = 1.0
+        if self.nx % 2 == 0:
+            w[-1] = 1.0
+        return w
+
+    def compute_1dspectra(self, energy_fft):
+        e = np.asarray(energy_fft, dtype=np.float64) * self.hermitian_weights()
+        iky = np.abs(k_adim_seq(self.ny))
+        sky = np.bincount(iky, weights=e.sum(axis=1), minlength=self.ny // 2 + 1)
+        return e.sum(axis=0) / self.deltakx, sky / self.deltaky
+
+    def compute_2dspectrum(self, energy_fft):
+        dk = min(self.deltakx, self.deltaky)
+        ik = np.floor(np.sqrt(self.K2) / dk + 0.5).astype(np.int64)
+        e = np.asarray(energy_fft, dtype=np.float64) * self.hermitian_weights()
+        return np.bincount(ik.ravel(), weights=e.ravel(), minlength=int(ik.max()) + 1) / dk
+
+    spectra1D_from_fft = compute_1dspectra
+    spectrum2D_from_fft = compute_2dspectrum
