@@ -35,11 +35,25 @@ EXPORTED = (
     "gbs_ens2d_mixed_create", "gbs_ens2d_mixed_destroy", "gbs_ens2d_mixed_step",
     "gbs_ens2d_mixed_set_tuning",
     "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection", "gbs_ns_set_phase_shifts",
-    "gbs_spectra_sizes", "gbs_spectra",
+    "gbs_spectra_sizes", "gbs_spectra", "gbs_forcing_coarse",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
            "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
            "RK2_phaseshift_random": 8}
+
+
+class ForcingParams(ctypes.Structure):
+    """Mirror of ``gbs_forcing_params``."""
+
+    _fields_ = [
+        ("ndim", ctypes.c_int),
+        ("nx", ctypes.c_int64), ("ny", ctypes.c_int64), ("nz", ctypes.c_int64),
+        ("nc", ctypes.c_int64),
+        ("nvar", ctypes.c_int), ("nkeys", ctypes.c_int), ("keys", ctypes.c_int * 8),
+        ("type", ctypes.c_int), ("which_root", ctypes.c_int),
+        ("forcing_rate", ctypes.c_double),
+        ("dtype", ctypes.c_int),
+    ]
 
 
 class NSParams(ctypes.Structure):
@@ -108,6 +122,8 @@ def _declare(lib):
                                                  ctypes.POINTER(MLPWeights)]),
         "gbs_mlp_grad_workspace": (ctypes.c_int64, [ctypes.c_int64]),
         "gbs_ns_set_forcing": (ctypes.c_int, [P, P]),
+        "gbs_forcing_coarse": (ctypes.c_int, [ctypes.POINTER(ForcingParams), P, P, P, P,
+                                              ctypes.c_double, ctypes.c_double, P, P, P]),
         "gbs_ens2d_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_double, PP]),

@@ -19,7 +19,7 @@ LIB = HERE / "libgbspec.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gbs_fft.cu", "gbs_ns.cu", "gbs_noalloc.cu", "gbs_fast_f32.cu", "gbs_fast_f64.cu",
            "gbs_turb.cu", "gbs_mlp.cu", "gbs_les.cu",
-           "gbs_ensemble.cu", "gbs_spectra.cu"]
+           "gbs_ensemble.cu", "gbs_spectra.cu", "gbs_forcing.cu"]
 
 
 def nvcc_path():

@@ -44,7 +44,14 @@ def make_sim(n, nu, cfl=0.5, precision="float32", turb=None, forcing=True, seed=
     ts = p.time_stepping
     ts.USE_CFL, ts.cfl_coef, ts.deltat0, ts.USE_T_END = True, cfl, 1e-3, False
     if forcing:
-        p.forcing.enable, p.forcing.type, p.forcing.seed = True, "tcrandom", seed
+        # tcrandom on the three velocity components in shells k in [2, 3]; each
+        # component is normalized to 1/3, a total injection rate of 1
+        pf = p.forcing
+        pf.enable, pf.type, pf.seed = True, "tcrandom", seed
+        pf.nkmin_forcing, pf.nkmax_forcing = 2, 3
+        pf.key_forced = ["vx_fft", "vy_fft", "vz_fft"]
+        pf.forcing_rate = 1.0 / 3
+        pf.tcrandom.time_correlation = 1.0
     if turb == "smagorinsky":
         p.turb_model.enable, p.turb_model.type = True, "smagorinsky"
     elif turb is not None:

@@ -340,9 +340,18 @@ class _SimulBase:
         TimeSteppingPseudoSpectral._complete_params_with_default(params)
         Output._complete_params_with_default(params)
         params._set_child("init_fields", attribs={"type": "in_script"})
+        # fluidsim/base/forcing/base.py:55-90 and specific.py:440-455,
+        # 736-745, 775-782 (defaults of ForcingBasePseudoSpectral, normalized,
+        # random, tcrandom); `seed` (None: the global np.random state, as the
+        # reference) is this build's addition
         params._set_child("forcing", attribs={
-            "enable": False, "type": "", "forcing_rate": 1.0, "nkmin_forcing": 2,
-            "nkmax_forcing": 3, "seed": 0})
+            "enable": False, "type": "", "forcing_rate": 1.0, "key_forced": None,
+            "nkmin_forcing": 4, "nkmax_forcing": 5, "seed": None})
+        params.forcing._set_child("normalized", attribs={
+            "type": "2nd_degree_eq", "which_root": "minabs", "constant_rate_of": None})
+        params.forcing._set_child("random", attribs={"only_positive": False})
+        params.forcing._set_child("tcrandom", attribs={
+            "time_correlation": "based_on_forcing_rate"})
         cls._complete_params_with_default(params)
         return params
 
@@ -352,8 +361,11 @@ class _SimulBase:
 
     def __init__(self, params):
         self.params = params
-        if params.forcing.enable and (self.ndim != 3 or params.forcing.type != "tcrandom"):
-            raise NotImplementedError("forcing on GB300: ns3d with type 'tcrandom' only")
+        if params.forcing.enable:
+            from .forcing import FORCING_TYPES
+            if self.ndim != 3 or params.forcing.type not in FORCING_TYPES:
+                raise NotImplementedError(f"forcing on GB300: ns3d with a type of "
+                                          f"{FORCING_TYPES}")
         if params.init_fields.type != "in_script":
             raise NotImplementedError("only init_fields.type = 'in_script' is supported")
         self._lib = _lib.load()
@@ -567,10 +579,8 @@ class SimulNS3D(_SimulBase):
         self.is_turb_model_enabled = False
         self._closure = None
         if params.forcing.enable:
-            from .forcing import TCRandomForcing3D
-            pf = params.forcing
-            self.forcing = TCRandomForcing3D(self, pf.nkmin_forcing, pf.nkmax_forcing,
-                                             pf.forcing_rate, seed=pf.seed)
+            from .forcing import CoarseForcing3D
+            self.forcing = CoarseForcing3D(self)
             self.is_forcing_enabled = True
         tm = params.turb_model
         if tm.enable:

@@ -209,6 +209,43 @@ int gbs_ns_set_turb_model(gbs_ns* solver, int type, double C,
  * sim.forcing.compute() does once per step); NULL disables. */
 int gbs_ns_set_forcing(gbs_ns* solver, const void* forcing);
 
+/* One step of fluidsim's coarse normalized forcings, computed on the device
+ * into the dense `forcing` array given to gbs_ns_set_forcing (replaces
+ * SpecificForcingPseudoSpectralCoarse / NormalizedForcing.compute /
+ * normalize_forcingc_2nd_degree_eq / coef_normalization_from_abc and
+ * Proportional.compute, fluidsim/base/forcing/specific.py:137-727, for
+ * TimeCorrelatedRandomPseudoSpectral and RandomSimplePseudoSpectral,
+ * 729-868).  The coarse grid has nc points per axis (coarse spectral shape
+ * (nc, nc, nc/2+1), 2D (nc, nc/2+1)); coarse mode ic maps to the full-grid
+ * mode ic if ic <= nc/2, else ic - nc + n (kx unchanged).  For each forced
+ * state variable keys[k]:
+ *   type 0 (normalized): fr = f1 - mix (f1 - f0) from the coarse complex128
+ *     device arrays f0, f1; R = root of (dt/2 sum w|fr|^2) R^2 +
+ *     (sum w Re(conj(v) fr)) R - forcing_rate = 0, which_root 0: "minabs",
+ *     1: "positive";
+ *   type 1 (proportional): fr = v on the modes where no_forcing[i] == 0,
+ *     R = (sqrt(1 + dt P / Z) - 1) / dt with Z = sum w |fr|^2 / 2;
+ * forcing[keys[k]] = R fr on the coarse modes (nothing else written).  Sums
+ * in FP64 with the coarse grid's Hermitian weights.  coef (device, nkeys
+ * doubles, may be NULL) receives R.  One CTA; no host synchronisation. */
+typedef struct gbs_forcing_params {
+  int ndim;
+  int64_t nx, ny, nz; /* full grid (nz ignored in 2D) */
+  int64_t nc;         /* coarse points per axis (even) */
+  int nvar;           /* state variables in state_spect / forcing */
+  int nkeys;          /* forced variables, 1..8 */
+  int keys[8];
+  int type;           /* 0 normalized, 1 proportional */
+  int which_root;     /* 0 minabs, 1 positive */
+  double forcing_rate;
+  int dtype;          /* GBS_F32 / GBS_F64: state and forcing arrays */
+} gbs_forcing_params;
+
+int gbs_forcing_coarse(const gbs_forcing_params* params, const void* state_spect,
+                       const void* f0, const void* f1,
+                       const unsigned char* no_forcing, double mix, double dt,
+                       void* forcing, double* coef, void* stream);
+
 /* ------------------------------------------------ batched ns2d ensembles
  * nruns independent ns2d runs of one grid (power-of-two nx/2, ny in
  * 64..512), float32, advanced together: one launch per pass covers the

@@ -127,8 +127,13 @@ class _Container:
         setattr(self, name, child)
         return child
 
+    def __getitem__(self, key):
+        return getattr(self, key)
+
 
 class _OutputStub:
+    path_run = "/nonexistent/refshim-run"  # no saved forcing state to resume
+
     def one_time_step(self):
         pass
 
@@ -261,6 +266,24 @@ def load_reference(root):
     m["get_phases_random_2d"] = _reference_method(
         fs / "operators" / "operators2d.py", "OperatorsPseudoSpectral2D", "get_phases_random")
 
+    # forcing: the reference's forcing makers (specific.py) with
+    # fluiddyn's fftw_grid_size raising ImportError, the path a fluidsim
+    # installation without pulp (not among fluidsim's dependencies) takes;
+    # the coarse-grid methods of its OperatorsPseudoSpectral3D are compiled
+    # from operators3d.py as written and bound to the numpy operator
+    def fftw_grid_size(nk_min, bases=None, debug=False):
+        raise ImportError("pulp is not installed")
+
+    _module("fluiddyn.calcul.easypyfft").fftw_grid_size = fftw_grid_size
+    _module("fluidsim.base.forcing", package=True)
+    m["forcing_specific"] = _module("fluidsim.base.forcing.specific",
+                                    fs / "base" / "forcing" / "specific.py")
+    glob = {"nb_proc": 1, "rank": 0,
+            "_ik_from_ikc": _reference_function(ops_path, "_ik_from_ikc")}
+    for name in ("project_fft_on_realX", "coarse_seq_from_fft_loc",
+                 "put_coarse_array_in_array_fft"):
+        m[name] = _reference_method(ops_path, "OperatorsPseudoSpectral3D", name, glob)
+
     # turbulence model: the reference's Smagorinsky + stress tensor, with the
     # SimulExtender plumbing of turb_model/base.py replaced by a stand-in
     _module("fluidsim.base.turb_model", package=True)
@@ -280,21 +303,36 @@ def load_reference(root):
     return m
 
 
-def _reference_method(path, class_name, name):
+def _compile_def(path, node, extra=None):
+    node.decorator_list = []
+    mod = ast.Module(body=[node], type_ignores=[])
+    ns = {"np": np, "Ac": object, "Af": object, "uniform": random.uniform}
+    ns.update(extra or {})
+    exec(compile(mod, str(path), "exec"), ns)
+    return ns[node.name]
+
+
+def _reference_method(path, class_name, name, extra=None):
     """Function object of method ``name`` of class ``class_name`` in the
     reference source file ``path``, compiled from that file (decorators such
-    as transonic's ``boost`` dropped, annotations resolved to placeholders)."""
+    as transonic's ``boost`` dropped, annotations resolved to placeholders,
+    module globals it reads given in ``extra``)."""
     tree = ast.parse(Path(path).read_text(), filename=str(path))
     for node in tree.body:
         if isinstance(node, ast.ClassDef) and node.name == class_name:
             for item in node.body:
                 if isinstance(item, ast.FunctionDef) and item.name == name:
-                    item.decorator_list = []
-                    mod = ast.Module(body=[item], type_ignores=[])
-                    ns = {"np": np, "Ac": object, "Af": object, "uniform": random.uniform}
-                    exec(compile(mod, str(path), "exec"), ns)
-                    return ns[name]
+                    return _compile_def(path, item, extra)
     raise LookupError(f"{class_name}.{name} not found in {path}")
+
+
+def _reference_function(path, name, extra=None):
+    """Module-level function ``name`` of the reference source file ``path``."""
+    tree = ast.parse(Path(path).read_text(), filename=str(path))
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name == name:
+            return _compile_def(path, node, extra)
+    raise LookupError(f"{name} not found in {path}")
 
 
 def _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0, deltat_max, cfl_coef,
@@ -352,13 +390,60 @@ def make_ns2d(mods, oper: OperNumpy2D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
     return sim
 
 
+class _ForcingStandIn:
+    """``sim.forcing`` (``fluidsim/base/forcing/base.py:143-150,194-195``):
+    ``compute()`` at most once per time, ``get_forcing()`` the maker's
+    ``forcing_fft``."""
+
+    def __init__(self, sim, maker):
+        self.sim = sim
+        self.forcing_maker = maker
+        self._t_last_computed = -np.inf
+
+    def compute(self):
+        time = self.sim.time_stepping.t
+        if time > self._t_last_computed:
+            self.forcing_maker.compute()
+            self._t_last_computed = time
+
+    def get_forcing(self):
+        return self.forcing_maker.forcing_fft
+
+
+def _params_oper_class(mods):
+    """The numpy operator constructed from ``params`` as fluidsim constructs
+    its operators (the forcing makers build their coarse operator with
+    ``sim.oper.__class__(params=...)``), carrying the reference's coarse-grid
+    methods and fluidfft's ``deltak`` (the largest deltak_i)."""
+
+    class OperNumpy3DFromParams(OperNumpy3D):
+        def __init__(self, params):
+            po = params.oper
+            super().__init__(po.nx, po.ny, po.nz, po.Lx, po.Ly, po.Lz,
+                             coef_dealiasing=po.coef_dealiasing)
+            self.deltak = max(self.deltakx, self.deltaky, self.deltakz)
+
+    for name in ("project_fft_on_realX", "coarse_seq_from_fft_loc",
+                 "put_coarse_array_in_array_fft"):
+        setattr(OperNumpy3DFromParams, name, mods[name])
+    return OperNumpy3DFromParams
+
+
+_FORCING_CLASSES = {"tcrandom": "TimeCorrelatedRandomPseudoSpectral",
+                    "random": "RandomSimplePseudoSpectral", "proportional": "Proportional"}
+
+
 def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
               nu_m4=0.0, f=None, USE_CFL=False, deltat0=0.2, deltat_max=0.2,
               cfl_coef=None, smagorinsky_C=None, type_time_scheme="RK4",
-              projection=None, no_vz_kz0=False, N=None, bouss=False):
+              projection=None, no_vz_kz0=False, N=None, bouss=False, forcing=None):
     """A reference ns3d ``Simul`` wired around ``oper`` (with ``N`` given:
     the ns3d.strat ``Simul`` and ``StateNS3DStrat``; with ``bouss`` as well:
-    the ns3d.bouss ``Simul``, whose tendencies do not use N)."""
+    the ns3d.bouss ``Simul``, whose tendencies do not use N).  ``forcing``:
+    a dict (type, key_forced, nkmin_forcing, nkmax_forcing, forcing_rate,
+    time_correlation, which_root, only_positive) for the reference's own
+    forcing maker of that type, created after the time stepping (it reads
+    ``time_stepping.t``) and drawing from the global ``np.random``."""
     strat = N is not None
     Simul = (mods["ns3d_bouss_solver"] if bouss else
              mods["ns3d_strat_solver"] if strat else mods["ns3d_solver"]).Simul
@@ -369,6 +454,23 @@ def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
         extra["N"] = N
     sim.params = _params(nu_2, nu_4, nu_8, nu_m4, USE_CFL, deltat0,
                          deltat_max, cfl_coef, extra, type_time_scheme)
+    if forcing is not None:
+        sim.params.oper = _Container(
+            nx=oper.nx, ny=oper.ny, nz=oper.nz, Lx=oper.Lx, Ly=oper.Ly, Lz=oper.Lz,
+            type_fft="default", coef_dealiasing=oper.coef_dealiasing)
+        sim.params.output = _Container(HAS_TO_SAVE=False)
+        fc = forcing
+        sim.params.forcing = _Container(
+            enable=True, type=fc["type"], key_forced=fc["key_forced"],
+            nkmin_forcing=fc["nkmin_forcing"], nkmax_forcing=fc["nkmax_forcing"],
+            forcing_rate=fc["forcing_rate"],
+            normalized=_Container(type="2nd_degree_eq",
+                                  which_root=fc.get("which_root", "minabs"),
+                                  constant_rate_of=None),
+            random=_Container(only_positive=fc.get("only_positive", False)),
+            tcrandom=_Container(time_correlation=fc.get("time_correlation",
+                                                        "based_on_forcing_rate")))
+        oper = _params_oper_class(mods)(sim.params)
     if projection is not None or type_time_scheme.endswith("_random"):
         oper = copy.copy(oper)
         for name in ("project_toroidal", "project_poloidal"):
@@ -392,4 +494,8 @@ def make_ns3d(mods, oper: OperNumpy3D, nu_2=0.0, nu_4=0.0, nu_8=0.0,
         sim.is_turb_model_enabled = True
         sim.turb_model = mods["smagorinsky"].SmagorinskyModel(sim)
     sim.time_stepping = mods["ns3d_ts"].TimeSteppingPseudoSpectralNS3D(sim)
+    if forcing is not None:
+        Maker = getattr(mods["forcing_specific"], _FORCING_CLASSES[forcing["type"]])
+        sim.forcing = _ForcingStandIn(sim, Maker(sim))
+        sim.is_forcing_enabled = True
     return sim

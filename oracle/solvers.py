@@ -72,6 +72,10 @@ class _SolverBase:
         self.it = 0
         self.state_spect = np.zeros((self.nvar,) + oper.shapeK, np.complex128)
         self.state_phys = np.zeros((len(self.keys_phys),) + oper.shapeX)
+        # sim.forcing (oracle.forcing.CoarseForcingOracle), computed once per
+        # step after the CFL update (base.py:208-213)
+        self.forcing = None
+        self._forcing_fft = None
         if type_time_scheme.endswith("_random"):
             self._init_phaseshift_random(nb_pairs, nb_steps_compute_new_pair)
 
@@ -302,9 +306,11 @@ class _SolverBase:
         getattr(self, "time_step_" + self.type_time_scheme)()
 
     def one_time_step(self):
-        """``base.py:208-244`` without outputs, forcing or signals."""
+        """``base.py:208-244`` without outputs or signals."""
         if self.USE_CFL:
             self.compute_time_increment_CLF()
+        if self.forcing is not None:
+            self._forcing_fft = self.forcing.compute(self.state_spect, self.t, self.deltat)
         self.one_time_step_computation()
         self.t += self.deltat
         self.it += 1
@@ -578,6 +584,8 @@ class NS3DOracle(_SolverBase):
         F[0] = oper.fft(fx)
         F[1] = oper.fft(fy)
         F[2] = oper.fft(fz)
+        if self._forcing_fft is not None:  # ns3d/solver.py:243-244
+            F += self._forcing_fft
         if self.turb_model is not None:  # ns3d/solver.py:246-249
             F += self.turb_model(oper, vx_fft, vy_fft, vz_fft)
         self.project_state_spect(F)

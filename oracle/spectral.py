@@ -210,6 +210,17 @@ class OperNumpy3D:
             a.fill(value)
         return a
 
+    def create_arrayK_random(self, min_val=None, max_val=None):
+        """Uniform random complex array drawn with the global ``np.random``:
+        real parts, then imaginary parts, each scaled to ``[min_val,
+        max_val)`` (defaults 0 and 1).  fluidfft's method is not in the
+        reference; this definition is the oracle's and the GPU forcing's."""
+        lo = 0.0 if min_val is None else float(min_val)
+        hi = 1.0 if max_val is None else float(max_val)
+        re = lo + (hi - lo) * np.random.random(self.shapeK)
+        im = lo + (hi - lo) * np.random.random(self.shapeK)
+        return re + 1j * im
+
     # -- spectral operators ---------------------------------------------------
     def rotfft_from_vecfft(self, vx, vy, vz):
         out = np.empty((3,) + np.shape(vx), np.complex128)

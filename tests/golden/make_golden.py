@@ -27,6 +27,7 @@ from oracle import refshim  # noqa: E402
 from oracle.spectral import OperNumpy2D, OperNumpy3D  # noqa: E402
 from oracle.solvers import NS2DOracle, NS2DStratOracle, NS3DOracle, NS3DStratOracle  # noqa: E402
 from oracle.turb import smagorinsky_forcing  # noqa: E402
+from oracle.forcing import CoarseForcingOracle  # noqa: E402
 from fluidsim_gb300.init_fields import (  # noqa: E402
     isotropic_3d, noise_rot_2d, taylor_green_3d)
 
@@ -127,6 +128,32 @@ CASES_3D = [
          init="iso", seed=20, b_seed=21, steps=10),
 ]
 
+# coarse normalized forcings (the reference's forcing makers of
+# fluidsim/base/forcing/specific.py run through refshim); np_seed seeds the
+# global np.random before the forcing is created
+CASES_3D += [
+    dict(name="ns3d_tcrandom_32", nx=32, ny=32, nz=32, nu_2=1e-2, USE_CFL=True,
+         deltat0=0.2, deltat_max=0.2, cfl_coef=0.5, init="iso", seed=30, steps=10,
+         np_seed=31, forcing=dict(type="tcrandom", key_forced=["vx_fft", "vy_fft", "vz_fft"],
+                                  nkmin_forcing=2, nkmax_forcing=3, forcing_rate=0.3,
+                                  time_correlation=0.02)),
+    dict(name="ns3d_tcrandom_vx_24x32x16", nx=24, ny=32, nz=16, Lx=2 * pi, Ly=4 * pi,
+         Lz=pi, nu_2=5e-3, USE_CFL=False, deltat0=5e-3, init="iso", seed=32, steps=10,
+         np_seed=33, forcing=dict(type="tcrandom", key_forced="vx_fft", nkmin_forcing=1,
+                                  nkmax_forcing=2, forcing_rate=1.0)),
+    dict(name="ns3d_random_32", nx=32, ny=32, nz=32, nu_2=5e-3, USE_CFL=False,
+         deltat0=4e-3, init="iso", seed=34, steps=10, np_seed=35,
+         forcing=dict(type="random", key_forced=["vz_fft"], nkmin_forcing=3, nkmax_forcing=4,
+                      forcing_rate=0.5)),
+    dict(name="ns3d_proportional_32", nx=32, ny=32, nz=32, nu_2=5e-3, USE_CFL=False,
+         deltat0=4e-3, init="iso", seed=36, steps=10, np_seed=37,
+         forcing=dict(type="proportional", key_forced="vy_fft", nkmin_forcing=2,
+                      nkmax_forcing=4, forcing_rate=0.2)),
+]
+
+FORCING_CODES = {"tcrandom": 0, "random": 1, "proportional": 2}
+KEY_BITS = {"vx_fft": 1, "vy_fft": 2, "vz_fft": 4}
+
 PROJECTION_CODES = {None: 0, "toroidal": 1, "vortical": 1, "poloidal": 2}
 
 SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
@@ -135,25 +162,35 @@ SCHEME_CODES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phase
 
 
 class _PhaseRNG:
-    """The random phase schemes draw with the global ``random`` module; the
-    reference solver and the oracle each get the sequence of ``random.seed``
-    (``phase_seed``), kept apart while their steps alternate."""
+    """The random phase schemes draw with the global ``random`` module and the
+    forcings with the global ``np.random``; the reference solver and the
+    oracle each get the sequences of ``random.seed(phase_seed)`` and
+    ``np.random.seed(np_seed)``, kept apart while their steps alternate."""
 
-    def __init__(self, seed):
+    def __init__(self, seed, np_seed=None):
         self.states = {}
+        self.np_states = {}
         self.seed = seed
+        self.np_seed = np_seed
 
     def run(self, who, fn):
-        if self.seed is None:
-            return fn()
-        if who in self.states:
-            random.setstate(self.states[who])
-        else:
-            random.seed(self.seed)
+        if self.seed is not None:
+            if who in self.states:
+                random.setstate(self.states[who])
+            else:
+                random.seed(self.seed)
+        if self.np_seed is not None:
+            if who in self.np_states:
+                np.random.set_state(self.np_states[who])
+            else:
+                np.random.seed(self.np_seed)
         try:
             return fn()
         finally:
-            self.states[who] = random.getstate()
+            if self.seed is not None:
+                self.states[who] = random.getstate()
+            if self.np_seed is not None:
+                self.np_states[who] = np.random.get_state()
 
 
 def _kw(case, keys):
@@ -224,10 +261,11 @@ def run_3d(mods, case):
                     "deltat_max", "cfl_coef", "type_time_scheme"])
     proj = dict(projection=case.get("projection"), no_vz_kz0=case.get("no_vz_kz0", False))
     strat = case.get("N") is not None
-    rng = _PhaseRNG(case.get("phase_seed"))
+    rng = _PhaseRNG(case.get("phase_seed"), case.get("np_seed"))
     sim = rng.run("ref", lambda: refshim.make_ns3d(
         mods, oper, f=case.get("f"), smagorinsky_C=case.get("smagorinsky_C"),
-        N=case.get("N"), bouss=bool(case.get("bouss")), **proj, **kw))
+        N=case.get("N"), bouss=bool(case.get("bouss")), forcing=case.get("forcing"),
+        **proj, **kw))
     sim.state.init_from_vxvyvzfft(*[c.copy() for c in v0])
     if strat:  # a buoyancy field as well (set after the velocity round trip)
         b0 = isotropic_3d(nx, ny, nz, *L, seed=case["b_seed"])[0]
@@ -252,6 +290,8 @@ def run_3d(mods, case):
     if strat:
         orc.state_spect[3] = b0
         orc.statephys_from_statespect()
+    if case.get("forcing") is not None:
+        orc.forcing = rng.run("orc", lambda: oracle_forcing(orc, case["forcing"]))
     assert np.abs(orc.state_spect - S_init).max() <= 1e-15 * np.abs(S_init).max()
     np.testing.assert_allclose(orc.tendencies_nonlin(orc.state_spect), tend0,
                                rtol=0, atol=1e-13 * np.abs(tend0).max())
@@ -274,6 +314,17 @@ def run_3d(mods, case):
     return out
 
 
+def oracle_forcing(orc, fc):
+    """The oracle's restatement of the forcing maker ``fc`` describes."""
+    keys = fc["key_forced"]
+    keys = [keys] if isinstance(keys, str) else keys
+    names = ["vx_fft", "vy_fft", "vz_fft"]
+    return CoarseForcingOracle(
+        orc.oper, orc.nvar, [names.index(k) for k in keys], fc["type"],
+        fc["nkmin_forcing"], fc["nkmax_forcing"], fc["forcing_rate"],
+        fc.get("time_correlation", "based_on_forcing_rate"))
+
+
 def _params_array(case):
     keys = ["nx", "ny", "nz", "Lx", "Ly", "Lz", "nu_2", "nu_4", "nu_8", "nu_m4",
             "beta", "f", "USE_CFL", "deltat0", "deltat_max", "cfl_coef", "steps",
@@ -285,6 +336,19 @@ def _params_array(case):
                                  dtype=np.float64)
     out["p_projection"] = np.asarray(PROJECTION_CODES[case.get("projection")], dtype=np.float64)
     out["p_no_vz_kz0"] = np.asarray(float(case.get("no_vz_kz0", False)))
+    fc = case.get("forcing")
+    if fc is not None:
+        keys = fc["key_forced"]
+        keys = [keys] if isinstance(keys, str) else keys
+        tc = fc.get("time_correlation", "based_on_forcing_rate")
+        for k, v in {"forcing_type": FORCING_CODES[fc["type"]],
+                     "forced_keys": sum(KEY_BITS[k] for k in keys),
+                     "nkmin_forcing": fc["nkmin_forcing"],
+                     "nkmax_forcing": fc["nkmax_forcing"],
+                     "forcing_rate": fc["forcing_rate"],
+                     "time_correlation": np.nan if tc == "based_on_forcing_rate" else tc,
+                     "np_seed": case["np_seed"]}.items():
+            out["p_" + k] = np.asarray(v, dtype=np.float64)
     return out
 
 

@@ -14,6 +14,11 @@ CASES_3D = ["ns3d_20x15x10", "ns3d_tgv_32", "ns3d_iso_24x16x32_f", "ns3d_smag_20
             "ns3d_toroidal_24x20x16", "ns3d_poloidal_32_novz", "ns3d_strat_64x32x32",
             "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f", "ns3d_eulerpsr_32",
             "ns3d_bouss_32x32x64"]
+CASES_FORCING = ["ns3d_tcrandom_32", "ns3d_tcrandom_vx_24x32x16", "ns3d_random_32",
+                 "ns3d_proportional_32"]
+CASES_3D = CASES_3D + CASES_FORCING
+FORCING_TYPES = {0: "tcrandom", 1: "random", 2: "proportional"}
+KEY_NAMES = ("vx_fft", "vy_fft", "vz_fft")
 PROJECTIONS = {0: None, 1: "toroidal", 2: "poloidal"}
 SCHEME_NAMES = {0: "RK4", 1: "Euler", 2: "RK2", 3: "RK2_trapezoid", 4: "Euler_phaseshift",
                 5: "RK2_phaseshift", 6: "RK2_phaseshift_exact", 7: "Euler_phaseshift_random",
@@ -52,3 +57,18 @@ def solver_kwargs(p):
 def lengths(p, ndim):
     keys = ("Lx", "Ly", "Lz")[:ndim]
     return tuple(p.get(k) if p.get(k) is not None else 2 * math.pi for k in keys)
+
+
+def forcing_config(p):
+    """(type, keys, nkmin, nkmax, rate, time_correlation, np_seed) of a forcing
+    fixture, or None."""
+    if p.get("forcing_type") is None:
+        return None
+    bits = int(p["forced_keys"])
+    keys = [k for i, k in enumerate(KEY_NAMES) if bits & (1 << i)]
+    tc = p.get("time_correlation")
+    return {"type": FORCING_TYPES[int(p["forcing_type"])], "key_forced": keys,
+            "nkmin_forcing": p["nkmin_forcing"], "nkmax_forcing": p["nkmax_forcing"],
+            "forcing_rate": p["forcing_rate"],
+            "time_correlation": "based_on_forcing_rate" if tc is None else tc,
+            "np_seed": int(p["np_seed"])}

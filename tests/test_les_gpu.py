@@ -15,10 +15,13 @@ def test_forcing_injects_the_requested_power(cuda):
     for _ in range(3):
         ts.one_time_step()
     sim.forcing.compute()
-    assert abs(sim.forcing.injection_rate() - 1.0) < 1e-4
-    # the forced modes are the only ones the forcing touches, and it is solenoidal
-    f = sim.forcing.dense.cpu().numpy()
-    assert np.count_nonzero(np.abs(f).sum(0)) == len(sim.forcing.flat)
+    # each forced component injects forcing_rate (1/3) at the current state
+    for p in sim.forcing.injection_rate():
+        assert abs(p - 1.0 / 3) < 1e-10
+    # the coarse forced modes carry the forcing (the others only the round-off
+    # of the coarse fft(ifft(.)) projection on real fields)
+    f = np.abs(sim.forcing.forcing_fft.cpu().numpy()).sum(0)
+    assert np.count_nonzero(f > 1e-10 * f.max()) == sim.forcing.nb_forced_modes
 
 
 def test_pipeline_small_grid(cuda):

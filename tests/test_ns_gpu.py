@@ -8,7 +8,8 @@ import random
 import numpy as np
 import pytest
 
-from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, scheme
+from golden_cases import (CASES_2D, CASES_3D, forcing_config, lengths, load, projection_kwargs,
+                          scheme)
 
 pytestmark = pytest.mark.gpu
 
@@ -60,6 +61,14 @@ def make_sim(name, precision="float64"):
     ts.it_end = int(p["steps"])
     if p.get("phase_seed") is not None:  # the random phase schemes draw with `random`
         random.seed(int(p["phase_seed"]))
+    fc = forcing_config(p)
+    if fc is not None:  # the reference's forcing maker, seeded as the fixture's run
+        pf = params.forcing
+        pf.enable, pf.type, pf.key_forced = True, fc["type"], fc["key_forced"]
+        pf.nkmin_forcing, pf.nkmax_forcing = fc["nkmin_forcing"], fc["nkmax_forcing"]
+        pf.forcing_rate = fc["forcing_rate"]
+        pf.tcrandom.time_correlation = fc["time_correlation"]
+        pf.seed = fc["np_seed"]
     sim = Simul(params)
     sim.state.init_statespect_from(**{k: torch.from_numpy(d["S_init"][i])
                                       for i, k in enumerate(sim.state.keys_state_spect)})
@@ -108,7 +117,7 @@ def test_ten_steps_fp64(cuda, name):
                                   "ns2d_40x32_rk2", "ns3d_heun_24x16x32_f", "ns2d_32_rk2ps",
                                   "ns3d_eulerps_32", "ns3d_rk2psx_16x24x32_f",
                                   "ns3d_strat_64_f_rk2", "ns3d_rk2psr_24x16x32_f",
-                                  "ns2d_32_eulerpsr", "ns2d_strat_64_rk2"])
+                                  "ns2d_32_eulerpsr", "ns2d_strat_64_rk2", "ns3d_tcrandom_32"])
 def test_ten_steps_fp32(cuda, name):
     sim, d, p = make_sim(name, "float32")
     sim.time_stepping.start()

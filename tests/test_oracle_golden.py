@@ -10,7 +10,9 @@ import random
 import numpy as np
 import pytest
 
-from golden_cases import CASES_2D, CASES_3D, lengths, load, projection_kwargs, solver_kwargs
+from golden_cases import (CASES_2D, CASES_3D, KEY_NAMES, forcing_config, lengths, load,
+                          projection_kwargs, solver_kwargs)
+from oracle.forcing import CoarseForcingOracle
 from oracle.spectral import OperNumpy2D, OperNumpy3D
 from oracle.solvers import NS2DOracle, NS2DStratOracle, NS3DOracle, NS3DStratOracle
 from oracle.turb import smagorinsky_forcing
@@ -42,6 +44,13 @@ def make_oracle(name):
                              **solver_kwargs(p))
     orc.state_spect[:] = d["S_init"]
     orc.state_phys[:] = d["phys_init"]
+    fc = forcing_config(p)
+    if fc is not None:  # drawn from np.random seeded as the reference run was
+        np.random.seed(fc["np_seed"])
+        orc.forcing = CoarseForcingOracle(
+            orc.oper, orc.nvar, [KEY_NAMES.index(k) for k in fc["key_forced"]], fc["type"],
+            fc["nkmin_forcing"], fc["nkmax_forcing"], fc["forcing_rate"],
+            fc["time_correlation"])
     return orc, d, p
 
 
