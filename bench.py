@@ -432,6 +432,36 @@ def fft_throughput(n, reps=20):
     return out
 
 
+MLP_FLOPS_PER_POINT = 2 * (9 * 64 + 64 * 64 + 64 * 6)  # 9 -> 64 -> 64 -> 6 network
+
+
+def mlp_throughput(n_points=128**3, reps=20):
+    """The learned closure's 9 -> 64 -> 64 -> 6 network (BF16 tensor-core
+    MMAs, FP32 accumulation) on n_points gradient tensors through
+    gbs_mlp_forward, the evaluation the 128^3 LES runs four times a step."""
+    import torch
+    from fluidsim_gb300.closure import ClosureMLP, predict
+    net = ClosureMLP(seed=0)
+    G = torch.randn((9, n_points), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        predict(net, G)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        predict(net, G)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / reps
+    alg = MLP_FLOPS_PER_POINT * n_points
+    return {"points": n_points, "ms": ms, "alg_flops": alg,
+            "alg_tflops": alg / ms / 1e9,
+            "tensor_flops_issued": 3 * 2 * n_points * (16 * 64 + 64 * 64 + 64 * 8),
+            "bytes": n_points * 15 * 4, "hbm_gbs": n_points * 15 * 4 / ms / 1e6,
+            "note": "mma.sync m16n8k16 BF16 x FP32-accumulate; activations as 3 BF16 "
+                    "terms (3 MMAs per tile), weights exact BF16"}
+
+
 def rel_l2(a, b):
     return max(float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(len(b)))
 
@@ -538,6 +568,7 @@ def main():
 
     if not args.no_fft and args.ny is None and args.nz is None:
         line["fft"] = fft_throughput(n)
+        line["mlp_closure"] = mlp_throughput()
 
     if not args.no_fp64:
         sim32 = make_sim(n, "float32", v0)

@@ -23,6 +23,7 @@
 #include "gbs_internal.cuh"
 #include "gbs_turb.h"
 #include "gbs_mlp_eval.cuh"
+#include "gbs_mlp_mma.cuh"
 
 namespace gbs {
 
@@ -251,22 +252,15 @@ __global__ void k_adam(float* __restrict__ master, float* __restrict__ m, float*
   else if (p >= kOffW3 && p < kOffB3) W3[p - kOffW3] = __float2bfloat16(w);
 }
 
-// inference on SoA fields (float), gbs_mlp_eval.cuh
+// inference on SoA fields (float): tensor-core tiles of 16 points per warp
+// (gbs_mlp_mma.cuh)
 __global__ void __launch_bounds__(256)
 k_mlp_forward(MLPWeights w, const float* __restrict__ g, int64_t ld, float* __restrict__ tau,
               int64_t n) {
-  __shared__ MLPShared sm;
-  mlp_stage(sm, w);
+  __shared__ MMAShared sm;
+  mma_stage(sm, w);
   __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float x[kIn], y[kOut];
-#pragma unroll
-    for (int c = 0; c < kIn; ++c) x[c] = g[c * ld + i];
-    mlp_eval(sm, x, y);
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) tau[o * ld + i] = y[o];
-  }
+  mma_eval_all<float, float>(sm, g, tau, ld, n);
 }
 
 static MLPWeights to_w(const gbs_mlp_weights* p) {
@@ -300,8 +294,8 @@ int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float*
   }
   if (n == 0) return GBS_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int64_t nb = (n + 255) / 256;
-  if (nb > 152 * 16) nb = 152 * 16;
+  int64_t nb = (n + 127) / 128;  // 8 warps of 16 points
+  if (nb > 152 * 8) nb = 152 * 8;
   gbs::k_mlp_forward<<<(int)nb, 256, 0, st>>>(gbs::to_w(w), g, ld, tau, n);
   GBS_CHECK_LAUNCH();
   return GBS_OK;

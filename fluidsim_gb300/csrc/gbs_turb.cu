@@ -18,7 +18,7 @@
 
 #include "gbs_internal.cuh"
 #include "gbs_turb.h"
-#include "gbs_mlp_eval.cuh"
+#include "gbs_mlp_mma.cuh"
 
 namespace gbs {
 
@@ -76,24 +76,16 @@ __global__ void k_smagorinsky(const T* __restrict__ g, T* __restrict__ tau, int6
   }
 }
 
-// Pointwise MLP 9 -> 64 -> 64 -> 6 (tanh), BF16 weights staged in shared
-// memory as float, FP32 accumulation (gbs_mlp_eval.cuh).  One point per
-// thread.
+// Pointwise MLP 9 -> 64 -> 64 -> 6 (tanh), BF16 weights, FP32 accumulation,
+// on the tensor cores: each warp evaluates tiles of 16 points with
+// mma.sync m16n8k16 (gbs_mlp_mma.cuh).
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mlp_closure(const T* __restrict__ g, T* __restrict__ tau, int64_t n, MLPWeights w) {
-  __shared__ MLPShared sm;
-  mlp_stage(sm, w);
+  __shared__ MMAShared sm;
+  mma_stage(sm, w);
   __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float x[kIn], y[kOut];
-#pragma unroll
-    for (int c = 0; c < kIn; ++c) x[c] = (float)g[i + c * n];
-    mlp_eval(sm, x, y);
-#pragma unroll
-    for (int o = 0; o < kOut; ++o) tau[i + o * n] = T(y[o]);
-  }
+  mma_eval_all<T, T>(sm, g, tau, n, n);
 }
 
 // f_i = coef * 1j * sum_j K_j t_hat_{ij}
@@ -144,8 +136,10 @@ int turb_forcing(const TurbCtx& t, const void* S, void* out, const void* extra,
     k_smagorinsky<T><<<grid_for(nX), 256, 0, st>>>(static_cast<const T*>(t.Gx),
                                                    static_cast<T*>(t.Tx), nX, T(t.C_nu_T));
   } else {
-    k_mlp_closure<T><<<grid_for(nX), 256, 0, st>>>(static_cast<const T*>(t.Gx),
-                                                   static_cast<T*>(t.Tx), nX, t.w);
+    int64_t nb = (nX + 127) / 128;  // 8 warps of 16 points
+    if (nb > 152 * 8) nb = 152 * 8;
+    k_mlp_closure<T><<<(int)nb, 256, 0, st>>>(static_cast<const T*>(t.Gx),
+                                             static_cast<T*>(t.Tx), nX, t.w);
   }
   GBS_CHECK_LAUNCH();
   rc = gbs_fft_r2c(t.plan6, t.Tx, t.Tk, st);

@@ -157,9 +157,9 @@ class CoarseForcing3D:
         self._fft = None
         self.min_val = None if pf.random.only_positive else -1
 
+        if getattr(pf, "seed", None) is not None:
+            np.random.seed(pf.seed)
         if self.type == "tcrandom":
-            if getattr(pf, "seed", None) is not None:
-                np.random.seed(pf.seed)
             self.t_last_change = sim.time_stepping.t
             self._seed0 = np.random.randint(0, 2**31)
             self._seed1 = np.random.randint(0, 2**31)

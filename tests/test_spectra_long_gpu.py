@@ -64,6 +64,7 @@ def long_run_ns2d(n=128, nu_2=5e-4, t_end=20.0, t_avg=10.0, every=0.5, seed=3,
         p = SimulNS2D.create_default_params()
         p.precision = prec
         p.oper.nx = p.oper.ny = n
+        p.oper.Lx = p.oper.Ly = 2 * pi  # the ns2d default box is 8 x 8
         p.nu_2 = nu_2
         ts = p.time_stepping
         ts.USE_CFL, ts.cfl_coef, ts.deltat0, ts.deltat_max = True, 0.5, 0.01, 0.05
@@ -108,15 +109,20 @@ def long_run_ns2d(n=128, nu_2=5e-4, t_end=20.0, t_avg=10.0, every=0.5, seed=3,
 
 
 def test_long_run_spectra_match_oracle_after_decorrelation(cuda):
+    """128^2, nu_2 = 5e-4, CFL 0.5, to t = 20 (about 4000 steps).  FP64 keeps
+    pointwise parity with the oracle (round-off amplified by the chaos:
+    ~2e-11 at t = 20); the FP32 run has decorrelated (~0.2 pointwise at
+    t = 20) while E(t), Z(t) and the octave bands of the time-averaged E(k)
+    and Z(k) over t in [10, 20] stay within 1e-4, 0.5 % and 0.5 % of the
+    oracle's (measured on GB300; the bounds below leave a factor ~10)."""
     out = long_run_ns2d()
-    for prec in ("float64", "float32"):
-        r = out[prec]
-        # E and Z stay within 2 % and every octave band of the time-averaged
-        # E(k) and Z(k) within 10 %, whether or not the run has decorrelated
-        assert r["E_max_rel_diff"] < 0.02, r["E_max_rel_diff"]
-        assert r["Z_max_rel_diff"] < 0.02, r["Z_max_rel_diff"]
-        assert max(r["Ek_bands_rel_diff"]) < 0.10, r["Ek_bands_rel_diff"]
-        assert max(r["Zk_bands_rel_diff"]) < 0.10, r["Zk_bands_rel_diff"]
-    # the FP32 run is chaotic: its final field differs from the oracle's at
-    # order one, so agreement above is statistical, not pointwise
-    assert out["float32"]["pointwise_rel_l2_end"] > 0.1
+    r = out["float64"]
+    assert r["pointwise_rel_l2_end"] < 1e-9, r["pointwise_rel_l2_end"]
+    assert r["E_max_rel_diff"] < 1e-12 and r["Z_max_rel_diff"] < 1e-10
+    assert max(r["Ek_bands_rel_diff"] + r["Zk_bands_rel_diff"]) < 1e-10
+    r = out["float32"]
+    assert r["pointwise_rel_l2_end"] > 0.05, r["pointwise_rel_l2_end"]  # decorrelated
+    assert r["E_max_rel_diff"] < 1e-3, r["E_max_rel_diff"]
+    assert r["Z_max_rel_diff"] < 0.02, r["Z_max_rel_diff"]
+    assert max(r["Ek_bands_rel_diff"]) < 0.05, r["Ek_bands_rel_diff"]
+    assert max(r["Zk_bands_rel_diff"]) < 0.05, r["Zk_bands_rel_diff"]
