@@ -16,10 +16,12 @@ GBS_EINVAL = -22
 GBS_ENOMEM = -12
 GBS_ECUDA = -5
 GBS_ENAN = -33
+GBS_ETIMEDOUT = -110
 GBS_F32 = 0
 GBS_F64 = 1
 GBS_STEP_CHECK_NAN = 1
 GBS_STEP_DEALIASED = 2
+GBS_STEP_TEST_STALL = 64
 
 EXPORTED = (
     "gbs_last_error", "gbs_version", "gbs_fft_plan_create",
@@ -36,6 +38,7 @@ EXPORTED = (
     "gbs_ens2d_mixed_set_tuning",
     "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection", "gbs_ns_set_phase_shifts",
     "gbs_spectra_sizes", "gbs_spectra", "gbs_forcing_coarse",
+    "gbs_ens2d_persistent_step", "gbs_ens2d_persistent_status",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
            "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
@@ -137,6 +140,10 @@ def _declare(lib):
         "gbs_ens2d_mixed_destroy": (ctypes.c_int, [P]),
         "gbs_ens2d_mixed_set_tuning": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int,
                                                       ctypes.c_int]),
+        "gbs_ens2d_persistent_step": (ctypes.c_int, [P, ctypes.POINTER(P), ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_double,
+                                                     ctypes.c_int, P]),
+        "gbs_ens2d_persistent_status": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
         "gbs_ens2d_mixed_step": (ctypes.c_int, [P, ctypes.POINTER(P), ctypes.c_int,
                                                 ctypes.c_int, P]),
         "gbs_spectral_resample": (ctypes.c_int, [I64P, I64P, ctypes.c_int, DP,

@@ -7,6 +7,9 @@
 // precision); single runs and float64 go through gbs_ns.
 #include <new>
 
+// The persistent step below runs the ns2d pass bodies on fields that other
+// CTAs write during the same launch: no read-only (non-coherent) loads.
+#define GBS_NS2D_RESTRICT
 #include "gbs_fast_launch.cuh"
 #include "gbs_internal.cuh"
 
@@ -216,6 +219,161 @@ template <int TH> static int mixC(const MixArgs& m, int ncta, cudaStream_t st) {
   return GBS_OK;
 }
 
+// ------------------------------------------- one persistent launch per call
+// Every CTA of one cooperative launch takes work items from a queue (an
+// atomic ticket) in the order (RK stage, pass, group, run, tile) and runs
+// the pass body of the item.  Dependencies are per run: the x pass of a run
+// waits until all inverse-y tiles of that run (this stage) are done, the
+// forward-y pass until all its x rows are done, and the inverse-y pass of
+// the next stage until all forward-y tiles of the previous one are done (the
+// next stage reads tmp1 and overwrites W, which those tiles used).  A wait
+// only ever targets items earlier in the queue, all taken by resident CTAs
+// (cooperative launch), so it ends; each wait is bounded by timeout_ns all
+// the same, after which the CTA writes an error status word and every CTA
+// leaves at its next wait or ticket.
+struct PersistArgs {
+  MixGroup grp[kMixMax];
+  int ngroups;
+  int nstages;            // 4 per RK4 step
+  int runs[kMixMax];      // runs per group
+  int run_base[kMixMax];  // first run of the group in the counters
+  int64_t nA, nB, nC;     // items per stage of each pass (all groups)
+  unsigned* ticket;       // queue position (zeroed before the launch)
+  unsigned* done;         // per run: completed A, B, C items (zeroed)
+  int* status;            // 0, or kPersistTimeout
+  unsigned long long timeout_ns;
+  int stall_test;         // test hook: one dependency needs an item too many
+};
+
+constexpr int kPersistTimeout = 1;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Thread 0 of a CTA: wait until *p >= target, another CTA failed, or the
+// time limit passed.  Returns false on failure (the status word is set).
+__device__ bool wait_count(const unsigned* p, unsigned target, int* status,
+                           unsigned long long timeout_ns) {
+  const unsigned long long t0 = globaltimer_ns();
+  for (;;) {
+    if (ld_acquire(p) >= target) return true;
+    if (*(volatile int*)status) return false;
+    if (globaltimer_ns() - t0 > timeout_ns) {
+      atomicCAS(status, 0, kPersistTimeout);
+      return false;
+    }
+    __nanosleep(100);
+  }
+}
+
+// Group of item `local` within a pass block (groups in order, `per` items
+// per run of each group).
+__device__ __forceinline__ int persist_group(const PersistArgs& p, int pass, int64_t& local) {
+  for (int k = 0; k < p.ngroups; ++k) {
+    const MixGroup& G = p.grp[k];
+    const int per = pass == 0 ? G.ctaA : (pass == 1 ? G.ctaB : G.ctaC);
+    const int64_t n = (int64_t)per * p.runs[k];
+    if (local < n) return k;
+    local -= n;
+  }
+  return p.ngroups - 1;
+}
+
+template <int TH>
+__global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_constant__ PersistArgs p) {
+  __shared__ int64_t s_item;
+  __shared__ int s_fail;
+  const int64_t per_stage = p.nA + p.nB + p.nC;
+  const int64_t total = per_stage * p.nstages;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = *(volatile int*)p.status ? total : (int64_t)atomicAdd(p.ticket, 1u);
+      s_fail = 0;
+    }
+    __syncthreads();
+    const int64_t t = s_item;
+    if (t >= total) break;
+    const int sigma = (int)(t / per_stage);  // stage of the launch
+    int64_t r = t % per_stage;
+    const int pass = r < p.nA ? 0 : (r < p.nA + p.nB ? 1 : 2);
+    r -= pass == 0 ? 0 : (pass == 1 ? p.nA : p.nA + p.nB);
+    const int gi = persist_group(p, pass, r);
+    const MixGroup& G = p.grp[gi];
+    const int per = pass == 0 ? G.ctaA : (pass == 1 ? G.ctaB : G.ctaC);
+    const int run = (int)(r / per), tile = (int)(r % per);
+    unsigned* cnt = p.done + 3 * (int64_t)(p.run_base[gi] + run);
+    if (threadIdx.x == 0) {
+      unsigned target = 0;
+      const unsigned* q = cnt;
+      if (pass == 0) {
+        q = cnt + 2;
+        target = (unsigned)sigma * G.ctaC;
+      } else if (pass == 1) {
+        q = cnt;
+        target = (unsigned)(sigma + 1) * G.ctaA;
+        if (p.stall_test && sigma == 0 && gi == 0 && run == 0) target += 1;
+      } else {
+        q = cnt + 1;
+        target = (unsigned)(sigma + 1) * G.ctaB;
+      }
+      if (target > 0 && !wait_count(q, target, p.status, p.timeout_ns)) s_fail = 1;
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_fail) break;
+    const int mode = kRK0 + (sigma & 3);
+    RKArgs a = G.a;
+    const float2* in = static_cast<const float2*>(mode == kRK0 ? a.S : a.tmp1);
+    if (pass == 0) {
+      const uint3 b = make_uint3(tile, 0, run);
+      float2* W = static_cast<float2*>(G.W);
+      const float2* tw = static_cast<const float2*>(G.twy);
+      switch (G.logy) {
+        case 6: kf2_inv_y_body<float, 6, MixTX<TH, 6>::v, false>(in, W, G.g, tw, b); break;
+        case 7: kf2_inv_y_body<float, 7, MixTX<TH, 7>::v, false>(in, W, G.g, tw, b); break;
+        case 8: kf2_inv_y_body<float, 8, MixTX<TH, 8>::v, false>(in, W, G.g, tw, b); break;
+        default: kf2_inv_y_body<float, 9, MixTX<TH, 9>::v, false>(in, W, G.g, tw, b); break;
+      }
+    } else if (pass == 1) {
+      const uint3 b = make_uint3(tile, run, 0);
+      const float2* W = static_cast<const float2*>(G.W);
+      float2* F = static_cast<float2*>(G.F);
+      const float2* tw = static_cast<const float2*>(G.twx);
+      switch (G.logm) {
+        case 5: kf2_x_any<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
+        case 6: kf2_x_any<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
+        case 7: kf2_x_any<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
+        case 8: kf2_x_any<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
+        default: kf2_x_any<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
+      }
+    } else {
+      const uint3 b = make_uint3(tile, 0, run);
+      const float2* F = static_cast<const float2*>(G.F);
+      const float2* tw = static_cast<const float2*>(G.twy);
+      switch (G.logy) {
+        case 6: kf2_fwd_y_body<float, 6, MixTX<TH, 6>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+        case 7: kf2_fwd_y_body<float, 7, MixTX<TH, 7>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+        case 8: kf2_fwd_y_body<float, 8, MixTX<TH, 8>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+        default: kf2_fwd_y_body<float, 9, MixTX<TH, 9>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+      }
+    }
+    __syncthreads();  // the item's writes are done (and its shared memory free)
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(cnt + pass, 1u);
+    }
+  }
+}
+
 }  // namespace fast
 
 struct Ensemble {
@@ -266,6 +424,8 @@ struct EnsembleMix {
   Ensemble* e[fast::kMixMax];
   int n;
   int thA, thB, thC;  // threads per CTA of the inverse, x and forward passes
+  unsigned* pbuf;     // persistent step: ticket, per-run counters, status
+  int nruns_total;
 };
 
 // every group's tiles at these thread counts: columns 4..64 wide, >= 1 row
@@ -325,6 +485,68 @@ static int mix_eval(EnsembleMix* x, void* const* states, int mode, bool pr, cuda
   return rc;
 }
 
+template <int TH>
+static int persist_launch(EnsembleMix* x, void* const* states, int nsteps,
+                          double timeout_s, bool stall_test, cudaStream_t st) {
+  fast::PersistArgs p;
+  memset(&p, 0, sizeof(p));
+  p.ngroups = x->n;
+  p.nstages = 4 * nsteps;
+  int rb = 0;
+  for (int k = 0; k < x->n; ++k) {
+    Ensemble* e = x->e[k];
+    fast::MixGroup& G = p.grp[k];
+    G.g = e->geo;
+    G.g.pr = 1;  // every stage of the launch starts from a dealiased state
+    G.g.ncx = G.g.kcx < G.g.nkx ? G.g.kcx : G.g.nkx;
+    G.W = e->W;
+    G.F = e->F;
+    G.twx = e->twx;
+    G.twy = e->twy;
+    G.a.S = states[k];
+    G.a.Sout = states[k];
+    G.a.tmp = e->tmp;
+    G.a.tmp1 = e->tmp1;
+    G.a.nan_flag = e->dflag;
+    G.pr = fast::PerRun{e->nu2, e->nu8, e->dt};
+    G.logy = ilog2(e->ny);
+    G.logm = ilog2(e->nx / 2);
+    G.ctaA = ceil_div(G.g.ncx, TH * 8 / e->ny);
+    G.ctaB = ceil_div(e->ny, 2 * TH / (e->nx / 2));
+    G.ctaC = G.ctaA;
+    p.runs[k] = e->nruns;
+    p.run_base[k] = rb;
+    rb += e->nruns;
+    p.nA += (int64_t)G.ctaA * e->nruns;
+    p.nB += (int64_t)G.ctaB * e->nruns;
+    p.nC += (int64_t)G.ctaC * e->nruns;
+  }
+  p.ticket = x->pbuf;
+  p.done = x->pbuf + 1;
+  p.status = reinterpret_cast<int*>(x->pbuf + 1 + 3 * (int64_t)rb);
+  p.timeout_ns = (unsigned long long)(timeout_s * 1e9);
+  p.stall_test = stall_test ? 1 : 0;
+  const size_t smem = (size_t)TH * 64;
+  int rc = fast::prep(fast::kpersist<TH>, smem);
+  if (rc) return rc;
+  int dev = 0, nsm = 0, per_sm = 0;
+  GBS_CUDA_TRY(cudaGetDevice(&dev));
+  GBS_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fast::kpersist<TH>, TH,
+                                                             smem));
+  if (per_sm < 1) {
+    set_error("ensemble persistent step: no CTA of %d threads fits on an SM", TH);
+    return GBS_EINVAL;
+  }
+  // the counters are zeroed except the status word, which keeps an earlier
+  // failure until gbs_ens2d_persistent_status reads it
+  GBS_CUDA_TRY(cudaMemsetAsync(x->pbuf, 0, sizeof(unsigned) * (1 + 3 * (size_t)rb), st));
+  void* args[] = {&p};
+  GBS_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)fast::kpersist<TH>, dim3(nsm * per_sm),
+                                           dim3(TH), args, smem, st));
+  return GBS_OK;
+}
+
 }  // namespace gbs
 
 struct gbs_ens2d_mixed {
@@ -357,6 +579,18 @@ int gbs_ens2d_mixed_create(gbs_ens2d* const* groups, int ngroups, gbs_ens2d_mixe
     gbs::set_error("gbs_ens2d_mixed_create: a group size has no single-launch tile");
     return GBS_EINVAL;
   }
+  int runs = 0;
+  for (int k = 0; k < ngroups; ++k) runs += h->x.e[k]->nruns;
+  h->x.nruns_total = runs;
+  const size_t pb = sizeof(unsigned) * (2 + 3 * (size_t)runs);
+  if (cudaMalloc(&h->x.pbuf, pb) != cudaSuccess ||
+      cudaMemset(h->x.pbuf, 0, pb) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+    (void)cudaGetLastError();
+    if (h->x.pbuf) cudaFree(h->x.pbuf);
+    delete h;
+    gbs::set_error("gbs_ens2d_mixed_create: device allocation failed");
+    return GBS_ENOMEM;
+  }
   *out = h;
   return GBS_OK;
 }
@@ -377,8 +611,51 @@ int gbs_ens2d_mixed_set_tuning(gbs_ens2d_mixed* h, int th_inverse, int th_x, int
 }
 
 int gbs_ens2d_mixed_destroy(gbs_ens2d_mixed* h) {
+  if (h && h->x.pbuf) cudaFree(h->x.pbuf);
   delete h;
   return GBS_OK;
+}
+
+// nsteps RK4 steps of every run of every group in one persistent cooperative
+// launch (after one ordinary step when the states are not known dealiased).
+int gbs_ens2d_persistent_step(gbs_ens2d_mixed* h, void* const* states, int nsteps,
+                              int threads, double timeout_s, int flags, void* stream) {
+  gbs::clear_error();
+  if (!h || !states || nsteps < 1 || (threads != 256 && threads != 512) ||
+      !(timeout_s > 0) || !gbs::mix_fits(&h->x, threads, threads, threads)) {
+    gbs::set_error("gbs_ens2d_persistent_step: invalid argument (threads 256 or 512 giving "
+                   "every group 4..64 columns and >= 1 row per CTA, timeout > 0)");
+    return GBS_EINVAL;
+  }
+  for (int k = 0; k < h->x.n; ++k) {
+    if (!states[k]) {
+      gbs::set_error("gbs_ens2d_persistent_step: null state");
+      return GBS_EINVAL;
+    }
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = GBS_OK;
+  if (!(flags & GBS_STEP_DEALIASED)) {  // first step from an arbitrary state
+    for (int m = gbs::kRK0; m <= gbs::kRK3 && !rc; ++m)
+      rc = gbs::mix_eval(&h->x, states, m, false, st);
+    if (rc || --nsteps == 0) return rc;
+  }
+  const bool stall = (flags & GBS_STEP_TEST_STALL) != 0;
+  if (threads == 256)
+    return gbs::persist_launch<256>(&h->x, states, nsteps, timeout_s, stall, st);
+  return gbs::persist_launch<512>(&h->x, states, nsteps, timeout_s, stall, st);
+}
+
+int gbs_ens2d_persistent_status(gbs_ens2d_mixed* h, int* status) {
+  gbs::clear_error();
+  if (!h || !status) {
+    gbs::set_error("gbs_ens2d_persistent_status: null argument");
+    return GBS_EINVAL;
+  }
+  int* d = reinterpret_cast<int*>(h->x.pbuf + 1 + 3 * (size_t)h->x.nruns_total);
+  GBS_CUDA_TRY(cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost));
+  GBS_CUDA_TRY(cudaMemset(d, 0, sizeof(int)));
+  return *status ? GBS_ETIMEDOUT : GBS_OK;
 }
 
 // nsteps RK4 steps of every run of every group; states[k]: the state of group

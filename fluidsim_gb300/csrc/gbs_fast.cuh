@@ -22,6 +22,14 @@ namespace fast {
 
 extern __shared__ __align__(16) unsigned char g_smem_fast[];
 
+// Pointer qualifier of the ns2d pass bodies' field arguments.  A translation
+// unit that runs the bodies inside one persistent launch, where the fields
+// are written and read again by other CTAs during the launch, defines it
+// empty so that no load goes through the non-coherent read-only path.
+#ifndef GBS_NS2D_RESTRICT
+#define GBS_NS2D_RESTRICT __restrict__
+#endif
+
 // min blocks per SM so that GBS_OCC_THREADS threads can be resident
 // (1536: <= 42 registers per thread; 1024: <= 64)
 #ifndef GBS_OCC_THREADS
@@ -944,9 +952,9 @@ kf3_fwd_z(const cplx<T>* __restrict__ F, Geo g, const cplx<T>* __restrict__ twz,
 // A: inverse y pass; fields ux, uy, d_x rot, d_y rot.  bid = (column tile,
 // -, run).
 template <typename T, int LOGN, int TX, bool PH>
-__device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* __restrict__ S,
-                                               cplx<T>* __restrict__ W, const Geo& g,
-                                               const cplx<T>* __restrict__ twy, uint3 bid) {
+__device__ __forceinline__ void kf2_inv_y_body(const cplx<T>* GBS_NS2D_RESTRICT S,
+                                               cplx<T>* GBS_NS2D_RESTRICT W, const Geo& g,
+                                               const cplx<T>* GBS_NS2D_RESTRICT twy, uint3 bid) {
   using C = cplx<T>;
   using P = Line<LOGN>;
   C* buf = reinterpret_cast<C*>(g_smem_fast);
@@ -1004,9 +1012,9 @@ kf2_inv_y(const cplx<T>* __restrict__ S, cplx<T>* __restrict__ W, Geo g,
 // tile, run, -).  ST (ns2d.strat, strat/solver.py:27-32): 6 fields, products
 // f_rot = -ux d_x rot - uy d_y rot and f_b = -ux d_x b - uy d_y b - N^2 uy.
 template <typename T, int LOGM, int L, bool ST = false>
-__device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
-                                           cplx<T>* __restrict__ F, const Geo& g,
-                                           const cplx<T>* __restrict__ twx,
+__device__ __forceinline__ void kf2_x_body(const cplx<T>* GBS_NS2D_RESTRICT W,
+                                           cplx<T>* GBS_NS2D_RESTRICT F, const Geo& g,
+                                           const cplx<T>* GBS_NS2D_RESTRICT twx,
                                            unsigned long long* vmax, uint3 bid) {
   constexpr int NF = ST ? 6 : 4, NFO = ST ? 2 : 1;
   using C = cplx<T>;
@@ -1104,9 +1112,9 @@ __device__ __forceinline__ void kf2_x_body(const cplx<T>* __restrict__ W,
 // CTA, N/8 threads per line, the same threads and shared memory as
 // kf2_x_body with L = 2 LP rows.
 template <typename T, int LOGN, int LP, bool ST = false>
-__device__ __forceinline__ void kf2_xp_body(const cplx<T>* __restrict__ W,
-                                            cplx<T>* __restrict__ F, const Geo& g,
-                                            const cplx<T>* __restrict__ twx,
+__device__ __forceinline__ void kf2_xp_body(const cplx<T>* GBS_NS2D_RESTRICT W,
+                                            cplx<T>* GBS_NS2D_RESTRICT F, const Geo& g,
+                                            const cplx<T>* GBS_NS2D_RESTRICT twx,
                                             unsigned long long* vmax, uint3 bid) {
   constexpr int NF = ST ? 6 : 4, NFO = ST ? 2 : 1;
   using C = cplx<T>;
@@ -1202,9 +1210,9 @@ __device__ __forceinline__ void kf2_xp_body(const cplx<T>* __restrict__ W,
 
 // The ns2d x pass for L rows per CTA: in pairs when L is even (FP32).
 template <typename T, int LOGM, int L, bool ST = false>
-__device__ __forceinline__ void kf2_x_any(const cplx<T>* __restrict__ W,
-                                          cplx<T>* __restrict__ F, const Geo& g,
-                                          const cplx<T>* __restrict__ twx,
+__device__ __forceinline__ void kf2_x_any(const cplx<T>* GBS_NS2D_RESTRICT W,
+                                          cplx<T>* GBS_NS2D_RESTRICT F, const Geo& g,
+                                          const cplx<T>* GBS_NS2D_RESTRICT twx,
                                           unsigned long long* vmax, uint3 bid) {
   if constexpr (sizeof(T) == 4 && L % 2 == 0)
     kf2_xp_body<T, LOGM + 1, L / 2, ST>(W, F, g, twx, vmax, bid);
@@ -1222,8 +1230,8 @@ kf2_x(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 // C: forward y pass + 1/N + dealiasing + RK4 stage (epilogue from registers).
 // bid = (column tile, -, run).
 template <typename T, int LOGN, int TX, bool EXT>
-__device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* __restrict__ F, Geo g,
-                                               const cplx<T>* __restrict__ twy, int mode,
+__device__ __forceinline__ void kf2_fwd_y_body(const cplx<T>* GBS_NS2D_RESTRICT F, Geo g,
+                                               const cplx<T>* GBS_NS2D_RESTRICT twy, int mode,
                                                RKArgs a, const PerRun& pr, uint3 bid) {
   using C = cplx<T>;
   using P = Line<LOGN>;

@@ -4,11 +4,15 @@ Runs of one size are advanced together by ``gbs_ens2d_step`` (one launch
 per pass for the whole group, per-run nu_2, nu_8 and dt).  The groups of
 different sizes either run on their own streams, or all together through
 ``gbs_ens2d_mixed_step``: one launch per pass covers every run of every
-size.  ``capture`` records ``steps_per_graph`` RK4 steps of every group
-into one CUDA graph; ``run`` replays it.  ``autotune`` times the compiled
-tile shapes of each group (column width of the y passes, rows per CTA of
-the x pass), keeps the fastest, then times the single-launch mode against
-the per-group streams and keeps the faster.
+size, or through ``gbs_ens2d_persistent_step``: all the steps of a call in
+one persistent cooperative launch whose CTAs take (stage, pass, group, run,
+tile) items from a device queue and wait, with a time limit, only on the
+items of their own run that they read.  ``capture`` records
+``steps_per_graph`` RK4 steps of every group into one CUDA graph; ``run``
+replays it.  ``autotune`` times the compiled tile shapes of each group
+(column width of the y passes, rows per CTA of the x pass), keeps the
+fastest, then times the three modes (per-group streams, one launch per
+pass, persistent) and keeps the fastest.
 
 ``python -m fluidsim_gb300.ensemble`` runs the 96-run configuration (32 each
 at 128^2, 256^2, 512^2, float32, 500 steps) and prints one JSON line with
@@ -90,6 +94,10 @@ class EnsembleNS2D:
         self._mix_states = (ctypes.c_void_p * len(order))(
             *[self.groups[k]["S"].data_ptr() for k in order])
         self.mixed = False
+        # persistent mode: all steps of a call in one cooperative launch
+        self.persistent = False
+        self.persist_threads = 512
+        self.persist_timeout_s = 1.0
 
     def __del__(self):
         if getattr(self, "_mix", None):
@@ -106,8 +114,14 @@ class EnsembleNS2D:
                                            _lib.GBS_STEP_DEALIASED,
                                            ctypes.c_void_p(stream.cuda_stream)), "ens2d_step")
 
-    def step(self, nsteps=1):
+    def step(self, nsteps=1, flags=_lib.GBS_STEP_DEALIASED):
         cur = torch.cuda.current_stream()
+        if self.persistent:
+            _lib.check(self.lib.gbs_ens2d_persistent_step(
+                self._mix, self._mix_states, nsteps, self.persist_threads,
+                self.persist_timeout_s, flags, ctypes.c_void_p(cur.cuda_stream)),
+                "ens2d_persistent_step")
+            return
         if self.mixed:
             _lib.check(self.lib.gbs_ens2d_mixed_step(self._mix, self._mix_states, nsteps,
                                                      _lib.GBS_STEP_DEALIASED,
@@ -164,12 +178,38 @@ class EnsembleNS2D:
                 best_mix = (ms, th)
         _lib.check(self.lib.gbs_ens2d_mixed_set_tuning(self._mix, *best_mix[1]))
         mode_ms["single_launch"] = best_mix[0]
-        self.mixed = mode_ms["single_launch"] < mode_ms["per_group_streams"]
+        self.mixed = False
+        self.persistent = True
+        best_p = None
+        for th in (256, 512):
+            self.persist_threads = th
+            try:
+                ms = time_all(steps)
+            except ValueError:  # a group has no tile at this thread count
+                continue
+            self.check_status()
+            if best_p is None or ms < best_p[0]:
+                best_p = (ms, th)
+        self.persistent = False
+        if best_p is not None:
+            self.persist_threads = best_p[1]
+            mode_ms["persistent"] = best_p[0]
+        mode = min(mode_ms, key=mode_ms.get)
+        self.mixed = mode == "single_launch"
+        self.persistent = mode == "persistent"
         table["all_groups_ms_per_step"] = mode_ms
         table["single_launch_threads"] = dict(zip(("inverse", "x", "forward"), best_mix[1]))
-        table["mode"] = "single_launch" if self.mixed else "per_group_streams"
+        table["persistent_threads"] = best_p[1] if best_p else None
+        table["mode"] = mode
         self.reset()
         return table
+
+    def check_status(self):
+        """Raise RuntimeError if a bounded wait of the persistent launch ran out
+        (the states are then undefined); clears the status word."""
+        st = ctypes.c_int()
+        _lib.check(self.lib.gbs_ens2d_persistent_status(self._mix, ctypes.byref(st)),
+                   "persistent ensemble step")
 
     def capture(self, steps_per_graph=10):
         torch.cuda.synchronize()
@@ -186,6 +226,7 @@ class EnsembleNS2D:
             self.graph.replay()
 
     def nan_flag(self):
+        self.check_status()
         flags = []
         for g in self.groups:
             f = ctypes.c_int()

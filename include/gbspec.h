@@ -32,6 +32,7 @@ extern "C" {
 #define GBS_ENOMEM (-12) /* device allocation failed (MemoryError)       */
 #define GBS_ECUDA (-5)   /* CUDA runtime error (RuntimeError)            */
 #define GBS_ENAN (-33)   /* NaN in the state after a step (ValueError)   */
+#define GBS_ETIMEDOUT (-110) /* a bounded device-side wait ran out (RuntimeError) */
 
 #define GBS_F32 0
 #define GBS_F64 1
@@ -283,6 +284,23 @@ int gbs_ens2d_mixed_set_tuning(gbs_ens2d_mixed* mixed, int th_inverse, int th_x,
                                int th_forward);
 int gbs_ens2d_mixed_step(gbs_ens2d_mixed* mixed, void* const* states, int nsteps, int flags,
                          void* stream);
+
+/* The same nsteps RK4 steps in ONE persistent cooperative launch (replaces
+ * the pass-by-pass launches of the batched form; fluidsim itself steps one
+ * run at a time, fluidsim/base/time_stepping/pseudo_spect.py:798-984).  The
+ * CTAs (`threads` each: 256 or 512) take work items from a device queue in
+ * the order (stage, pass, group, run, tile); each item first waits until
+ * the items of its own run that it reads are done (per-run counters, no
+ * grid-wide barrier).  Every wait gives up after timeout_s seconds: the
+ * launch then stops early, leaves the states undefined, and
+ * gbs_ens2d_persistent_status returns GBS_ETIMEDOUT with *status = 1 (and
+ * clears it).  Without GBS_STEP_DEALIASED the first step runs as
+ * gbs_ens2d_mixed_step.  GBS_STEP_TEST_STALL (test hook) makes one wait
+ * need an item that does not exist, so that it runs out. */
+#define GBS_STEP_TEST_STALL 64
+int gbs_ens2d_persistent_step(gbs_ens2d_mixed* mixed, void* const* states, int nsteps,
+                              int threads, double timeout_s, int flags, void* stream);
+int gbs_ens2d_persistent_status(gbs_ens2d_mixed* mixed, int* status);
 
 /* Filtered-DNS data for the learned closure (no reference counterpart):
  *   gbs_spectral_resample: nfields spectral fields of shape_in (nz, ny, nx)
