@@ -10,8 +10,8 @@
 // in_scale, then tanh outputs) are FP32 values carried as the sum of three
 // BF16 terms a = a0 + a1 + a2 (a0 = bf16(a), a1 = bf16(a - a0), a2 =
 // bf16(a - a0 - a1)), so each layer is three MMAs per tile whose FP32 sum
-// equals the FP32 product to within the FP32 accumulation error; the result
-// matches the FP32 FMA evaluation to ~1e-7 relative.
+// equals the FP32 product to within the FP32 accumulation error; with the
+// tanh below the result matches the FP32 evaluation to ~1e-7 relative.
 //
 // Fragment layouts (PTX ISA, mma.m16n8k16 .bf16, g = lane / 4, q = lane % 4):
 //   A (row-major 16 x 16): a0 = (g, 2q..2q+1), a1 = (g+8, 2q..), a2 = (g,
@@ -92,6 +92,13 @@ __device__ __forceinline__ void split3(float x, float y, uint32_t& p0, uint32_t&
   p2 = *reinterpret_cast<const uint32_t*>(&h2);
 }
 
+// tanh x = 1 - 2 / (exp(2x) + 1) with the hardware exponential and divide
+// intrinsics: absolute error ~1e-7 over the whole line (the activations feed
+// linear layers, where absolute errors are what count), +-1 in the limits.
+__device__ __forceinline__ float tanh_act(float x) {
+  return 1.f - __fdividef(2.f, __expf(2.f * x) + 1.f);
+}
+
 __device__ __forceinline__ uint32_t ld_b32(const __nv_bfloat16* p) {
   return *reinterpret_cast<const uint32_t*>(p);
 }
@@ -143,7 +150,7 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
 #pragma unroll
       for (int p = 0; p < 3; ++p) mma_bf16(c[h], A[p], b0, b1);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) c[h][e] = tanhf(c[h][e]);
+      for (int e = 0; e < 4; ++e) c[h][e] = tanh_act(c[h][e]);
     }
     split3(c[0][0], c[0][1], H[0][t][0], H[1][t][0], H[2][t][0]);
     split3(c[0][2], c[0][3], H[0][t][1], H[1][t][1], H[2][t][1]);
@@ -172,7 +179,7 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
         for (int p = 0; p < 3; ++p) mma_bf16(c[h], H[p][kt], b0, b1);
       }
 #pragma unroll
-      for (int e = 0; e < 4; ++e) c[h][e] = tanhf(c[h][e]);
+      for (int e = 0; e < 4; ++e) c[h][e] = tanh_act(c[h][e]);
     }
     uint32_t A3[3][4];
     split3(c[0][0], c[0][1], A3[0][0], A3[1][0], A3[2][0]);

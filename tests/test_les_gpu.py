@@ -16,8 +16,9 @@ def test_forcing_injects_the_requested_power(cuda):
         ts.one_time_step()
     sim.forcing.compute()
     # each forced component injects forcing_rate (1/3) at the current state
+    # (the LES solver runs in FP32: the forcing is stored in complex64)
     for p in sim.forcing.injection_rate():
-        assert abs(p - 1.0 / 3) < 1e-10
+        assert abs(p - 1.0 / 3) < 1e-6 / 3
     # the coarse forced modes carry the forcing (the others only the round-off
     # of the coarse fft(ifft(.)) projection on real fields)
     f = np.abs(sim.forcing.forcing_fft.cpu().numpy()).sum(0)
@@ -31,3 +32,8 @@ def test_pipeline_small_grid(cuda):
     assert out["train"]["rel_mse"] < 1.0
     for name in ("none", "smagorinsky", "learned"):
         assert np.isfinite(out["les"][name]["spectral_error"])
+    # what the trained network gains over the method without it: the LES
+    # energy spectrum is closer to the filtered DNS one with the learned
+    # closure than without any closure (on GB300: 5.25 against 5.84, the
+    # mean relative shell error; training and runs are deterministic)
+    assert out["les"]["learned"]["spectral_error"] < 0.95 * out["les"]["none"]["spectral_error"]
