@@ -33,8 +33,43 @@ template <> struct cvec<double> { using type = double2; };
 template <typename T> using cplx = typename cvec<T>::type;
 
 template <typename C> GBS_HD C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
-template <typename C> GBS_HD C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
-template <typename C> GBS_HD C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+
+// FP32 complex add / subtract as one packed instruction on the paired
+// registers (add.rn.f32x2 / sub.rn.f32x2, sm_100 and later): each component
+// is rounded exactly as by the scalar instruction, so results are unchanged
+// and the butterflies issue half the FP32 adds.  -DGBS_NO_F32X2 turns it off.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000) && !defined(GBS_NO_F32X2)
+#define GBS_F32X2 1
+__device__ __forceinline__ float2 f32x2_add(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
+        "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+__device__ __forceinline__ float2 f32x2_sub(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
+        "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return *reinterpret_cast<const float2*>(&d);
+}
+#endif
+
+template <typename C> GBS_HD C cadd(C a, C b) {
+#ifdef GBS_F32X2
+  if constexpr (sizeof(C) == 8) return f32x2_add(a, b);
+#endif
+  return mk<C>(a.x + b.x, a.y + b.y);
+}
+template <typename C> GBS_HD C csub(C a, C b) {
+#ifdef GBS_F32X2
+  if constexpr (sizeof(C) == 8) return f32x2_sub(a, b);
+#endif
+  return mk<C>(a.x - b.x, a.y - b.y);
+}
 template <typename C> GBS_HD C cmul(C a, C b) {
   return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
