@@ -453,8 +453,25 @@ def mlp_throughput(n_points=128**3, reps=20):
     ev[1].record()
     torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / reps
+    # one training gradient (forward + backward on the tensor cores, then the
+    # weight-gradient reduction) of a 65536-sample batch
+    from fluidsim_gb300.closure import ClosureTrainer
+    batch = 65536
+    tr = ClosureTrainer(net, batch=batch)
+    Tau = torch.randn((6, n_points), dtype=torch.float32, device="cuda")
+    idx = torch.randint(0, n_points, (batch,), device="cuda", dtype=torch.int64)
+    for _ in range(3):
+        tr.gradient(G, Tau, idx)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        tr.gradient(G, Tau, idx)
+    ev[1].record()
+    torch.cuda.synchronize()
+    grad_ms = ev[0].elapsed_time(ev[1]) / reps
     alg = MLP_FLOPS_PER_POINT * n_points
-    return {"points": n_points, "ms": ms, "alg_flops": alg,
+    return {"points": n_points, "ms": ms, "train_gradient_ms": grad_ms,
+            "train_batch": batch, "alg_flops": alg,
             "alg_tflops": alg / ms / 1e9,
             "tensor_flops_issued": 3 * 2 * n_points * (16 * 64 + 64 * 64 + 64 * 8),
             "bytes": n_points * 15 * 4, "hbm_gbs": n_points * 15 * 4 / ms / 1e6,

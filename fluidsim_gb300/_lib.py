@@ -39,6 +39,7 @@ EXPORTED = (
     "gbs_ns_is_dealiased", "gbs_ns_step", "gbs_ns_set_projection", "gbs_ns_set_phase_shifts",
     "gbs_spectra_sizes", "gbs_spectra", "gbs_forcing_coarse",
     "gbs_ens2d_persistent_step", "gbs_ens2d_persistent_status",
+    "gbs_ens2d_persistent_set_chunk",
 )
 SCHEMES = {"RK4": 0, "Euler": 1, "RK2": 2, "RK2_trapezoid": 3, "Euler_phaseshift": 4,
            "RK2_phaseshift": 5, "RK2_phaseshift_exact": 6, "Euler_phaseshift_random": 7,
@@ -144,6 +145,7 @@ def _declare(lib):
                                                      ctypes.c_int, ctypes.c_double,
                                                      ctypes.c_int, P]),
         "gbs_ens2d_persistent_status": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "gbs_ens2d_persistent_set_chunk": (ctypes.c_int, [P, ctypes.c_int]),
         "gbs_ens2d_mixed_step": (ctypes.c_int, [P, ctypes.POINTER(P), ctypes.c_int,
                                                 ctypes.c_int, P]),
         "gbs_spectral_resample": (ctypes.c_int, [I64P, I64P, ctypes.c_int, DP,

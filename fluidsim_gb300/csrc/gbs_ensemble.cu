@@ -243,6 +243,7 @@ struct PersistArgs {
   int* status;            // 0, or kPersistTimeout
   unsigned long long timeout_ns;
   int stall_test;         // test hook: one dependency needs an item too many
+  int chunk;              // tickets a CTA takes at a time
 };
 
 constexpr int kPersistTimeout = 1;
@@ -294,9 +295,40 @@ __global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_cons
   __shared__ int s_fail;
   const int64_t per_stage = p.nA + p.nB + p.nC;
   const int64_t total = per_stage * p.nstages;
+  // thread 0's queue state (in shared memory: only thread 0 uses it): the
+  // rest of its chunk of tickets, the last dependency known to be met, and
+  // completions not yet published (published before any wait, when the
+  // counter changes, and at the end of a chunk)
+  __shared__ int64_t next, chunk_end;
+  __shared__ const unsigned* known_q;
+  __shared__ unsigned known_target, npend;
+  __shared__ unsigned* pend;
+  if (threadIdx.x == 0) {
+    next = chunk_end = 0;
+    known_q = nullptr;
+    known_target = npend = 0;
+    pend = nullptr;
+  }
+  auto flush = [&]() {
+    if (npend) {
+      __threadfence();
+      atomicAdd(pend, npend);
+      npend = 0;
+    }
+  };
   for (;;) {
     if (threadIdx.x == 0) {
-      s_item = *(volatile int*)p.status ? total : (int64_t)atomicAdd(p.ticket, 1u);
+      int64_t item = total;
+      if (!*(volatile int*)p.status) {
+        if (next == chunk_end) {
+          flush();
+          next = (int64_t)atomicAdd(p.ticket, (unsigned)p.chunk);
+          chunk_end = next + p.chunk;
+        }
+        item = next < total ? next++ : total;
+      }
+      if (item >= total) flush();
+      s_item = item;
       s_fail = 0;
     }
     __syncthreads();
@@ -325,8 +357,15 @@ __global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_cons
         q = cnt + 1;
         target = (unsigned)(sigma + 1) * G.ctaB;
       }
-      if (target > 0 && !wait_count(q, target, p.status, p.timeout_ns)) s_fail = 1;
-      __threadfence();
+      if (target > 0 && !(q == known_q && target <= known_target)) {
+        flush();
+        if (wait_count(q, target, p.status, p.timeout_ns)) {
+          known_q = q;
+          known_target = target;
+        } else {
+          s_fail = 1;
+        }
+      }
     }
     __syncthreads();
     if (s_fail) break;
@@ -368,8 +407,11 @@ __global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_cons
     }
     __syncthreads();  // the item's writes are done (and its shared memory free)
     if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(cnt + pass, 1u);
+      if (pend != cnt + pass) {
+        flush();
+        pend = cnt + pass;
+      }
+      ++npend;
     }
   }
 }
@@ -426,6 +468,7 @@ struct EnsembleMix {
   int thA, thB, thC;  // threads per CTA of the inverse, x and forward passes
   unsigned* pbuf;     // persistent step: ticket, per-run counters, status
   int nruns_total;
+  int persist_chunk;  // tickets per grab of the persistent step
 };
 
 // every group's tiles at these thread counts: columns 4..64 wide, >= 1 row
@@ -487,7 +530,7 @@ static int mix_eval(EnsembleMix* x, void* const* states, int mode, bool pr, cuda
 
 template <int TH>
 static int persist_launch(EnsembleMix* x, void* const* states, int nsteps,
-                          double timeout_s, bool stall_test, cudaStream_t st) {
+                          double timeout_s, bool stall_test, int chunk, cudaStream_t st) {
   fast::PersistArgs p;
   memset(&p, 0, sizeof(p));
   p.ngroups = x->n;
@@ -526,6 +569,7 @@ static int persist_launch(EnsembleMix* x, void* const* states, int nsteps,
   p.status = reinterpret_cast<int*>(x->pbuf + 1 + 3 * (int64_t)rb);
   p.timeout_ns = (unsigned long long)(timeout_s * 1e9);
   p.stall_test = stall_test ? 1 : 0;
+  p.chunk = chunk;
   const size_t smem = (size_t)TH * 64;
   int rc = fast::prep(fast::kpersist<TH>, smem);
   if (rc) return rc;
@@ -574,6 +618,7 @@ int gbs_ens2d_mixed_create(gbs_ens2d* const* groups, int ngroups, gbs_ens2d_mixe
     h->x.e[k] = &groups[k]->e;
   }
   h->x.thA = h->x.thB = h->x.thC = 512;
+  h->x.persist_chunk = 4;
   if (!gbs::mix_fits(&h->x, 512, 512, 512)) {
     delete h;
     gbs::set_error("gbs_ens2d_mixed_create: a group size has no single-launch tile");
@@ -641,9 +686,20 @@ int gbs_ens2d_persistent_step(gbs_ens2d_mixed* h, void* const* states, int nstep
     if (rc || --nsteps == 0) return rc;
   }
   const bool stall = (flags & GBS_STEP_TEST_STALL) != 0;
+  const int chunk = h->x.persist_chunk;
   if (threads == 256)
-    return gbs::persist_launch<256>(&h->x, states, nsteps, timeout_s, stall, st);
-  return gbs::persist_launch<512>(&h->x, states, nsteps, timeout_s, stall, st);
+    return gbs::persist_launch<256>(&h->x, states, nsteps, timeout_s, stall, chunk, st);
+  return gbs::persist_launch<512>(&h->x, states, nsteps, timeout_s, stall, chunk, st);
+}
+
+int gbs_ens2d_persistent_set_chunk(gbs_ens2d_mixed* h, int chunk) {
+  gbs::clear_error();
+  if (!h || chunk < 1 || chunk > 64) {
+    gbs::set_error("gbs_ens2d_persistent_set_chunk: chunk in 1..64");
+    return GBS_EINVAL;
+  }
+  h->x.persist_chunk = chunk;
+  return GBS_OK;
 }
 
 int gbs_ens2d_persistent_status(gbs_ens2d_mixed* h, int* status) {

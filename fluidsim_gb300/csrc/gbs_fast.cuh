@@ -68,7 +68,14 @@ template <typename C>
 __device__ __forceinline__ int swz(int q) {
   constexpr int E = 128 / sizeof(C);
   constexpr int LG = E == 16 ? 4 : 3;
+#ifdef GBS_SWZ_LIN2
+  // x ^ (x << 1) of the sweep index: still linear over GF(2) (an XOR of
+  // shifts), so swz_join below applies unchanged
+  const int x = q >> LG;
+  return q ^ ((x ^ (x << 1)) & (E - 1));
+#else
   return q ^ ((q >> LG) & (E - 1));
+#endif
 }
 
 // swz(b | K) from sb = swz(b), for b and K with no bit in common (b per

@@ -31,6 +31,13 @@
 
 #include "gbs_turb.h"
 
+// CTAs of 256 threads per SM the inference kernels are compiled for (3 fits
+// 80 registers but spills, and measured slower: 0.297 against 0.290 ms for
+// 2.1 M points)
+#ifndef GBS_MLP_MINB
+#define GBS_MLP_MINB 2
+#endif
+
 namespace gbs {
 
 constexpr int kW1S = 24, kW2S = 72, kOutP = 8;

@@ -80,7 +80,7 @@ __global__ void k_smagorinsky(const T* __restrict__ g, T* __restrict__ tau, int6
 // on the tensor cores: each warp evaluates tiles of 16 points with
 // mma.sync m16n8k16 (gbs_mlp_mma.cuh).
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, GBS_MLP_MINB)
 k_mlp_closure(const T* __restrict__ g, T* __restrict__ tau, int64_t n, MLPWeights w) {
   __shared__ MMAShared sm;
   mma_stage(sm, w);

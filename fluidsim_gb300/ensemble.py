@@ -98,6 +98,7 @@ class EnsembleNS2D:
         self.persistent = False
         self.persist_threads = 512
         self.persist_timeout_s = 1.0
+        self.persist_chunk = 4  # work items a CTA takes from the queue at a time
 
     def __del__(self):
         if getattr(self, "_mix", None):
@@ -117,6 +118,7 @@ class EnsembleNS2D:
     def step(self, nsteps=1, flags=_lib.GBS_STEP_DEALIASED):
         cur = torch.cuda.current_stream()
         if self.persistent:
+            _lib.check(self.lib.gbs_ens2d_persistent_set_chunk(self._mix, self.persist_chunk))
             _lib.check(self.lib.gbs_ens2d_persistent_step(
                 self._mix, self._mix_states, nsteps, self.persist_threads,
                 self.persist_timeout_s, flags, ctypes.c_void_p(cur.cuda_stream)),
@@ -181,18 +183,18 @@ class EnsembleNS2D:
         self.mixed = False
         self.persistent = True
         best_p = None
-        for th in (256, 512):
-            self.persist_threads = th
+        for th, chunk in itertools.product((256, 512), (1, 4, 16)):
+            self.persist_threads, self.persist_chunk = th, chunk
             try:
                 ms = time_all(steps)
             except ValueError:  # a group has no tile at this thread count
                 continue
             self.check_status()
             if best_p is None or ms < best_p[0]:
-                best_p = (ms, th)
+                best_p = (ms, th, chunk)
         self.persistent = False
         if best_p is not None:
-            self.persist_threads = best_p[1]
+            self.persist_threads, self.persist_chunk = best_p[1], best_p[2]
             mode_ms["persistent"] = best_p[0]
         mode = min(mode_ms, key=mode_ms.get)
         self.mixed = mode == "single_launch"
@@ -200,6 +202,7 @@ class EnsembleNS2D:
         table["all_groups_ms_per_step"] = mode_ms
         table["single_launch_threads"] = dict(zip(("inverse", "x", "forward"), best_mix[1]))
         table["persistent_threads"] = best_p[1] if best_p else None
+        table["persistent_chunk"] = best_p[2] if best_p else None
         table["mode"] = mode
         self.reset()
         return table

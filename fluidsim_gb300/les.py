@@ -1,7 +1,8 @@
 """Learned subgrid closure for coarse-grid LES, end to end on one GB300.
 
-1. ``forced_dns``: ns3d DNS (FP32) forced by ``TCRandomForcing3D`` in the
-   shells ``k in [2, 3]`` at power 1, brought to its statistically steady
+1. ``forced_dns``: ns3d DNS (FP32) forced by the ``tcrandom`` forcing of
+   ``fluidsim_gb300.forcing`` on the three velocity components (1/3 each) in
+   the shells ``k in [2, 3]``, total power 1, brought to its statistically steady
    state (coarse-grid spin-up, prolongation, fine-grid spin-up); snapshots
    of the spectral state.
 2. ``filtered_data``: for each snapshot, top-hat filter of width

@@ -301,6 +301,10 @@ int gbs_ens2d_mixed_step(gbs_ens2d_mixed* mixed, void* const* states, int nsteps
 int gbs_ens2d_persistent_step(gbs_ens2d_mixed* mixed, void* const* states, int nsteps,
                               int threads, double timeout_s, int flags, void* stream);
 int gbs_ens2d_persistent_status(gbs_ens2d_mixed* mixed, int* status);
+/* work items a CTA of the persistent step takes from the queue at a time
+ * (1..64, default 4): its completions are published per (run, pass) group,
+ * before any wait and at the end of each chunk */
+int gbs_ens2d_persistent_set_chunk(gbs_ens2d_mixed* mixed, int chunk);
 
 /* Filtered-DNS data for the learned closure (no reference counterpart):
  *   gbs_spectral_resample: nfields spectral fields of shape_in (nz, ny, nx)
