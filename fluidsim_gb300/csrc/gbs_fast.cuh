@@ -56,25 +56,24 @@ struct Line {
 };
 
 // Shared-memory swizzle: XOR the element index inside each 128-byte bank
-// sweep (E = 128 / sizeof(C) elements) with the index of the sweep, so the
-// strided Stockham writes, the unit-stride reads and the column-tile
-// accesses spread over the 32 banks.  A permutation inside every E-aligned
-// group, so any E-aligned slot keeps its extent.  (Two 8-byte writes of a
-// half-warp still share a bank in the first-stage writes of the 8-column
-// tiles and the second-stage writes of the rows, 1.2x the ideal wavefronts;
-// XOR-ing with x ^ (x << 1) instead removes that but its extra address
-// arithmetic made the issue-bound passes 5-13 % slower at 512^3.)
+// sweep (E = 128 / sizeof(C) elements) with x ^ (x << 1), x the index of
+// the sweep, so the strided Stockham writes, the unit-stride reads and the
+// column-tile accesses spread over the 32 banks.  A permutation inside
+// every E-aligned group, so any E-aligned slot keeps its extent.  XOR-ing
+// with x alone (-DGBS_SWZ_XOR1) leaves two 8-byte writes of a half-warp on
+// one bank in the first-stage writes of the 8-column tiles and the
+// second-stage writes of the rows: 2.8x the bank conflicts of x ^ (x << 1)
+// in the x pass at 512^2 x 64 (7.3 M against 2.6 M), 2.3 % slower.
 template <typename C>
 __device__ __forceinline__ int swz(int q) {
   constexpr int E = 128 / sizeof(C);
   constexpr int LG = E == 16 ? 4 : 3;
-#ifdef GBS_SWZ_LIN2
-  // x ^ (x << 1) of the sweep index: still linear over GF(2) (an XOR of
-  // shifts), so swz_join below applies unchanged
+#ifdef GBS_SWZ_XOR1
+  return q ^ ((q >> LG) & (E - 1));
+#else
+  // linear over GF(2) (an XOR of shifts), so swz_join below applies
   const int x = q >> LG;
   return q ^ ((x ^ (x << 1)) & (E - 1));
-#else
-  return q ^ ((q >> LG) & (E - 1));
 #endif
 }
 
@@ -112,6 +111,11 @@ __device__ __forceinline__ bool kept(int p, int n, int kc) {
 // Fetch the line holding p into L2 (writes no register).
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Fetch bytes [p, p + n) into L2 (p 16-byte aligned, n a multiple of 16).
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned n) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(n) : "memory");
 }
 
 // Asynchronous copy of one complex value into shared memory (zeros when
@@ -791,6 +795,205 @@ kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
     if (v0) F0[k] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
     if (v1) F1[k] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
   }
+}
+
+// p, opaque to the compiler from here on: loads through the result are
+// neither merged with loads through earlier copies nor moved above the
+// volatile asm statements (barriers) that precede this one.  Keeps the
+// per-field loads and stage twiddles of kf3_xr from being hoisted and held
+// across all nine transforms.
+template <typename X>
+__device__ __forceinline__ const X* opaque(const X* p) {
+  const X* r;
+  asm volatile("mov.b64 %0, %1;" : "=l"(r) : "l"(p));
+  return r;
+}
+
+// Register index holding stage-0 position jt + r N/8 in the output order of
+// run(): the i with Line::outm(i) == r.
+template <int LOGN>
+__device__ __forceinline__ constexpr int inv_outm(int r) {
+  int i = 0;
+  while (Line<LOGN>::outm(i) != r) ++i;
+  return i;
+}
+
+#ifndef GBS_XR_MINB
+#define GBS_XR_MINB 2
+#endif
+#ifndef GBS_XR_THREADS
+#define GBS_XR_THREADS 256
+#endif
+
+// B, rows in pairs (as kf3_xp), with all six fields of a pair transformed by
+// the same N/8 threads, one field after the other.  run() leaves each
+// inverse transform's outputs in registers at positions jt + outm(i) N/8,
+// the same positions in every field, so v x omega forms in registers, and
+// each product line enters its forward transform from registers: no
+// shared-memory round trip for the products (a third of kf3_xp's
+// shared-memory traffic).  The products accumulate as the omega lines
+// arrive (ox: p_y, p_z; oy: p_z complete, p_x; oz: p_x, p_y complete); p_z
+// is transformed before oz, and vx waits in shared memory (each thread
+// reads back only its own values), so at most four lines are held in
+// registers besides the line being transformed.  The split of each product line into the two
+// rows' spectra reads Z[N - k] from a half-line region that holds
+// positions N/2 .. N-1.  Barriers: the pair's two exchange slots alternate
+// (three-stage lines), so consecutive transforms need no barrier of their
+// own (a slot is written again only after a barrier that every reader of
+// its previous contents has passed).  Not for ns3d.strat (kf3_xp).
+template <typename T, int LOGN, int LP>
+__global__ void __launch_bounds__(LP * (1 << LOGN) / 8, GBS_XR_MINB)
+kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
+       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+  using C = cplx<T>;
+  using P = Line<LOGN>;
+  constexpr int N = P::N, N8 = P::N8, H = N / 2;
+  constexpr bool WARP = N8 <= 32;
+  constexpr int E = 128 / sizeof(C);
+  constexpr int ALT = xp_alt<LOGN>() ? N : 0;
+  constexpr int PART = H > E ? H : E;
+  constexpr int SLOT = N + ALT + PART + N;  // exchange slots, partner half, stash
+  static_assert(P::NST >= 2, "a line needs at least one exchange");
+  C* buf = reinterpret_cast<C*>(g_smem_fast);
+  const int jt = threadIdx.x % N8;
+  const int lp = threadIdx.x / N8;
+  const int64_t nrows = (int64_t)g.nz * g.ny;
+  const int64_t nK = nrows * g.nkx;
+  const int64_t row0 = ((int64_t)blockIdx.x * LP + lp) * 2;
+  const bool v0 = row0 < nrows, v1 = row0 + 1 < nrows;
+  const SwzView<C, 1> acc{buf + lp * SLOT, 0};
+  const SwzView<C, 1> part{buf + lp * SLOT + N + ALT, 0};
+  C* stash = buf + lp * SLOT + N + ALT + PART;
+  const int bar = WARP ? 0 : 1 + lp;
+  const int kcx = g.pr ? g.kcx : g.nkx + 1;
+  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  const C* r0base = W + row0 * g.nkx;
+  // the pair's rows of fields 1..5 into L2 now (one bulk prefetch per row,
+  // its kept modes; 16-byte aligned inside the row), so that the loads of
+  // each field, issued only after the previous field's transform, hit L2
+  if (jt < 10) {
+    const int f = 1 + jt / 2, rr = jt & 1;
+    if (rr == 0 ? v0 : v1) {
+      const int nk = kcx < g.nkx ? kcx : g.nkx;
+      const char* a = reinterpret_cast<const char*>(r0base + f * nK + rr * g.nkx);
+      const char* a16 = reinterpret_cast<const char*>(reinterpret_cast<uintptr_t>(a) & ~uintptr_t(15));
+      const unsigned bytes = (unsigned)((a + nk * sizeof(C) - a16) & ~size_t(15));
+      if (bytes) prefetch_l2_bulk(a16, bytes);
+    }
+  }
+
+  // raw inputs of field f at this thread's eight positions (rows row0 and
+  // row0 + 1), loaded one transform ahead of their use
+  auto load = [&](int f, C(&a0)[8], C(&a1)[8]) {
+    const C* r0 = opaque(r0base) + f * nK;
+    const C* r1 = r0 + g.nkx;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int idx = r < 4 ? jt + r * N8 : (8 - r) * N8 - jt;
+      const bool in = idx < kcx;
+      a0[r] = (v0 && in) ? r0[idx] : mk<C>(0, 0);
+      a1[r] = (v1 && in) ? r1[idx] : mk<C>(0, 0);
+    }
+  };
+  // inverse transform of the raw inputs into v (output order of run())
+  auto inverse = [&](C(&a0)[8], C(&a1)[8], C(&v)[8]) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      if ((r == 0 || r == 4) && jt == 0) {
+        a0[r].y = 0;
+        a1[r].y = 0;
+      }
+      v[r] = r < 4 ? mk<C>(a0[r].x - a1[r].y, a0[r].y + a1[r].x)
+                   : mk<C>(a0[r].x + a1[r].y, a1[r].x - a0[r].y);
+    }
+    run<+1, LOGN, WARP, ALT>(v, jt, true, acc, opaque(twx), 1, bar);
+  };
+  // forward transform of product line p (output order of run()) into field f
+  auto forward = [&](int f, const C(&p)[8]) {
+    C v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = p[inv_outm<LOGN>(r)];
+    run<-1, LOGN, WARP, ALT>(v, jt, true, acc, opaque(twx), 1, bar);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (P::outm(i) >= 4) part(jt + (P::outm(i) - 4) * N8) = v[i];
+    line_sync<WARP, N8>(bar);
+    C* F0 = F + f * nK + row0 * g.nkx;
+    C* F1 = F0 + g.nkx;
+    const T h = T(0.5);
+#pragma unroll
+    for (int r = 0; r <= 4; ++r) {
+      const int k = r < 4 ? jt + r * N8 : H;
+      if ((r == 4 && jt != 0) || k >= nout) continue;
+      const C z = v[inv_outm<LOGN>(r)];
+      const C m = (k == 0 || k == H) ? z : part(N - k - H);
+      if (v0) F0[k] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
+      if (v1) F1[k] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
+    }
+  };
+
+  T mx = 0, my = 0, mz = 0;
+  auto vmax_of = [](const C(&v)[8], T& m) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) m = fmax(m, fmax(fabs(v[i].x), fabs(v[i].y)));
+  };
+  // two raw buffers: the loads of the next field are in flight during the
+  // current transform, except oz's, issued after p_z's forward transform
+  // (its raw inputs there would take the live floats from 80 to 96 and
+  // spill at 128 registers); every field after the first is already on its
+  // way to L2 (bulk prefetch above)
+  C a0[8], a1[8], b0[8], b1[8];
+  load(0, a0, a1);
+  load(1, b0, b1);
+  {
+    C v[8];
+    inverse(a0, a1, v);  // vx waits in this thread's own stash slots
+    vmax_of(v, mx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) stash[i * N8 + jt] = v[i];
+  }
+  load(2, a0, a1);
+  C vy[8], vz[8], px[8], py[8], pz[8];
+  inverse(b0, b1, vy);
+  vmax_of(vy, my);
+  load(3, b0, b1);
+  inverse(a0, a1, vz);
+  vmax_of(vz, mz);
+  load(4, a0, a1);
+  {
+    C o[8];
+    inverse(b0, b1, o);  // ox
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      py[i] = mk<C>(vz[i].x * o[i].x, vz[i].y * o[i].y);
+      pz[i] = mk<C>(-(vy[i].x * o[i].x), -(vy[i].y * o[i].y));
+    }
+  }
+  {
+    C o[8];
+    inverse(a0, a1, o);  // oy
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const C vx = stash[i * N8 + jt];
+      pz[i] = mk<C>(fma(vx.x, o[i].x, pz[i].x), fma(vx.y, o[i].y, pz[i].y));
+      px[i] = mk<C>(-(vz[i].x * o[i].x), -(vz[i].y * o[i].y));
+    }
+  }
+  forward(2, pz);
+  load(5, b0, b1);
+  {
+    C o[8];
+    inverse(b0, b1, o);  // oz
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const C vx = stash[i * N8 + jt];
+      px[i] = mk<C>(fma(vy[i].x, o[i].x, px[i].x), fma(vy[i].y, o[i].y, px[i].y));
+      py[i] = mk<C>(fma(-vx.x, o[i].x, py[i].x), fma(-vx.y, o[i].y, py[i].y));
+    }
+  }
+  forward(0, px);
+  forward(1, py);
+  if (vmax) block_max3(mx, my, mz, vmax);
 }
 
 #ifndef GBS_FWDZ_BATCH

@@ -234,9 +234,35 @@ static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
   return GBS_OK;
 }
 
+// Rows in pairs with the products in registers (kf3_xr): FP32 ns3d for
+// 16 <= nx <= 1024, LP pairs per CTA up to GBS_XR_THREADS threads.
+template <typename T, int LOGM>
+static int B3r_launch(const Geo& g, const void* W, void* F, const void* tw,
+                      unsigned long long* vmax, cudaStream_t st) {
+  using C = cplx<T>;
+  constexpr int LOGN = LOGM + 1, N = 1 << LOGN, N8 = N / 8;
+  constexpr int LP = GBS_XR_THREADS / N8 > 0 ? GBS_XR_THREADS / N8 : 1;
+  static_assert(N8 <= 32 || LP <= 15, "one named barrier per pair (ids 1..15)");
+  constexpr int TH = LP * N8;
+  constexpr int E = 128 / sizeof(C);
+  constexpr int PART = N / 2 > E ? N / 2 : E;
+  const size_t smem = sizeof(C) * (size_t)LP * (N + (xp_alt<LOGN>() ? N : 0) + PART + N);
+  int rc = prep(kf3_xr<T, LOGN, LP>, smem);
+  if (rc) return rc;
+  const int64_t npairs = ((int64_t)g.nz * g.ny + 1) / 2;
+  kf3_xr<T, LOGN, LP><<<ceil_div(npairs, LP), TH, smem, st>>>(
+      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
 template <typename T, int LOGM, bool ST>
 static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
                    unsigned long long* vmax, cudaStream_t st) {
+#ifndef GBS_X_NOREG
+  if constexpr (sizeof(T) == 4 && !ST && LOGM >= 3 && LOGM <= 9)
+    return B3r_launch<T, LOGM>(g, W, F, tw, vmax, st);
+#endif
   if constexpr (sizeof(T) == 4 && LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
   else return B3_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
 }
