@@ -560,7 +560,7 @@ def main():
     host_in = torch.empty(S.shape, dtype=S.dtype, pin_memory=True)
     host_in.copy_(S)
     host_out = torch.empty_like(host_in, pin_memory=True)
-    e_steps = max(3, steps // 2)
+    e_steps = max(3, steps)
     e2e_serial = e2e_run(ts, S, host_in, host_out, e_steps, world, dist, pipelined=False)
     e2e_run(ts, S, host_in, host_out, 2, world, dist, pipelined=True)  # warm-up
     e2e_rate = e2e_run(ts, S, host_in, host_out, e_steps, world, dist, pipelined=True)

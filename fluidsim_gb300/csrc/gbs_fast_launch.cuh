@@ -234,8 +234,10 @@ static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
   return GBS_OK;
 }
 
-// Rows in pairs with the products in registers (kf3_xr): FP32 ns3d for
-// 16 <= nx <= 1024, LP pairs per CTA up to GBS_XR_THREADS threads.
+// Rows in pairs with the products in registers (kf3_xr): FP32 ns3d, LP
+// pairs per CTA up to GBS_XR_THREADS threads.  Used for nx = 256 and 512
+// (x pass -6 % and -3 % against kf3_xp); at nx = 128 and 1024 the 128
+// registers it needs spill and kf3_xp is 3-4 % faster.
 template <typename T, int LOGM>
 static int B3r_launch(const Geo& g, const void* W, void* F, const void* tw,
                       unsigned long long* vmax, cudaStream_t st) {
@@ -260,7 +262,7 @@ template <typename T, int LOGM, bool ST>
 static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
                    unsigned long long* vmax, cudaStream_t st) {
 #ifndef GBS_X_NOREG
-  if constexpr (sizeof(T) == 4 && !ST && LOGM >= 3 && LOGM <= 9)
+  if constexpr (sizeof(T) == 4 && !ST && (LOGM == 7 || LOGM == 8))
     return B3r_launch<T, LOGM>(g, W, F, tw, vmax, st);
 #endif
   if constexpr (sizeof(T) == 4 && LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
