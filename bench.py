@@ -453,6 +453,15 @@ def mlp_throughput(n_points=128**3, reps=20):
     ev[1].record()
     torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / reps
+    for _ in range(3):
+        predict(net, G, precision="bf16")
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        predict(net, G, precision="bf16")
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms_bf16 = ev[0].elapsed_time(ev[1]) / reps
     # one training gradient (forward + backward on the tensor cores, then the
     # weight-gradient reduction) of a 65536-sample batch
     from fluidsim_gb300.closure import ClosureTrainer
@@ -470,13 +479,15 @@ def mlp_throughput(n_points=128**3, reps=20):
     torch.cuda.synchronize()
     grad_ms = ev[0].elapsed_time(ev[1]) / reps
     alg = MLP_FLOPS_PER_POINT * n_points
-    return {"points": n_points, "ms": ms, "train_gradient_ms": grad_ms,
+    return {"points": n_points, "ms": ms, "ms_bf16": ms_bf16, "train_gradient_ms": grad_ms,
             "train_batch": batch, "alg_flops": alg,
             "alg_tflops": alg / ms / 1e9,
             "tensor_flops_issued": 3 * 2 * n_points * (16 * 64 + 64 * 64 + 64 * 8),
             "bytes": n_points * 15 * 4, "hbm_gbs": n_points * 15 * 4 / ms / 1e6,
-            "note": "mma.sync m16n8k16 BF16 x FP32-accumulate; activations as 3 BF16 "
-                    "terms (3 MMAs per tile), weights exact BF16"}
+            "alg_tflops_bf16": alg / ms_bf16 / 1e9,
+            "note": "mma.sync m16n8k16 BF16 x FP32-accumulate, weights exact BF16; ms: "
+                    "FP32 activations as 3 BF16 terms (3 MMAs per tile); ms_bf16: "
+                    "activations rounded to BF16, hardware tanh (1 MMA per tile)"}
 
 
 def rel_l2(a, b):

@@ -30,7 +30,8 @@ EXPORTED = (
     "gbs_ns_max_velocity", "gbs_cfl_update", "gbs_ns_spatial_means",
     "gbs_ns_spectrum_size", "gbs_ns_spectrum", "gbs_ns_timing",
     "gbs_ns_timing_report", "gbs_fft_c2r_noalloc", "gbs_ns_set_turb_model",
-    "gbs_mlp_grad_workspace", "gbs_mlp_forward", "gbs_mlp_grad", "gbs_mlp_adam",
+    "gbs_mlp_grad_workspace", "gbs_mlp_forward", "gbs_mlp_forward_bf16", "gbs_mlp_grad",
+    "gbs_mlp_adam",
     "gbs_ns_set_forcing", "gbs_spectral_resample", "gbs_products6",
     "gbs_velocity_gradients", "gbs_ens2d_create", "gbs_ens2d_destroy",
     "gbs_ens2d_set_params", "gbs_ens2d_set_tuning", "gbs_ens2d_step", "gbs_ens2d_nan_flag",
@@ -154,6 +155,8 @@ def _declare(lib):
         "gbs_velocity_gradients": (ctypes.c_int, [I64P, DP, I64P, ctypes.c_int, P, P, P]),
         "gbs_mlp_forward": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, ctypes.c_int64, P,
                                            ctypes.c_int64, P]),
+        "gbs_mlp_forward_bf16": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, ctypes.c_int64,
+                                                P, ctypes.c_int64, P]),
         "gbs_mlp_grad": (ctypes.c_int, [ctypes.POINTER(MLPWeights), P, P, ctypes.c_int64, P,
                                         ctypes.c_int64, ctypes.c_double, P, P, P, P]),
         "gbs_mlp_adam": (ctypes.c_int, [P, P, P, P, ctypes.c_int64, ctypes.c_double,

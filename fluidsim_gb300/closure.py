@@ -172,13 +172,23 @@ def subgrid_dissipation(G, Tau):
             + (G[2] + G[6]) * Tau[4] + (G[5] + G[7]) * Tau[5])
 
 
-def predict(net: ClosureMLP, G):
-    """tau = MLP(G) for a (9, n) float32 CUDA tensor (inference kernel)."""
+PRECISIONS = ("fp32", "bf16")
+
+
+def predict(net: ClosureMLP, G, precision="fp32"):
+    """tau = MLP(G) for a (9, n) float32 CUDA tensor (inference kernel).
+
+    precision "fp32": FP32 activations (three BF16 terms per tensor-core
+    operand); "bf16": activations rounded to BF16 and the hardware tanh
+    (relative error ~3e-3, a third of the tensor-core work)."""
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision {precision!r} not in {PRECISIONS}")
     lib = _lib.load()
     n = G.shape[1]
     tau = torch.empty((N_OUT, n), dtype=torch.float32, device=G.device)
     w = net.c_weights()
-    _lib.check(lib.gbs_mlp_forward(ctypes.byref(w), ctypes.c_void_p(G.data_ptr()), n,
-                                   ctypes.c_void_p(tau.data_ptr()), n,
-                                   current_stream_handle()), "gbs_mlp_forward")
+    fn = lib.gbs_mlp_forward if precision == "fp32" else lib.gbs_mlp_forward_bf16
+    _lib.check(fn(ctypes.byref(w), ctypes.c_void_p(G.data_ptr()), n,
+                  ctypes.c_void_p(tau.data_ptr()), n, current_stream_handle()),
+               "gbs_mlp_forward")
     return tau

@@ -444,14 +444,15 @@ __global__ void k_adam(float* __restrict__ master, float* __restrict__ m, float*
 }
 
 // inference on SoA fields (float): tensor-core tiles of 16 points per warp
-// (gbs_mlp_mma.cuh)
-__global__ void __launch_bounds__(256, GBS_MLP_MINB)
+// (gbs_mlp_mma.cuh), activations as three BF16 terms or one (BF16 form)
+template <int TERMS>
+__global__ void __launch_bounds__(256, mlp_minb<TERMS>())
 k_mlp_forward(MLPWeights w, const float* __restrict__ g, int64_t ld, float* __restrict__ tau,
               int64_t n) {
   __shared__ MMAShared sm;
   mma_stage(sm, w);
   __syncthreads();
-  mma_eval_all<float, float>(sm, g, tau, ld, n);
+  mma_eval_all<TERMS, float, float>(sm, g, tau, ld, n);
 }
 
 static MLPWeights to_w(const gbs_mlp_weights* p) {
@@ -467,6 +468,23 @@ static MLPWeights to_w(const gbs_mlp_weights* p) {
   return w;
 }
 
+template <int TERMS>
+static int mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float* tau,
+                       int64_t n, void* stream, const char* name) {
+  clear_error();
+  if (!w || !g || !tau || n < 0 || ld < n) {
+    set_error("%s: invalid argument", name);
+    return GBS_EINVAL;
+  }
+  if (n == 0) return GBS_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int64_t nb = (n + 127) / 128;  // 8 warps of 16 points
+  if (nb > 152 * 8) nb = 152 * 8;
+  k_mlp_forward<TERMS><<<(int)nb, 256, 0, st>>>(to_w(w), g, ld, tau, n);
+  GBS_CHECK_LAUNCH();
+  return GBS_OK;
+}
+
 }  // namespace gbs
 
 extern "C" {
@@ -478,18 +496,12 @@ int64_t gbs_mlp_grad_workspace(int64_t batch) {
 
 int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld, float* tau,
                     int64_t n, void* stream) {
-  gbs::clear_error();
-  if (!w || !g || !tau || n < 0 || ld < n) {
-    gbs::set_error("gbs_mlp_forward: invalid argument");
-    return GBS_EINVAL;
-  }
-  if (n == 0) return GBS_OK;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int64_t nb = (n + 127) / 128;  // 8 warps of 16 points
-  if (nb > 152 * 8) nb = 152 * 8;
-  gbs::k_mlp_forward<<<(int)nb, 256, 0, st>>>(gbs::to_w(w), g, ld, tau, n);
-  GBS_CHECK_LAUNCH();
-  return GBS_OK;
+  return gbs::mlp_forward<3>(w, g, ld, tau, n, stream, "gbs_mlp_forward");
+}
+
+int gbs_mlp_forward_bf16(const gbs_mlp_weights* w, const float* g, int64_t ld, float* tau,
+                         int64_t n, void* stream) {
+  return gbs::mlp_forward<1>(w, g, ld, tau, n, stream, "gbs_mlp_forward_bf16");
 }
 
 int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau, int64_t ld,

@@ -24,6 +24,12 @@
 // Shared memory holds the weights as BF16 with row strides of 24 (W1) and
 // 72 (W2, W3) elements: the B-fragment loads (32 bits at row n0 + g, column
 // k0 + 2q) then fall in 32 distinct banks.
+//
+// TERMS = 1 is the BF16 form: each activation enters as one BF16 value
+// (BF16 operands, FP32 accumulation, the tensor-core precision of mixed-
+// precision inference) and tanh is the hardware tanh.approx.f32; a third of
+// the MMAs, no splitting, one MUFU operation per tanh instead of two.
+// Relative error ~3e-3 against the FP32 evaluation.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -37,6 +43,11 @@
 #ifndef GBS_MLP_MINB
 #define GBS_MLP_MINB 2
 #endif
+// the same for the BF16 form (TERMS = 1)
+#ifndef GBS_MLP_MINB_BF16
+#define GBS_MLP_MINB_BF16 3
+#endif
+template <int TERMS> constexpr int mlp_minb() { return TERMS == 1 ? GBS_MLP_MINB_BF16 : GBS_MLP_MINB; }
 
 namespace gbs {
 
@@ -106,13 +117,38 @@ __device__ __forceinline__ float tanh_act(float x) {
   return 1.f - __fdividef(2.f, __expf(2.f * x) + 1.f);
 }
 
+// TERMS = 3: split3; TERMS = 1: one BF16 pair in p0 (p1, p2 untouched).
+template <int TERMS>
+__device__ __forceinline__ void split_t(float x, float y, uint32_t& p0, uint32_t& p1,
+                                        uint32_t& p2) {
+  if constexpr (TERMS == 3) {
+    split3(x, y, p0, p1, p2);
+  } else {
+    const __nv_bfloat162 h0 = __floats2bfloat162_rn(x, y);
+    p0 = *reinterpret_cast<const uint32_t*>(&h0);
+  }
+}
+
+// TERMS = 3: tanh_act; TERMS = 1: the hardware approximation (MUFU.TANH,
+// relative error ~2^-11, below the BF16 rounding of its result).
+template <int TERMS>
+__device__ __forceinline__ float act_t(float x) {
+  if constexpr (TERMS == 3) {
+    return tanh_act(x);
+  } else {
+    float r;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+}
+
 __device__ __forceinline__ uint32_t ld_b32(const __nv_bfloat16* p) {
   return *reinterpret_cast<const uint32_t*>(p);
 }
 
 // The network on the 16 points p0 .. p0 + 15 (< n) of SoA fields:
 // input c of point i at g[i + c * ld], output o at tau[i + o * ld].
-template <typename TI, typename TO>
+template <int TERMS, typename TI, typename TO>
 __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restrict__ g,
                                            TO* __restrict__ tau, int64_t ld, int64_t p0,
                                            int64_t n) {
@@ -133,10 +169,10 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
       x[0][u] = ok ? (float)g[la + c * ld] * s.sin[c] : 0.f;
       x[1][u] = ok ? (float)g[lb + c * ld] * s.sin[c] : 0.f;
     }
-    split3(x[0][0], x[0][1], A[0][0], A[1][0], A[2][0]);
-    split3(x[1][0], x[1][1], A[0][1], A[1][1], A[2][1]);
-    split3(x[0][2], x[0][3], A[0][2], A[1][2], A[2][2]);
-    split3(x[1][2], x[1][3], A[0][3], A[1][3], A[2][3]);
+    split_t<TERMS>(x[0][0], x[0][1], A[0][0], A[1][0], A[2][0]);
+    split_t<TERMS>(x[1][0], x[1][1], A[0][1], A[1][1], A[2][1]);
+    split_t<TERMS>(x[0][2], x[0][3], A[0][2], A[1][2], A[2][2]);
+    split_t<TERMS>(x[1][2], x[1][3], A[0][3], A[1][3], A[2][3]);
   }
 
   // layer 1 -> h1 as the A fragments of layer 2 (3 terms x 4 k-tiles)
@@ -155,14 +191,14 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
       const __nv_bfloat16* wr = s.W1 + (8 * nt + gq) * kW1S + 2 * q;
       const uint32_t b0 = ld_b32(wr), b1 = ld_b32(wr + 8);
 #pragma unroll
-      for (int p = 0; p < 3; ++p) mma_bf16(c[h], A[p], b0, b1);
+      for (int p = 0; p < TERMS; ++p) mma_bf16(c[h], A[p], b0, b1);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) c[h][e] = tanh_act(c[h][e]);
+      for (int e = 0; e < 4; ++e) c[h][e] = act_t<TERMS>(c[h][e]);
     }
-    split3(c[0][0], c[0][1], H[0][t][0], H[1][t][0], H[2][t][0]);
-    split3(c[0][2], c[0][3], H[0][t][1], H[1][t][1], H[2][t][1]);
-    split3(c[1][0], c[1][1], H[0][t][2], H[1][t][2], H[2][t][2]);
-    split3(c[1][2], c[1][3], H[0][t][3], H[1][t][3], H[2][t][3]);
+    split_t<TERMS>(c[0][0], c[0][1], H[0][t][0], H[1][t][0], H[2][t][0]);
+    split_t<TERMS>(c[0][2], c[0][3], H[0][t][1], H[1][t][1], H[2][t][1]);
+    split_t<TERMS>(c[1][0], c[1][1], H[0][t][2], H[1][t][2], H[2][t][2]);
+    split_t<TERMS>(c[1][2], c[1][3], H[0][t][3], H[1][t][3], H[2][t][3]);
   }
 
   // layer 2, two n-tiles at a time, each pair feeding k-tile t of layer 3
@@ -183,20 +219,20 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
       for (int kt = 0; kt < 4; ++kt) {
         const uint32_t b0 = ld_b32(wr + 16 * kt), b1 = ld_b32(wr + 16 * kt + 8);
 #pragma unroll
-        for (int p = 0; p < 3; ++p) mma_bf16(c[h], H[p][kt], b0, b1);
+        for (int p = 0; p < TERMS; ++p) mma_bf16(c[h], H[p][kt], b0, b1);
       }
 #pragma unroll
-      for (int e = 0; e < 4; ++e) c[h][e] = tanh_act(c[h][e]);
+      for (int e = 0; e < 4; ++e) c[h][e] = act_t<TERMS>(c[h][e]);
     }
     uint32_t A3[3][4];
-    split3(c[0][0], c[0][1], A3[0][0], A3[1][0], A3[2][0]);
-    split3(c[0][2], c[0][3], A3[0][1], A3[1][1], A3[2][1]);
-    split3(c[1][0], c[1][1], A3[0][2], A3[1][2], A3[2][2]);
-    split3(c[1][2], c[1][3], A3[0][3], A3[1][3], A3[2][3]);
+    split_t<TERMS>(c[0][0], c[0][1], A3[0][0], A3[1][0], A3[2][0]);
+    split_t<TERMS>(c[0][2], c[0][3], A3[0][1], A3[1][1], A3[2][1]);
+    split_t<TERMS>(c[1][0], c[1][1], A3[0][2], A3[1][2], A3[2][2]);
+    split_t<TERMS>(c[1][2], c[1][3], A3[0][3], A3[1][3], A3[2][3]);
     const __nv_bfloat16* wr = s.W3 + gq * kW2S + 16 * t + 2 * q;
     const uint32_t b0 = ld_b32(wr), b1 = ld_b32(wr + 8);
 #pragma unroll
-    for (int p = 0; p < 3; ++p) mma_bf16(y, A3[p], b0, b1);
+    for (int p = 0; p < TERMS; ++p) mma_bf16(y, A3[p], b0, b1);
   }
 
   // outputs 2q, 2q+1 of points ra (y[0], y[1]) and rb (y[2], y[3])
@@ -214,12 +250,12 @@ __device__ __forceinline__ void mma_eval16(const MMAShared& s, const TI* __restr
 }
 
 // Grid-stride loop of warps over tiles of 16 points.
-template <typename TI, typename TO>
+template <int TERMS, typename TI, typename TO>
 __device__ __forceinline__ void mma_eval_all(const MMAShared& s, const TI* __restrict__ g,
                                              TO* __restrict__ tau, int64_t ld, int64_t n) {
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  for (int64_t t = w0; t * 16 < n; t += warps) mma_eval16<TI, TO>(s, g, tau, ld, t * 16, n);
+  for (int64_t t = w0; t * 16 < n; t += warps) mma_eval16<TERMS, TI, TO>(s, g, tau, ld, t * 16, n);
 }
 
 }  // namespace gbs

@@ -1276,7 +1276,7 @@ int gbs_ns_spatial_means(gbs_ns* h, const void* S, double* out, void* stream) {
 int gbs_ns_set_turb_model(gbs_ns* h, int type, double C,
                           const gbs_mlp_weights* w) {
   gbs::clear_error();
-  if (!h || type < 0 || type > 2 || (type == 2 && !w)) {
+  if (!h || type < 0 || type > 3 || (type >= 2 && !w)) {
     gbs::set_error("gbs_ns_set_turb_model: invalid argument");
     return GBS_EINVAL;
   }
@@ -1297,7 +1297,7 @@ int gbs_ns_set_turb_model(gbs_ns* h, int type, double C,
   t.dky = s->q.dky;
   t.dkz = s->q.dkz;
   t.C_nu_T = C * (s->p.Lx / s->p.nx) * (s->p.Lx / s->p.nx) * sqrt(2.0);
-  if (type == 2) {
+  if (type >= 2) {
     t.w.W1 = static_cast<const __nv_bfloat16*>(w->W1);
     t.w.W2 = static_cast<const __nv_bfloat16*>(w->W2);
     t.w.W3 = static_cast<const __nv_bfloat16*>(w->W3);

@@ -78,14 +78,15 @@ __global__ void k_smagorinsky(const T* __restrict__ g, T* __restrict__ tau, int6
 
 // Pointwise MLP 9 -> 64 -> 64 -> 6 (tanh), BF16 weights, FP32 accumulation,
 // on the tensor cores: each warp evaluates tiles of 16 points with
-// mma.sync m16n8k16 (gbs_mlp_mma.cuh).
-template <typename T>
-__global__ void __launch_bounds__(256, GBS_MLP_MINB)
+// mma.sync m16n8k16 (gbs_mlp_mma.cuh); activations as three BF16 terms
+// (TERMS = 3) or one (TERMS = 1, the BF16 form).
+template <typename T, int TERMS>
+__global__ void __launch_bounds__(256, mlp_minb<TERMS>())
 k_mlp_closure(const T* __restrict__ g, T* __restrict__ tau, int64_t n, MLPWeights w) {
   __shared__ MMAShared sm;
   mma_stage(sm, w);
   __syncthreads();
-  mma_eval_all<T, T>(sm, g, tau, n, n);
+  mma_eval_all<TERMS, T, T>(sm, g, tau, n, n);
 }
 
 // f_i = coef * 1j * sum_j K_j t_hat_{ij}
@@ -138,8 +139,12 @@ int turb_forcing(const TurbCtx& t, const void* S, void* out, const void* extra,
   } else {
     int64_t nb = (nX + 127) / 128;  // 8 warps of 16 points
     if (nb > 152 * 8) nb = 152 * 8;
-    k_mlp_closure<T><<<(int)nb, 256, 0, st>>>(static_cast<const T*>(t.Gx),
-                                             static_cast<T*>(t.Tx), nX, t.w);
+    if (t.type == kTurbMLPBF16)
+      k_mlp_closure<T, 1><<<(int)nb, 256, 0, st>>>(static_cast<const T*>(t.Gx),
+                                                  static_cast<T*>(t.Tx), nX, t.w);
+    else
+      k_mlp_closure<T, 3><<<(int)nb, 256, 0, st>>>(static_cast<const T*>(t.Gx),
+                                                  static_cast<T*>(t.Tx), nX, t.w);
   }
   GBS_CHECK_LAUNCH();
   rc = gbs_fft_r2c(t.plan6, t.Tx, t.Tk, st);

@@ -10,7 +10,7 @@
 namespace gbs {
 
 constexpr int kIn = 9, kH = 64, kOut = 6;
-constexpr int kTurbNone = 0, kTurbSmagorinsky = 1, kTurbMLP = 2;
+constexpr int kTurbNone = 0, kTurbSmagorinsky = 1, kTurbMLP = 2, kTurbMLPBF16 = 3;
 
 // Device pointers of the closure network (row-major W[out][in]).
 struct MLPWeights {

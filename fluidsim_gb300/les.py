@@ -37,7 +37,8 @@ from .init_fields import cubic_dealias_cutoff, isotropic_3d
 from .solvers import SimulNS3D
 
 
-def make_sim(n, nu, cfl=0.5, precision="float32", turb=None, forcing=True, seed=0):
+def make_sim(n, nu, cfl=0.5, precision="float32", turb=None, forcing=True, seed=0,
+             closure_precision="fp32"):
     p = SimulNS3D.create_default_params()
     p.precision = precision
     p.oper.nx = p.oper.ny = p.oper.nz = n
@@ -59,7 +60,7 @@ def make_sim(n, nu, cfl=0.5, precision="float32", turb=None, forcing=True, seed=
         p.turb_model.enable, p.turb_model.type = True, "mlp_closure"
     sim = SimulNS3D(p)
     if turb is not None and turb != "smagorinsky":
-        sim.set_closure(turb)
+        sim.set_closure(turb, precision=closure_precision)
     return sim
 
 
@@ -221,11 +222,12 @@ def train_closure(G, Tau, steps=3000, batch=65536, lr=2e-3, lr_final=1e-4, seed=
                  "batch": batch, "samples": int(G.shape[1]), "lambda_pi": lambda_pi}
 
 
-def run_les(n, model, nu=3e-4, steps=2000, avg_last=1000, init=None, seed=0):
+def run_les(n, model, nu=3e-4, steps=2000, avg_last=1000, init=None, seed=0,
+            closure_precision="bf16"):
     """Forced LES; returns ((k, time-averaged E(k)), stats).  A run that
     produces NaN stops there and reports ``"nan": true`` (its spectrum is
     then the average of what was collected)."""
-    sim = make_sim(n, nu, turb=model, seed=seed)
+    sim = make_sim(n, nu, turb=model, seed=seed, closure_precision=closure_precision)
     if init is None:
         init = isotropic_3d(n, n, n, k0=3.0, energy=0.5, seed=seed)
     sim.state.init_statespect_from(**{k: init[i] for i, k in enumerate(sim.state.keys_state_spect)})
@@ -265,9 +267,11 @@ def spectral_error(k_les, E_les, k_ref, E_ref, kmin=1.0, kmax=None, reduce=np.me
 
 
 def pipeline(n_dns=512, n_les=128, nu=3e-4, t_coarse=6.0, t_fine=1.5, n_snap=4,
-             t_between=0.25, train_steps=3000, les_steps=2000, lambda_pi=1.0, seed=0):
+             t_between=0.25, train_steps=3000, les_steps=2000, lambda_pi=1.0, seed=0,
+             closure_precision="bf16"):
     out = {"config": {"n_dns": n_dns, "n_les": n_les, "nu": nu, "forcing": "tcrandom k in [2,3], P=1",
                       "closure": "MLP 9-64-64-6 tanh, BF16 weights, FP32 accumulation",
+                      "closure_precision_in_les": closure_precision,
                       "filter": "top-hat width L/n_les, then the LES grid's 2/3 truncation"}}
     snaps, (k_dns, E_dns), st_dns = forced_dns(n_dns, nu, t_coarse=t_coarse, t_fine=t_fine,
                                               n_snap=n_snap, t_between=t_between, seed=seed)
@@ -290,6 +294,7 @@ def pipeline(n_dns=512, n_les=128, nu=3e-4, t_coarse=6.0, t_fine=1.5, n_snap=4,
     res = {}
     for name, model in (("none", None), ("smagorinsky", "smagorinsky"), ("learned", net)):
         (k_l, E_l), st = run_les(n_les, model, nu=nu, steps=les_steps, avg_last=les_steps // 2,
+                                 closure_precision=closure_precision,
                                  init=init_les, seed=seed)
         st["spectral_error"] = spectral_error(k_l, E_l, k_f, E_f, kmin=1.0, kmax=kc)
         st["spectral_error_k_ge_4"] = spectral_error(k_l, E_l, k_f, E_f, kmin=4.0, kmax=kc)

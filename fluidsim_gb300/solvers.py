@@ -593,12 +593,16 @@ class SimulNS3D(_SimulBase):
                     f"Wrong value ('{tm.type}') of params.turb_model.type. "
                     "It should be in ('smagorinsky', 'mlp_closure')")
 
-    def set_closure(self, closure):
-        """Use a trained ``fluidsim_gb300.closure.ClosureMLP`` as turb model."""
+    def set_closure(self, closure, precision="fp32"):
+        """Use a trained ``fluidsim_gb300.closure.ClosureMLP`` as turb model
+        (precision "fp32" or "bf16", as ``closure.predict``)."""
+        from .closure import PRECISIONS
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision {precision!r} not in {PRECISIONS}")
         self._closure = closure  # keeps the device weights alive
         w = closure.c_weights()
-        _lib.check(self._lib.gbs_ns_set_turb_model(self._solver, 2, 0.0, ctypes.byref(w)),
-                   "turb_model")
+        _lib.check(self._lib.gbs_ns_set_turb_model(
+            self._solver, 2 if precision == "fp32" else 3, 0.0, ctypes.byref(w)), "turb_model")
         self.is_turb_model_enabled = True
 
     def _ns_params(self):

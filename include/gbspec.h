@@ -185,7 +185,10 @@ int gbs_ns_set_phase_shifts(gbs_ns* solver, const double* alpha, const double* b
  *   type 1: Smagorinsky with constant C (turb_model/smagorinsky.py:56-110,
  *           Delta = Lx / nx);
  *   type 2: learned closure, tau_ij = MLP(d_j u_i) (9 -> 64 -> 64 -> 6, tanh,
- *           BF16 weights, FP32 accumulation), forcing -d_j tau_ij.
+ *           BF16 weights, FP32 activations and accumulation), forcing
+ *           -d_j tau_ij;
+ *   type 3: the same network in BF16 form (activations rounded to BF16,
+ *           hardware tanh; relative error ~3e-3, see gbs_mlp_forward_bf16).
  * The weights are device pointers owned by the caller, read at every step.
  * Allocates the model's work buffers (synchronises the device). */
 typedef struct gbs_mlp_weights {
@@ -329,7 +332,11 @@ int gbs_velocity_gradients(const int64_t* shape, const double* L,
  * Fields are structure-of-arrays float32: g[c * ld + i] (9 rows, the
  * velocity gradients d_j u_i with c = 3 i + j), tau[o * ld + i] (6 rows,
  * xx yy zz xy xz yz).
- *   gbs_mlp_forward: tau = MLP(g) for points 0..n-1.
+ *   gbs_mlp_forward: tau = MLP(g) for points 0..n-1 (FP32 activations:
+ *     three BF16 terms per tensor-core operand).
+ *   gbs_mlp_forward_bf16: the same in BF16 form, the activations rounded to
+ *     BF16 operands and tanh by the hardware approximation (relative error
+ *     ~3e-3 against gbs_mlp_forward, a third of its tensor-core work).
  *   gbs_mlp_grad: loss over the `batch` points idx[0..batch-1] (device
  *     int64): mean squared error of MLP(g) / out_scale against
  *     tau / out_scale, plus pi_weight (>= 0) times the mean of
@@ -343,6 +350,8 @@ int gbs_velocity_gradients(const int64_t* shape, const double* L,
 int64_t gbs_mlp_grad_workspace(int64_t batch);
 int gbs_mlp_forward(const gbs_mlp_weights* w, const float* g, int64_t ld,
                     float* tau, int64_t n, void* stream);
+int gbs_mlp_forward_bf16(const gbs_mlp_weights* w, const float* g, int64_t ld,
+                         float* tau, int64_t n, void* stream);
 int gbs_mlp_grad(const gbs_mlp_weights* w, const float* g, const float* tau,
                  int64_t ld, const int64_t* idx, int64_t batch,
                  double pi_weight, void* workspace, float* grad, float* loss,

@@ -32,6 +32,21 @@ def test_forward_matches_oracle(cuda):
     assert np.abs(tau - ref).max() / np.abs(ref).max() < 1e-5
 
 
+def test_forward_bf16_close_to_oracle(cuda):
+    """The BF16 form (activations rounded to BF16, hardware tanh): relative
+    error of the order of the BF16 rounding (2^-9), not of FP32."""
+    from fluidsim_gb300.closure import predict
+    net, G, _ = _net_and_data(7000)
+    tau = predict(net, G, precision="bf16").cpu().numpy()
+    ref = _oracle(net).forward(G.cpu().numpy().astype(np.float64).T).T
+    err_max = np.abs(tau - ref).max() / np.abs(ref).max()
+    err_l2 = np.linalg.norm(tau - ref) / np.linalg.norm(ref)
+    assert err_max < 3e-2 and err_l2 < 1e-2, (err_max, err_l2)
+    assert err_l2 > 1e-5  # a different evaluation from the FP32 form
+    with pytest.raises(ValueError):
+        predict(net, G, precision="fp16")
+
+
 @pytest.mark.parametrize("pi_weight", [0.0, 0.05])
 def test_gradient_matches_oracle(cuda, pi_weight):
     import torch
