@@ -75,6 +75,21 @@ class StatePseudoSpectral:
     def has_vars(self, *keys):
         return set(keys).issubset(set(self.keys_state_spect + self.keys_state_phys))
 
+    def set_state_spect(self, tensor):
+        """Make the device tensor ``tensor`` (shape, dtype and device of
+        ``state_spect``, contiguous) the spectral state, without a copy: the
+        next steps read and update it in place.  Lets a caller rotate state
+        buffers, e.g. fill one from the host while a step runs on another."""
+        s = self.state_spect
+        if (not isinstance(tensor, torch.Tensor) or tensor.shape != s.shape
+                or tensor.dtype != s.dtype or tensor.device != s.device
+                or not tensor.is_contiguous()):
+            raise ValueError("set_state_spect: a contiguous tensor of shape "
+                             f"{tuple(s.shape)}, dtype {s.dtype} on {s.device} is required")
+        self.state_spect = tensor
+        self._phys = None
+        self.sim.time_stepping._dealiased_version = None
+
     def init_statespect_from(self, **kwargs):
         """``fluidsim/base/state.py:345-382``: other keys are set to zero."""
         self.state_spect.zero_()
@@ -182,8 +197,8 @@ class TimeSteppingPseudoSpectral:
         if hasattr(sim, "deltat_cap"):  # ns2d.strat: dispersion-relation time
             self.deltat_max = min(self.deltat_max, sim.deltat_cap())
         self._nan_check = True
-        # state_spect._version right after our last step: while it is
-        # unchanged the state is the dealiased output of that step
+        # (address, _version) of state_spect right after our last step:
+        # while both are unchanged the state is the dealiased output of it
         self._dealiased_version = None
 
         def handler(signum, stack):
@@ -246,7 +261,7 @@ class TimeSteppingPseudoSpectral:
             cfl = None  # dt already updated before the forcing was computed
         S = self.sim.state.state_spect
         flags = _lib.GBS_STEP_CHECK_NAN if self._nan_check else 0
-        if self._dealiased_version is not None and S._version == self._dealiased_version:
+        if self._dealiased_version == (S.data_ptr(), S._version):
             flags |= _lib.GBS_STEP_DEALIASED
         else:
             # a state set through torch: prune only if it is exactly zero
@@ -267,7 +282,7 @@ class TimeSteppingPseudoSpectral:
             self.sim._solver, self._scheme, ctypes.c_void_p(S.data_ptr()), ctypes.byref(dt),
             cfl, flags, current_stream_handle())
         self.deltat = dt.value
-        self._dealiased_version = S._version
+        self._dealiased_version = (S.data_ptr(), S._version)
         self.sim.state._phys = None
         if rc == _lib.GBS_ENAN:
             raise ValueError(f"nan at it = {self.it}, t = {self.t:.4f}")
