@@ -191,3 +191,26 @@ def test_max_velocity_matches_state_phys(cuda):
     vmax = sim.max_velocity()
     phys = sim.state.state_phys.cpu().numpy()
     np.testing.assert_allclose(vmax, np.abs(phys).reshape(3, -1).max(axis=1), rtol=1e-14)
+
+
+def test_set_state_spect_rotation_matches_in_place(cuda):
+    """Steps on rotated state buffers (set_state_spect) give the same states
+    as steps on one buffer; a tensor of another shape or dtype is refused."""
+    import torch
+    sim_a, d, _ = make_sim("ns3d_iso_24x16x32_f")
+    sim_b, _, _ = make_sim("ns3d_iso_24x16x32_f")
+    S0 = sim_a.state.state_spect.clone()
+    bufs = [torch.empty_like(S0) for _ in range(3)]
+    for i in range(4):
+        sim_a.time_stepping.one_time_step()
+        nxt = bufs[i % 3]
+        nxt.copy_(sim_b.state.state_spect)
+        sim_b.state.set_state_spect(nxt)
+        sim_b.time_stepping.one_time_step()
+        assert sim_b.state.state_spect.data_ptr() == nxt.data_ptr()
+        assert torch.equal(sim_a.state.state_spect, nxt)
+    with pytest.raises(ValueError):
+        sim_b.state.set_state_spect(S0[:2].clone())
+    with pytest.raises(ValueError):
+        sim_b.state.set_state_spect(S0.to(torch.complex64 if S0.dtype == torch.complex128
+                                          else torch.complex128))
