@@ -81,9 +81,21 @@ def test_ns3d_fast_fp32_error(cuda):
 
 
 def test_ns3d_fast_fp32_nx512_error(cuda):
-    """nx = 512 in FP32 runs the 16 x 16 x pass (CFL maxima and f included)."""
+    """nx = 512 in FP32 runs the register x pass (kf3_xr: the six fields of a
+    row pair by one group of 64 threads, named barriers; CFL maxima and f
+    included)."""
     # a 2 pi cube: the energetic modes (|k| ~ 4) vary along y and z too
     sim, orc = run_3d((32, 32, 512), "float32", 6, USE_CFL=True, cfl_coef=0.5, f=0.7,
+                      L=(2 * pi,) * 3)
+    got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
+    assert rel(got, orc.state_spect) < 1e-5
+    assert abs(sim.time_stepping.deltat - orc.deltat) <= 1e-5 * orc.deltat
+
+
+def test_ns3d_fast_fp32_nx256_error(cuda):
+    """nx = 256 in FP32: the register x pass on 256-point lines inside one
+    warp (8 row pairs per CTA), CFL maxima included."""
+    sim, orc = run_3d((32, 32, 256), "float32", 5, USE_CFL=True, cfl_coef=0.5,
                       L=(2 * pi,) * 3)
     got = sim.state.state_spect.cpu().numpy().astype(np.complex128)
     assert rel(got, orc.state_spect) < 1e-5
