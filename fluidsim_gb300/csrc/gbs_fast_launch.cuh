@@ -9,16 +9,21 @@
 namespace gbs {
 namespace fast {
 
-// columns per CTA for the strided passes: 64 B segments in FP32 and FP64;
-// FP32 widths per pass are compile-time knobs (A/B at 512^3)
+// columns per CTA for the strided passes (FP64: 4, 64 B segments); FP32
+// widths per pass are compile-time knobs, set by A/B at 512^3 (ms per pruned
+// launch): the plain column kernel 8 (16: inverse y 0.94 -> 1.11, and the
+// z passes of the standalone FFT 0.80 -> 0.85 ms per transform), the fused
+// z passes of the ns3d step 16 (128 B segments of lines 1 MB apart: curl +
+// inverse z 0.779 -> 0.756, forward z + RK4 0.843 -> 0.758; 4: 1.146 and
+// 1.281)
 #ifndef GBS_TX_COL
 #define GBS_TX_COL 8
 #endif
 #ifndef GBS_TX_INVZ
-#define GBS_TX_INVZ 8
+#define GBS_TX_INVZ 16
 #endif
 #ifndef GBS_TX_FWDZ
-#define GBS_TX_FWDZ 8
+#define GBS_TX_FWDZ 16
 #endif
 // (capped so that a CTA has at most 1024 threads: TX * N / 8 <= 1024)
 constexpr int tx_cap(int tx, int logn) { return tx * (1 << logn) / 8 <= 1024 ? tx : 8192 >> logn; }
