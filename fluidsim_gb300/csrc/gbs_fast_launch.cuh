@@ -30,11 +30,15 @@ constexpr int tx_cap(int tx, int logn) { return tx * (1 << logn) / 8 <= 1024 ? t
 template <typename T, int LOGN> constexpr int tx_cols() {
   return tx_cap(sizeof(T) == 4 ? GBS_TX_COL : 4, LOGN);
 }
+// FP64 z passes: 4 columns (8: 512^3 FP64 3.20 -> 3.17 steps/s)
+#ifndef GBS_TX_Z64
+#define GBS_TX_Z64 4
+#endif
 template <typename T, int LOGN> constexpr int tx_invz() {
-  return tx_cap(sizeof(T) == 4 ? GBS_TX_INVZ : 4, LOGN);
+  return tx_cap(sizeof(T) == 4 ? GBS_TX_INVZ : GBS_TX_Z64, LOGN);
 }
 template <typename T, int LOGN> constexpr int tx_fwdz() {
-  return tx_cap(sizeof(T) == 4 ? GBS_TX_FWDZ : 4, LOGN);
+  return tx_cap(sizeof(T) == 4 ? GBS_TX_FWDZ : GBS_TX_Z64, LOGN);
 }
 // rows per CTA for the x passes
 #ifndef GBS_X_THREADS
