@@ -16,6 +16,7 @@
 
 #include "gbs_internal.cuh"
 #include "gbs_ns.cuh"
+#include "gbs_fast_api.h"
 
 namespace gbs {
 namespace fast {
@@ -116,6 +117,66 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 // Fetch bytes [p, p + n) into L2 (p 16-byte aligned, n a multiple of 16).
 __device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned n) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(n) : "memory");
+}
+
+// mbarrier and bulk-copy primitives (one CTA, no cluster).
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count)
+               : "memory");
+}
+// makes initialised mbarriers visible to the asynchronous proxy
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier shared-memory accesses before later
+// asynchronous-proxy (bulk copy) accesses
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// one arrival that also expects `bytes` of transactions on the phase
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* m, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)),
+               "r"(bytes)
+               : "memory");
+}
+// bytes [src, src + n) of global memory to shared memory at dst; completes
+// n bytes of transactions on mbarrier m (src, dst 16-byte aligned, n a
+// multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned n, uint64_t* m) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(n), "r"(smem_u32(m))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_test_parity(uint64_t* m, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+      "selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait until the phase of parity `parity` of m has completed, for at most
+// timeout_ns; false when the time ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* m, unsigned parity,
+                                                  unsigned long long timeout_ns) {
+  if (mbar_test_parity(m, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (mbar_test_parity(m, parity)) return true;
+    if (global_ns() - t0 > timeout_ns) return false;
+  }
 }
 
 // Asynchronous copy of one complex value into shared memory (zeros when
@@ -809,6 +870,17 @@ __device__ __forceinline__ const X* opaque(const X* p) {
   return r;
 }
 
+// Shared memory of one row pair of kf3_xr, in complex elements: exchange
+// slot(s), partner half-line, stash, two staging buffers of two rows
+// (N/2 + 1 modes each); a multiple of 16 elements, so that every pair's
+// exchange slot starts a 128-byte bank sweep.
+template <int LOGN>
+__host__ __device__ constexpr int xr_slot() {
+  constexpr int N = 1 << LOGN, H = N / 2, E = 16;
+  constexpr int n = N + (xp_alt<LOGN>() ? N : 0) + (H > E ? H : E) + N + 2 * (N + 2);
+  return (n + E - 1) / E * E;
+}
+
 // Register index holding stage-0 position jt + r N/8 in the output order of
 // run(): the i with Line::outm(i) == r.
 template <int LOGN>
@@ -835,16 +907,28 @@ __device__ __forceinline__ constexpr int inv_outm(int r) {
 // arrive (ox: p_y, p_z; oy: p_z complete, p_x; oz: p_x, p_y complete); p_z
 // is transformed before oz, and vx waits in shared memory (each thread
 // reads back only its own values), so at most four lines are held in
-// registers besides the line being transformed.  The split of each product line into the two
-// rows' spectra reads Z[N - k] from a half-line region that holds
-// positions N/2 .. N-1.  Barriers: the pair's two exchange slots alternate
-// (three-stage lines), so consecutive transforms need no barrier of their
-// own (a slot is written again only after a barrier that every reader of
-// its previous contents has passed).  Not for ns3d.strat (kf3_xp).
+// registers besides the line being transformed.  The split of each product
+// line into the two rows' spectra reads Z[N - k] from a half-line region
+// that holds positions N/2 .. N-1.  Barriers: the pair's two exchange slots
+// alternate (three-stage lines), so consecutive transforms need no barrier
+// of their own (a slot is written again only after a barrier that every
+// reader of its previous contents has passed).  Not for ns3d.strat
+// (kf3_xp).
+//
+// Inputs: the kept modes of the two rows of field f arrive by two bulk
+// copies (cp.async.bulk) into one of two staging buffers of the pair,
+// issued two fields ahead by thread 0 of the pair and awaited on the
+// buffer's mbarrier.  Rows have nx/2 + 1 modes and row0 is even, so row0
+// starts 16-byte aligned and row0 + 1 8 bytes past a 16-byte boundary: its
+// copy starts at the last mode of row0 (the Nyquist mode, which a pruned
+// pass does not read); the wait is bounded by
+// xs.timeout_ns, after which *xs.status is set and the pass goes on (the
+// step then returns GBS_ETIMEDOUT).  Fields 2..5 are also prefetched into
+// L2 at the start.  The grid must cover whole pairs (nz ny even).
 template <typename T, int LOGN, int LP>
 __global__ void __launch_bounds__(LP * (1 << LOGN) / 8, GBS_XR_MINB)
 kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
-       const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
+       const cplx<T>* __restrict__ twx, unsigned long long* vmax, XStage xs) {
   using C = cplx<T>;
   using P = Line<LOGN>;
   constexpr int N = P::N, N8 = P::N8, H = N / 2;
@@ -852,61 +936,80 @@ kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   constexpr int E = 128 / sizeof(C);
   constexpr int ALT = xp_alt<LOGN>() ? N : 0;
   constexpr int PART = H > E ? H : E;
-  constexpr int SLOT = N + ALT + PART + N;  // exchange slots, partner half, stash
+  constexpr int RB = N + 2;  // staging buffer: two rows of N/2 + 1 modes
+  constexpr int SLOT = xr_slot<LOGN>();
   static_assert(P::NST >= 2, "a line needs at least one exchange");
+  static_assert((N + ALT + PART + N) % 2 == 0 && RB % 2 == 0, "16-byte aligned buffers");
+  __shared__ uint64_t mbar[LP][2];
   C* buf = reinterpret_cast<C*>(g_smem_fast);
   const int jt = threadIdx.x % N8;
   const int lp = threadIdx.x / N8;
   const int64_t nrows = (int64_t)g.nz * g.ny;
   const int64_t nK = nrows * g.nkx;
   const int64_t row0 = ((int64_t)blockIdx.x * LP + lp) * 2;
-  const bool v0 = row0 < nrows, v1 = row0 + 1 < nrows;
+  const bool v0 = row0 < nrows;  // the pair (row0 + 1 < nrows with it)
   const SwzView<C, 1> acc{buf + lp * SLOT, 0};
   const SwzView<C, 1> part{buf + lp * SLOT + N + ALT, 0};
   C* stash = buf + lp * SLOT + N + ALT + PART;
+  C* stage = stash + N;  // stage + b * RB: staging buffer b
   const int bar = WARP ? 0 : 1 + lp;
   const int kcx = g.pr ? g.kcx : g.nkx + 1;
-  const int nout = g.pr ? (g.kcx < g.nkx ? g.kcx : g.nkx) : g.nkx;
+  const int nk = kcx < g.nkx ? kcx : g.nkx;  // kept modes of a row
+  const int nout = nk;
   const C* r0base = W + row0 * g.nkx;
-  // the pair's rows of fields 1..5 into L2 now (one bulk prefetch per row,
-  // its kept modes; 16-byte aligned inside the row), so that the loads of
-  // each field, issued only after the previous field's transform, hit L2
-  if (jt < 10) {
-    const int f = 1 + jt / 2, rr = jt & 1;
-    if (rr == 0 ? v0 : v1) {
-      const int nk = kcx < g.nkx ? kcx : g.nkx;
-      const char* a = reinterpret_cast<const char*>(r0base + f * nK + rr * g.nkx);
-      const char* a16 = reinterpret_cast<const char*>(reinterpret_cast<uintptr_t>(a) & ~uintptr_t(15));
-      const unsigned bytes = (unsigned)((a + nk * sizeof(C) - a16) & ~size_t(15));
-      if (bytes) prefetch_l2_bulk(a16, bytes);
-    }
+  // copy of row0: modes 0 .. nk - 1 rounded up to 16 bytes, at most up to
+  // mode nkx - 2 (the row's last mode comes with the copy of row0 + 1);
+  // copy of row0 + 1: from mode nkx - 1 of row0 to mode nk - 1 of row0 + 1,
+  // rounded up to 16 bytes (at most to its last mode), into buffer slots
+  // nkx - 1 .. (row0 + 1 at nkx .. 2 nkx - 1)
+  const unsigned c0bytes = (unsigned)min((nk * sizeof(C) + 15) & ~size_t(15),
+                                         (size_t)(g.nkx - 1) * sizeof(C));
+  const unsigned c1bytes = (unsigned)(((nk + 1) * sizeof(C) + 15) & ~size_t(15));
+  if (jt == 0) {
+    mbar_init(&mbar[lp][0], 1);
+    mbar_init(&mbar[lp][1], 1);
+    mbar_init_fence();
   }
+  if (jt < 8 && v0) {  // fields 2..5 into L2
+    const C* a = r0base + (2 + (jt >> 1)) * nK;
+    if (jt & 1) prefetch_l2_bulk(a + g.nkx - 1, c1bytes);
+    else prefetch_l2_bulk(a, c0bytes);
+  }
+  line_sync<WARP, N8>(bar);  // the barriers are initialised
 
-  // raw inputs of field f at this thread's eight positions (rows row0 and
-  // row0 + 1), loaded one transform ahead of their use
-  auto load = [&](int f, C(&a0)[8], C(&a1)[8]) {
-    const C* r0 = opaque(r0base) + f * nK;
+  // field f into staging buffer b (thread 0 of the pair)
+  auto issue = [&](int f, int b) {
+    if (jt != 0 || !v0) return;
+    if (xs.stall && f == 5 && blockIdx.x == 0 && lp == 0) return;  // test hook
+    fence_proxy_async();  // the buffer's earlier reads come first
+    mbar_arrive_expect_tx(&mbar[lp][b], c0bytes + c1bytes);
+    const C* src = r0base + f * nK;
+    bulk_g2s(stage + b * RB, src, c0bytes, &mbar[lp][b]);
+    bulk_g2s(stage + b * RB + g.nkx - 1, src + g.nkx - 1, c1bytes, &mbar[lp][b]);
+  };
+  // inverse transform of field f (staging buffer f % 2) into v (output
+  // order of run())
+  auto inverse = [&](int f, C(&v)[8]) {
+    const int b = f & 1;
+    if (v0 && !mbar_wait_bounded(&mbar[lp][b], (f >> 1) & 1, xs.timeout_ns))
+      atomicOr(xs.status, 1);
+    const C* r0 = stage + b * RB;
     const C* r1 = r0 + g.nkx;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int idx = r < 4 ? jt + r * N8 : (8 - r) * N8 - jt;
-      const bool in = idx < kcx;
-      a0[r] = (v0 && in) ? r0[idx] : mk<C>(0, 0);
-      a1[r] = (v1 && in) ? r1[idx] : mk<C>(0, 0);
-    }
-  };
-  // inverse transform of the raw inputs into v (output order of run())
-  auto inverse = [&](C(&a0)[8], C(&a1)[8], C(&v)[8]) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
+      const bool in = v0 && idx < kcx;
+      C a0 = in ? r0[idx] : mk<C>(0, 0);
+      C a1 = in ? r1[idx] : mk<C>(0, 0);
       if ((r == 0 || r == 4) && jt == 0) {
-        a0[r].y = 0;
-        a1[r].y = 0;
+        a0.y = 0;
+        a1.y = 0;
       }
-      v[r] = r < 4 ? mk<C>(a0[r].x - a1[r].y, a0[r].y + a1[r].x)
-                   : mk<C>(a0[r].x + a1[r].y, a1[r].x - a0[r].y);
+      v[r] = r < 4 ? mk<C>(a0.x - a1.y, a0.y + a1.x) : mk<C>(a0.x + a1.y, a1.x - a0.y);
     }
     run<+1, LOGN, WARP, ALT>(v, jt, true, acc, opaque(twx), 1, bar);
+    // every thread of the pair has read the buffer (run's barriers)
+    if (f + 2 <= 5) issue(f + 2, b);
   };
   // forward transform of product line p (output order of run()) into field f
   auto forward = [&](int f, const C(&p)[8]) {
@@ -924,45 +1027,36 @@ kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 #pragma unroll
     for (int r = 0; r <= 4; ++r) {
       const int k = r < 4 ? jt + r * N8 : H;
-      if ((r == 4 && jt != 0) || k >= nout) continue;
+      if ((r == 4 && jt != 0) || k >= nout || !v0) continue;
       const C z = v[inv_outm<LOGN>(r)];
       const C m = (k == 0 || k == H) ? z : part(N - k - H);
-      if (v0) F0[k] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
-      if (v1) F1[k] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
+      F0[k] = mk<C>(h * (z.x + m.x), h * (z.y - m.y));
+      F1[k] = mk<C>(h * (z.y + m.y), h * (m.x - z.x));
     }
   };
 
+  issue(0, 0);
+  issue(1, 1);
   T mx = 0, my = 0, mz = 0;
   auto vmax_of = [](const C(&v)[8], T& m) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) m = fmax(m, fmax(fabs(v[i].x), fabs(v[i].y)));
   };
-  // two raw buffers: the loads of the next field are in flight during the
-  // current transform, except oz's, issued after p_z's forward transform
-  // (its raw inputs there would take the live floats from 80 to 96 and
-  // spill at 128 registers); every field after the first is already on its
-  // way to L2 (bulk prefetch above)
-  C a0[8], a1[8], b0[8], b1[8];
-  load(0, a0, a1);
-  load(1, b0, b1);
   {
     C v[8];
-    inverse(a0, a1, v);  // vx waits in this thread's own stash slots
+    inverse(0, v);  // vx waits in this thread's own stash slots
     vmax_of(v, mx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) stash[i * N8 + jt] = v[i];
   }
-  load(2, a0, a1);
   C vy[8], vz[8], px[8], py[8], pz[8];
-  inverse(b0, b1, vy);
+  inverse(1, vy);
   vmax_of(vy, my);
-  load(3, b0, b1);
-  inverse(a0, a1, vz);
+  inverse(2, vz);
   vmax_of(vz, mz);
-  load(4, a0, a1);
   {
     C o[8];
-    inverse(b0, b1, o);  // ox
+    inverse(3, o);  // ox
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       py[i] = mk<C>(vz[i].x * o[i].x, vz[i].y * o[i].y);
@@ -971,7 +1065,7 @@ kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
   }
   {
     C o[8];
-    inverse(a0, a1, o);  // oy
+    inverse(4, o);  // oy
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const C vx = stash[i * N8 + jt];
@@ -980,10 +1074,9 @@ kf3_xr(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
     }
   }
   forward(2, pz);
-  load(5, b0, b1);
   {
     C o[8];
-    inverse(b0, b1, o);  // oz
+    inverse(5, o);  // oz
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const C vx = stash[i * N8 + jt];

@@ -13,6 +13,14 @@ namespace fast {
 struct ColArgs;
 struct Geo;
 
+// Staging of the x pass's inputs (kf3_xr): bulk copies into shared memory
+// whose completion is awaited on mbarriers with a bounded wait.
+struct XStage {
+  int* status;                    // device word: set to 1 when a wait ran out
+  unsigned long long timeout_ns;  // limit of each wait
+  int stall;                      // test hook: one copy of the launch is never issued
+};
+
 // Axis lengths with compiled kernels: 2^kMinLog .. 2^kMaxLog.
 constexpr int kMinLog = 5;
 constexpr int kMaxLog = 10;
@@ -32,7 +40,7 @@ template <typename T>
 int A3(const Geo& g, const void* S, void* W, const void* twz, cudaStream_t st);
 template <typename T>
 int B3(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
-       cudaStream_t st);
+       const XStage& xs, cudaStream_t st);
 template <typename T>
 int C3(const Geo& g, const void* F, const void* twz, int mode, const RKArgs& a,
        cudaStream_t st);

@@ -249,30 +249,29 @@ static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
 // registers it needs spill and kf3_xp is 3-4 % faster.
 template <typename T, int LOGM>
 static int B3r_launch(const Geo& g, const void* W, void* F, const void* tw,
-                      unsigned long long* vmax, cudaStream_t st) {
+                      unsigned long long* vmax, const XStage& xs, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int LOGN = LOGM + 1, N = 1 << LOGN, N8 = N / 8;
+  constexpr int LOGN = LOGM + 1, N8 = (1 << LOGN) / 8;
   constexpr int LP = GBS_XR_THREADS / N8 > 0 ? GBS_XR_THREADS / N8 : 1;
   static_assert(N8 <= 32 || LP <= 15, "one named barrier per pair (ids 1..15)");
   constexpr int TH = LP * N8;
-  constexpr int E = 128 / sizeof(C);
-  constexpr int PART = N / 2 > E ? N / 2 : E;
-  const size_t smem = sizeof(C) * (size_t)LP * (N + (xp_alt<LOGN>() ? N : 0) + PART + N);
+  const size_t smem = sizeof(C) * (size_t)LP * xr_slot<LOGN>();
   int rc = prep(kf3_xr<T, LOGN, LP>, smem);
   if (rc) return rc;
   const int64_t npairs = ((int64_t)g.nz * g.ny + 1) / 2;
   kf3_xr<T, LOGN, LP><<<ceil_div(npairs, LP), TH, smem, st>>>(
-      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax);
+      static_cast<const C*>(W), static_cast<C*>(F), g, static_cast<const C*>(tw), vmax, xs);
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
 
 template <typename T, int LOGM, bool ST>
 static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
-                   unsigned long long* vmax, cudaStream_t st) {
+                   unsigned long long* vmax, const XStage& xs, cudaStream_t st) {
 #ifndef GBS_X_NOREG
+  // (whole row pairs: the pair's staging copy spans both rows)
   if constexpr (sizeof(T) == 4 && !ST && (LOGM == 7 || LOGM == 8))
-    return B3r_launch<T, LOGM>(g, W, F, tw, vmax, st);
+    if (((int64_t)g.nz * g.ny) % 2 == 0) return B3r_launch<T, LOGM>(g, W, F, tw, vmax, xs, st);
 #endif
   if constexpr (sizeof(T) == 4 && LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
   else return B3_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
@@ -280,11 +279,11 @@ static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
 
 template <typename T>
 int B3(const Geo& g, const void* W, void* F, const void* twx, unsigned long long* vmax,
-       cudaStream_t st) {
+       const XStage& xs, cudaStream_t st) {
   if (g.strat) {
-    GBS_LOG_SWITCH(ilog2(g.M), return (B3_pick<T, LG, true>(g, W, F, twx, vmax, st)));
+    GBS_LOG_SWITCH(ilog2(g.M), return (B3_pick<T, LG, true>(g, W, F, twx, vmax, xs, st)));
   } else {
-    GBS_LOG_SWITCH(ilog2(g.M), return (B3_pick<T, LG, false>(g, W, F, twx, vmax, st)));
+    GBS_LOG_SWITCH(ilog2(g.M), return (B3_pick<T, LG, false>(g, W, F, twx, vmax, xs, st)));
   }
   return GBS_OK;
 }
@@ -419,7 +418,7 @@ int C2(const Geo& g, const void* F, const void* twy, int mode, const RKArgs& a,
                       int, cudaStream_t);                                                    \
   template int A3<T>(const Geo&, const void*, void*, const void*, cudaStream_t);             \
   template int B3<T>(const Geo&, const void*, void*, const void*, unsigned long long*,       \
-                     cudaStream_t);                                                          \
+                     const XStage&, cudaStream_t);                                           \
   template int C3<T>(const Geo&, const void*, const void*, int, const RKArgs&, cudaStream_t); \
   template int A2<T>(const Geo&, const void*, void*, const void*, cudaStream_t);             \
   template int B2<T>(const Geo&, const void*, void*, const void*, unsigned long long*,       \

@@ -373,6 +373,9 @@ constexpr int kKinds = 5;     // A, inverse y, B, forward y, C
 constexpr int kMaxEv = 2048;  // event pairs recorded before a harvest
 
 constexpr int kHostBuf = 16;  // doubles in the pinned host mirror
+// limit of a device-side wait for a staging copy (the copies take
+// microseconds; a wait this long means the copy engine failed)
+constexpr unsigned long long kStageTimeoutNs = 1000000000ull;
 
 struct Solver {
   gbs_ns_params p;
@@ -387,7 +390,8 @@ struct Solver {
   void* tmp1;
   void* tmp2;                // RK2_phaseshift_exact only (allocated at first use)
   unsigned long long* dmax;  // 3 maxima (double bits)
-  int* dflag;
+  int* dflag;                // [0] NaN flag, [1] staging status of the x pass (sticky)
+  int stall_test;            // test hook for the next x pass (GBS_STEP_TEST_STALL)
   double* dred;              // reduction partials
   double* hbuf;              // pinned host mirror (kHostBuf doubles)
   double* hbuf_dev;          // the same memory in the device address space
@@ -553,7 +557,10 @@ static int eval_fast(Solver* s, const void* in, bool pruned, bool want_max, int 
     if (rc) return rc;
     {
       LaunchScope ls(s, 2, st);
-      rc = fast::B3<T>(g, s->W, s->F, s->tw[0], vmax, st);
+      fast::XStage xs{s->dflag + 1, s->stall_test ? 1000000ull : kStageTimeoutNs,
+                      s->stall_test};
+      s->stall_test = 0;
+      rc = fast::B3<T>(g, s->W, s->F, s->tw[0], vmax, xs, st);
     }
     if (rc) return rc;
     ca.kc_in = g.ny + 1;
@@ -782,6 +789,7 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
                 cudaStream_t st) {
   const int check_nan = flags & GBS_STEP_CHECK_NAN;
   const bool pr = (flags & GBS_STEP_DEALIASED) != 0;
+  s->stall_test = (flags & GBS_STEP_TEST_STALL) ? 1 : 0;
   Stage stages[4];
   const int nst = scheme_stages(scheme, stages);
   if (nst == 0) {
@@ -851,11 +859,17 @@ static int step(Solver* s, int scheme, void* S, double* dt, const double* cfl, i
     if (rc) return rc;
   }
   if (check_nan) {
-    rc = publish(s, s->dflag, 4, sizeof(int), st);
+    rc = publish(s, s->dflag, 4, 2 * sizeof(int), st);
     if (rc) return rc;
-    int flag;
-    memcpy(&flag, s->hbuf + 4, sizeof(int));
-    if (flag) {
+    int flag[2];
+    memcpy(flag, s->hbuf + 4, sizeof(flag));
+    if (flag[1]) {  // reported once, then cleared
+      GBS_CUDA_TRY(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), st));
+      set_error("x pass: a staging copy did not arrive within the time limit "
+                "(the step's result is not valid)");
+      return GBS_ETIMEDOUT;
+    }
+    if (flag[0]) {
       set_error("nan in state_spect[0] after the time step");
       return GBS_ENAN;
     }
@@ -1150,7 +1164,7 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
         cudaMalloc(&s->tmp, fb * s->nvar) != cudaSuccess ||
         cudaMalloc(&s->tmp1, fb * s->nvar) != cudaSuccess ||
         cudaMalloc(&s->dmax, 4 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMalloc(&s->dflag, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&s->dflag, 2 * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&s->dred, sizeof(double) * (gbs::kNQ * gbs::kRedBlocks + 16)) != cudaSuccess ||
         cudaHostAlloc(&s->hbuf, gbs::kHostBuf * sizeof(double), cudaHostAllocMapped) !=
             cudaSuccess ||
@@ -1159,6 +1173,10 @@ int gbs_ns_create(const gbs_ns_params* prm, gbs_ns** out) {
                      (size_t)(fb * (nW + nF + 2 * s->nvar) >> 20));
       rc = GBS_ENOMEM;
     }
+  }
+  if (!rc && cudaMemset(s->dflag, 0, 2 * sizeof(int)) != cudaSuccess) {
+    gbs::set_error("gbs_ns_create: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = GBS_ECUDA;
   }
   if (!rc) rc = p.dtype == GBS_F64 ? gbs::setup_shapes<double>(s) : gbs::setup_shapes<float>(s);
   if (!rc) {

@@ -140,7 +140,13 @@ int gbs_ns_tendencies(gbs_ns* solver, const void* state_spect, void* tend,
  * synchronises the stream once.  With GBS_STEP_CHECK_NAN, returns GBS_ENAN
  * (after completing the step) when state_spect[0] holds a NaN.  With
  * GBS_STEP_DEALIASED the caller asserts that the state is dealiased; the
- * result is the same, the transforms skip the modes the 2/3 rule zeroes. */
+ * result is the same, the transforms skip the modes the 2/3 rule zeroes.
+ * The FP32 ns3d x pass stages its inputs with bulk copies awaited on
+ * mbarriers (bounded waits, 1 s); if a wait runs out the step completes
+ * with an invalid result and, at the next step with GBS_STEP_CHECK_NAN,
+ * returns GBS_ETIMEDOUT (once).  GBS_STEP_TEST_STALL (test hook, defined
+ * below) withholds one staging copy of the step's first x pass and waits
+ * 1 ms for it. */
 int gbs_ns_step_rk4(gbs_ns* solver, void* state_spect, double* dt,
                     const double* cfl, int flags, void* stream);
 

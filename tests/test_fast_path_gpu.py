@@ -277,3 +277,48 @@ def test_pruned_step_is_bit_identical_and_detected(cuda, precision, shape):
     assert is_dealiased(c) == 0
     c[1, 0, 0, kc] = 0
     assert is_dealiased(c) == 1
+
+
+def test_x_pass_staging_timeout_is_reported(cuda):
+    """The FP32 x pass at nx = 512 stages each field's rows by a bulk copy
+    awaited on an mbarrier with a bounded wait.  The test hook withholds one
+    copy: the wait runs out (1 ms), the step returns GBS_ETIMEDOUT once, the
+    context stays usable and the next steps equal those of a fresh solver."""
+    import ctypes
+    import torch
+    from fluidsim_gb300 import _lib
+    from fluidsim_gb300.fft import current_stream_handle
+    from fluidsim_gb300.init_fields import isotropic_3d
+    from fluidsim_gb300.solvers import SimulNS3D
+    nz, ny, nx = 32, 32, 512
+    L = (2 * pi,) * 3
+
+    def make():
+        p = SimulNS3D.create_default_params()
+        p.precision = "float32"
+        p.oper.nx, p.oper.ny, p.oper.nz = nx, ny, nz
+        p.oper.Lx, p.oper.Ly, p.oper.Lz = L
+        p.nu_2 = 1e-3
+        sim = SimulNS3D(p)
+        v0 = isotropic_3d(nx, ny, nz, *L, seed=5)
+        sim.state.init_statespect_from(vx_fft=v0[0], vy_fft=v0[1], vz_fft=v0[2])
+        sim.oper.dealiasing(sim.state.state_spect)
+        return sim
+
+    def step(sim, S, flags):
+        dt = ctypes.c_double(2e-3)
+        return sim._lib.gbs_ns_step_rk4(sim._solver, ctypes.c_void_p(S.data_ptr()),
+                                        ctypes.byref(dt), None, flags, current_stream_handle())
+
+    base = _lib.GBS_STEP_CHECK_NAN | _lib.GBS_STEP_DEALIASED
+    sim, ref = make(), make()
+    S0 = sim.state.state_spect.clone()
+    S = sim.state.state_spect
+    assert step(sim, S, base | _lib.GBS_STEP_TEST_STALL) == _lib.GBS_ETIMEDOUT
+    assert "staging copy" in _lib.load().gbs_last_error().decode()
+    S.copy_(S0)
+    for _ in range(2):
+        assert step(sim, S, base) == _lib.GBS_OK
+        assert step(ref, ref.state.state_spect, base) == _lib.GBS_OK
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(S), torch.view_as_real(ref.state.state_spect))
