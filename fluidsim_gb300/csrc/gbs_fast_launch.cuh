@@ -244,9 +244,17 @@ static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
 }
 
 // Rows in pairs with the products in registers (kf3_xr): FP32 ns3d, LP
-// pairs per CTA up to GBS_XR_THREADS threads.  Used for nx = 256 and 512
-// (x pass -6 % and -3 % against kf3_xp); at nx = 128 and 1024 the 128
-// registers it needs spill and kf3_xp is 3-4 % faster.
+// pairs per CTA up to GBS_XR_THREADS threads.  Used for nx = 256 .. 1024
+// (ms per pruned launch against kf3_xp: nx = 256 0.150 / 0.185 at 256^3,
+// 512 1.210 / 1.324 at 512^3, 1024 0.412 / 0.452 at 1024x256x128); at
+// nx = 64 and 128 its 16 warps per SM lose to kf3_xp's occupancy (0.0142 /
+// 0.0101 at 64^3, 0.0407 / 0.0283 at 128^3).
+#ifndef GBS_XR_LOGM_MIN
+#define GBS_XR_LOGM_MIN 7
+#endif
+#ifndef GBS_XR_LOGM_MAX
+#define GBS_XR_LOGM_MAX 9
+#endif
 template <typename T, int LOGM>
 static int B3r_launch(const Geo& g, const void* W, void* F, const void* tw,
                       unsigned long long* vmax, const XStage& xs, cudaStream_t st) {
@@ -270,7 +278,7 @@ static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
                    unsigned long long* vmax, const XStage& xs, cudaStream_t st) {
 #ifndef GBS_X_NOREG
   // (whole row pairs: the pair's staging copy spans both rows)
-  if constexpr (sizeof(T) == 4 && !ST && (LOGM == 7 || LOGM == 8))
+  if constexpr (sizeof(T) == 4 && !ST && LOGM >= GBS_XR_LOGM_MIN && LOGM <= GBS_XR_LOGM_MAX)
     if (((int64_t)g.nz * g.ny) % 2 == 0) return B3r_launch<T, LOGM>(g, W, F, tw, vmax, xs, st);
 #endif
   if constexpr (sizeof(T) == 4 && LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
