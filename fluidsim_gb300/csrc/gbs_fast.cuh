@@ -358,8 +358,14 @@ struct ColArgs {
   int pf;  // L2 prefetch distance in grid rows (0: none); set by the launcher
 };
 
-template <typename T, int LOGN, int TX, int DIR>
-__global__ void __launch_bounds__(TX * (1 << LOGN) / 8, min_blocks(TX * (1 << LOGN) / 8))
+// SLOT1: one exchange slot (a barrier after each exchange's reads as well)
+// and two CTAs of TX N/8 threads per SM: wide tiles at half the shared
+// memory of two slots.
+template <int TH, bool SLOT1>
+constexpr int col_minb() { return SLOT1 ? (2048 / TH > 0 ? 2048 / TH : 1) : min_blocks(TH); }
+template <typename T, int LOGN, int TX, int DIR, bool SLOT1 = false>
+__global__ void __launch_bounds__(TX * (1 << LOGN) / 8,
+                                  col_minb<TX * (1 << LOGN) / 8, SLOT1>())
 kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ tw,
        T scale) {
   using C = cplx<T>;
@@ -393,7 +399,7 @@ kf_col(const cplx<T>* in, cplx<T>* out, ColArgs a, const cplx<T>* __restrict__ t
     v[r] = (valid && kept(p, P::N, a.kc_in)) ? in[base + p * a.es] : mk<C>(0, 0);
   }
   const SwzView<C, TX> acc{buf, c};
-  run<DIR, LOGN, false, P::N * TX>(v, jt, true, acc, tw, 1);  // two exchange slots
+  run<DIR, LOGN, false, SLOT1 ? 0 : P::N * TX>(v, jt, true, acc, tw, 1);  // exchange slots
   if (!valid) return;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {

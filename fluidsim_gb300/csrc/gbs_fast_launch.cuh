@@ -11,11 +11,10 @@ namespace fast {
 
 // columns per CTA for the strided passes (FP64: 4, 64 B segments); FP32
 // widths per pass are compile-time knobs, set by A/B at 512^3 (ms per pruned
-// launch): the plain column kernel 8 (16: inverse y 0.94 -> 1.11, and the
-// z passes of the standalone FFT 0.80 -> 0.85 ms per transform), the fused
-// z passes of the ns3d step 16 (128 B segments of lines 1 MB apart: curl +
-// inverse z 0.779 -> 0.756, forward z + RK4 0.843 -> 0.758; 4: 1.146 and
-// 1.281)
+// launch): the ns2d column passes GBS_TX_COL = 8, the plain column kernel
+// below (col_launch), the fused z passes of the ns3d step 16 (128 B
+// segments of lines 1 MB apart: curl + inverse z 0.779 -> 0.756, forward z
+// + RK4 0.843 -> 0.758; 4: 1.146 and 1.281)
 #ifndef GBS_TX_COL
 #define GBS_TX_COL 8
 #endif
@@ -97,26 +96,43 @@ static int prefetch_distance(K kernel, int threads, size_t smem) {
       return GBS_EINVAL;                              \
   }
 
-template <typename T, int LOGN, int DIR>
+// Plain column passes (FP32): GBS_TX_COLY columns for row-strided lines
+// (y passes), GBS_TX_COLZ for plane-strided ones (lines >= 64 KB apart: z
+// passes of the standalone FFT).  Tiles of 16 columns (128-byte row
+// segments) take one exchange slot, so that two CTAs of 1024 threads (32
+// registers) fit; 8 columns take two slots.  Measured at 512^3 (ms per
+// pruned launch, 8 -> 16 columns): inverse y 0.942 -> 0.930, forward y
+// 0.500 -> 0.452; standalone R2C + C2R 0.803 -> 0.748 ms each (16 columns
+// with two slots: inverse y 1.11, one CTA per SM); steps/s +3 % at 256^3,
+// +4 % at 128^3, but -1.5 % at 64^3: lines shorter than 128 points keep 8.
+#ifndef GBS_TX_COLY
+#define GBS_TX_COLY 16
+#endif
+#ifndef GBS_TX_COLZ
+#define GBS_TX_COLZ 16
+#endif
+template <typename T, int LOGN, int DIR, bool PLANE>
 static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, int nfields,
                       const void* tw, double scale, cudaStream_t st) {
   using C = cplx<T>;
-  constexpr int TX = tx_cols<T, LOGN>();
+  constexpr int TX = sizeof(T) != 4 ? tx_cols<T, LOGN>()
+                     : (LOGN < 7 ? 8 : tx_cap(PLANE ? GBS_TX_COLZ : GBS_TX_COLY, LOGN));
+  constexpr bool SLOT1 = sizeof(T) == 4 && TX > 8;
   constexpr int TH = TX * (1 << LOGN) / 8;
-  const size_t smem = 2 * sizeof(C) * (size_t)(1 << LOGN) * TX;  // two exchange slots
-  int rc = prep(kf_col<T, LOGN, TX, DIR>, smem);
+  const size_t smem = (SLOT1 ? 1 : 2) * sizeof(C) * (size_t)(1 << LOGN) * TX;
+  int rc = prep(kf_col<T, LOGN, TX, DIR, SLOT1>, smem);
   if (rc) return rc;
-  static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR>, TH, smem);
+  static const int pf = prefetch_distance(kf_col<T, LOGN, TX, DIR, SLOT1>, TH, smem);
   ColArgs ap = a;
   dim3 grid(ceil_div(a.ncols, TX), nouter, nfields);
   // in grid rows (a resident wave of CTAs, rounded up); only for
   // row-strided columns (y passes): with plane strides (z passes) the next
   // wave's tiles span every plane
   const int dy = (int)((pf + grid.x - 1) / grid.x);
-  ap.pf = (a.es * (int64_t)sizeof(C) <= 65536 && dy < (int)grid.y) ? dy : 0;
-  kf_col<T, LOGN, TX, DIR><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
-                                                 static_cast<C*>(out), ap,
-                                                 static_cast<const C*>(tw), T(scale));
+  ap.pf = (!PLANE && dy < (int)grid.y) ? dy : 0;
+  kf_col<T, LOGN, TX, DIR, SLOT1><<<grid, TH, smem, st>>>(static_cast<const C*>(in),
+                                                        static_cast<C*>(out), ap,
+                                                        static_cast<const C*>(tw), T(scale));
   GBS_CHECK_LAUNCH();
   return GBS_OK;
 }
@@ -125,10 +141,15 @@ template <typename T>
 int col(int n, const void* in, void* out, const ColArgs& a, int nouter, int nfields,
         const void* tw, double scale, int dir, cudaStream_t st) {
   const int lg = ilog2(n);
-  if (dir > 0) {
-    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, 1>(in, out, a, nouter, nfields, tw, scale, st)));
+  const bool plane = a.es * (int64_t)sizeof(cplx<T>) > 65536;
+  if (dir > 0 && plane) {
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, 1, true>(in, out, a, nouter, nfields, tw, scale, st)));
+  } else if (dir > 0) {
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, 1, false>(in, out, a, nouter, nfields, tw, scale, st)));
+  } else if (plane) {
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, -1, true>(in, out, a, nouter, nfields, tw, scale, st)));
   } else {
-    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, -1>(in, out, a, nouter, nfields, tw, scale, st)));
+    GBS_LOG_SWITCH(lg, return (col_launch<T, LG, -1, false>(in, out, a, nouter, nfields, tw, scale, st)));
   }
   return GBS_OK;
 }
