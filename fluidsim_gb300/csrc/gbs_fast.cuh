@@ -867,7 +867,7 @@ kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
 // p, opaque to the compiler from here on: loads through the result are
 // neither merged with loads through earlier copies nor moved above the
 // volatile asm statements (barriers) that precede this one.  Keeps the
-// per-field loads and stage twiddles of kf3_xr from being hoisted and held
+// stage twiddles of kf3_xr from being computed once and held in registers
 // across all nine transforms.
 template <typename X>
 __device__ __forceinline__ const X* opaque(const X* p) {
@@ -896,6 +896,8 @@ __device__ __forceinline__ constexpr int inv_outm(int r) {
   return i;
 }
 
+// kf3_xr: CTAs of GBS_XR_THREADS threads per SM (2: 128 registers; 3 fits
+// 80 and spills 184-316 bytes)
 #ifndef GBS_XR_MINB
 #define GBS_XR_MINB 2
 #endif
