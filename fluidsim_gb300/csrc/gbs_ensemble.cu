@@ -244,7 +244,24 @@ struct PersistArgs {
   unsigned long long timeout_ns;
   int stall_test;         // test hook: one dependency needs an item too many
   int chunk;              // tickets a CTA takes at a time
+  int tpi[3];             // tiles per work item of each pass (grp[].cta*: items per run)
+  int tiles[kMixMax][3];  // tiles per run of each pass
 };
+
+// tiles per work item of the persistent step's passes: the x pass's tiles
+// (a few rows) are small next to an item's fixed costs (ticket, decode,
+// dependency check, two CTA barriers).  96-run C4 ensemble, ms per step:
+// x-pass tiles per item 1: 0.787, 4: 0.731, 8: 0.728; two column tiles
+// per item as well: 0.838.
+#ifndef GBS_PERSIST_TPI_A
+#define GBS_PERSIST_TPI_A 1
+#endif
+#ifndef GBS_PERSIST_TPI_B
+#define GBS_PERSIST_TPI_B 8
+#endif
+#ifndef GBS_PERSIST_TPI_C
+#define GBS_PERSIST_TPI_C 1
+#endif
 
 constexpr int kPersistTimeout = 1;
 
@@ -341,7 +358,7 @@ __global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_cons
     const int gi = persist_group(p, pass, r);
     const MixGroup& G = p.grp[gi];
     const int per = pass == 0 ? G.ctaA : (pass == 1 ? G.ctaB : G.ctaC);
-    const int run = (int)(r / per), tile = (int)(r % per);
+    const int run = (int)(r / per), item = (int)(r % per);
     unsigned* cnt = p.done + 3 * (int64_t)(p.run_base[gi] + run);
     if (threadIdx.x == 0) {
       unsigned target = 0;
@@ -372,37 +389,43 @@ __global__ void __launch_bounds__(TH, min_blocks(TH)) kpersist(const __grid_cons
     const int mode = kRK0 + (sigma & 3);
     RKArgs a = G.a;
     const float2* in = static_cast<const float2*>(mode == kRK0 ? a.S : a.tmp1);
-    if (pass == 0) {
-      const uint3 b = make_uint3(tile, 0, run);
-      float2* W = static_cast<float2*>(G.W);
-      const float2* tw = static_cast<const float2*>(G.twy);
-      switch (G.logy) {
-        case 6: kf2_inv_y_body<float, 6, MixTX<TH, 6>::v, false>(in, W, G.g, tw, b); break;
-        case 7: kf2_inv_y_body<float, 7, MixTX<TH, 7>::v, false>(in, W, G.g, tw, b); break;
-        case 8: kf2_inv_y_body<float, 8, MixTX<TH, 8>::v, false>(in, W, G.g, tw, b); break;
-        default: kf2_inv_y_body<float, 9, MixTX<TH, 9>::v, false>(in, W, G.g, tw, b); break;
-      }
-    } else if (pass == 1) {
-      const uint3 b = make_uint3(tile, run, 0);
-      const float2* W = static_cast<const float2*>(G.W);
-      float2* F = static_cast<float2*>(G.F);
-      const float2* tw = static_cast<const float2*>(G.twx);
-      switch (G.logm) {
-        case 5: kf2_x_any<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
-        case 6: kf2_x_any<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
-        case 7: kf2_x_any<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
-        case 8: kf2_x_any<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
-        default: kf2_x_any<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
-      }
-    } else {
-      const uint3 b = make_uint3(tile, 0, run);
-      const float2* F = static_cast<const float2*>(G.F);
-      const float2* tw = static_cast<const float2*>(G.twy);
-      switch (G.logy) {
-        case 6: kf2_fwd_y_body<float, 6, MixTX<TH, 6>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
-        case 7: kf2_fwd_y_body<float, 7, MixTX<TH, 7>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
-        case 8: kf2_fwd_y_body<float, 8, MixTX<TH, 8>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
-        default: kf2_fwd_y_body<float, 9, MixTX<TH, 9>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+    const int tpi = p.tpi[pass], ntile = p.tiles[gi][pass];
+    for (int sub = 0; sub < tpi; ++sub) {
+      const int tile = item * tpi + sub;
+      if (tile >= ntile) break;
+      if (sub) __syncthreads();  // the previous tile's shared memory is free
+      if (pass == 0) {
+        const uint3 b = make_uint3(tile, 0, run);
+        float2* W = static_cast<float2*>(G.W);
+        const float2* tw = static_cast<const float2*>(G.twy);
+        switch (G.logy) {
+          case 6: kf2_inv_y_body<float, 6, MixTX<TH, 6>::v, false>(in, W, G.g, tw, b); break;
+          case 7: kf2_inv_y_body<float, 7, MixTX<TH, 7>::v, false>(in, W, G.g, tw, b); break;
+          case 8: kf2_inv_y_body<float, 8, MixTX<TH, 8>::v, false>(in, W, G.g, tw, b); break;
+          default: kf2_inv_y_body<float, 9, MixTX<TH, 9>::v, false>(in, W, G.g, tw, b); break;
+        }
+      } else if (pass == 1) {
+        const uint3 b = make_uint3(tile, run, 0);
+        const float2* W = static_cast<const float2*>(G.W);
+        float2* F = static_cast<float2*>(G.F);
+        const float2* tw = static_cast<const float2*>(G.twx);
+        switch (G.logm) {
+          case 5: kf2_x_any<float, 5, MixRows<TH, 5>::v>(W, F, G.g, tw, nullptr, b); break;
+          case 6: kf2_x_any<float, 6, MixRows<TH, 6>::v>(W, F, G.g, tw, nullptr, b); break;
+          case 7: kf2_x_any<float, 7, MixRows<TH, 7>::v>(W, F, G.g, tw, nullptr, b); break;
+          case 8: kf2_x_any<float, 8, MixRows<TH, 8>::v>(W, F, G.g, tw, nullptr, b); break;
+          default: kf2_x_any<float, 9, MixRows<TH, 9>::v>(W, F, G.g, tw, nullptr, b); break;
+        }
+      } else {
+        const uint3 b = make_uint3(tile, 0, run);
+        const float2* F = static_cast<const float2*>(G.F);
+        const float2* tw = static_cast<const float2*>(G.twy);
+        switch (G.logy) {
+          case 6: kf2_fwd_y_body<float, 6, MixTX<TH, 6>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+          case 7: kf2_fwd_y_body<float, 7, MixTX<TH, 7>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+          case 8: kf2_fwd_y_body<float, 8, MixTX<TH, 8>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+          default: kf2_fwd_y_body<float, 9, MixTX<TH, 9>::v, false>(F, G.g, tw, mode, a, G.pr, b); break;
+        }
       }
     }
     __syncthreads();  // the item's writes are done (and its shared memory free)
@@ -535,6 +558,9 @@ static int persist_launch(EnsembleMix* x, void* const* states, int nsteps,
   memset(&p, 0, sizeof(p));
   p.ngroups = x->n;
   p.nstages = 4 * nsteps;
+  p.tpi[0] = GBS_PERSIST_TPI_A;
+  p.tpi[1] = GBS_PERSIST_TPI_B;
+  p.tpi[2] = GBS_PERSIST_TPI_C;
   int rb = 0;
   for (int k = 0; k < x->n; ++k) {
     Ensemble* e = x->e[k];
@@ -554,9 +580,13 @@ static int persist_launch(EnsembleMix* x, void* const* states, int nsteps,
     G.pr = fast::PerRun{e->nu2, e->nu8, e->dt};
     G.logy = ilog2(e->ny);
     G.logm = ilog2(e->nx / 2);
-    G.ctaA = ceil_div(G.g.ncx, TH * 8 / e->ny);
-    G.ctaB = ceil_div(e->ny, 2 * TH / (e->nx / 2));
-    G.ctaC = G.ctaA;
+    // tiles per run of each pass, then work items per run
+    p.tiles[k][0] = ceil_div(G.g.ncx, TH * 8 / e->ny);
+    p.tiles[k][1] = ceil_div(e->ny, 2 * TH / (e->nx / 2));
+    p.tiles[k][2] = p.tiles[k][0];
+    G.ctaA = ceil_div(p.tiles[k][0], p.tpi[0]);
+    G.ctaB = ceil_div(p.tiles[k][1], p.tpi[1]);
+    G.ctaC = ceil_div(p.tiles[k][2], p.tpi[2]);
     p.runs[k] = e->nruns;
     p.run_base[k] = rb;
     rb += e->nruns;
