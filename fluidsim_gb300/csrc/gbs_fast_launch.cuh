@@ -61,9 +61,12 @@ static int prep(K kernel, size_t smem) {
 }
 
 // L2 prefetch distance of the plain column passes: the CTAs resident on the
-// whole GPU (x GBS_PF from the environment, default 1; 0 turns it off).
+// whole GPU (x GBS_PF from the environment, default 0.5; 0 turns it off).
 // (Measured at 512^3 FP32: inverse y -9 %, forward y -15 %; the same
-// prefetch slowed the curl / x / forward-z kernels, which do not use it.)
+// prefetch slowed the curl / x / forward-z kernels, which do not use it.
+// With the 16-column tiles, ms per pruned launch inverse / forward y:
+// GBS_PF 0: 1.076 / 0.566, 0.5: 0.905 / 0.447, 1: 0.920 / 0.452, 2: 1.026 /
+// 0.587.)
 static double env_knob(const char* name, double dflt) {
   const char* e = getenv(name);
   return e && *e ? atof(e) : dflt;
@@ -71,7 +74,7 @@ static double env_knob(const char* name, double dflt) {
 
 template <typename K>
 static int prefetch_distance(K kernel, int threads, size_t smem) {
-  static const double scale = env_knob("GBS_PF", 1.0);
+  static const double scale = env_knob("GBS_PF", 0.5);
   int nb = 0, dev = 0, nsm = 0;
   if (scale <= 0) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess ||
