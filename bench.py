@@ -11,7 +11,7 @@ so no explicit L2 flush is needed between steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU
-(the spec path has no data-path exchange); value = steps of all ranks
+(one simulation per GPU: no data-path exchange); value = steps of all ranks
 divided by the slowest rank's time.  The reference arm times whole RK4
 steps of the CPU restatement of the reference algorithm (float64, scipy.fft
 and slab-parallel numpy on all host cores) on the same workload, honouring
