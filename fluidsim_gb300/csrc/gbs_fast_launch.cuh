@@ -120,7 +120,8 @@ static int col_launch(const void* in, void* out, const ColArgs& a, int nouter, i
   using C = cplx<T>;
   constexpr int TX = sizeof(T) != 4 ? tx_cols<T, LOGN>()
                      : (LOGN < 7 ? 8 : tx_cap(PLANE ? GBS_TX_COLZ : GBS_TX_COLY, LOGN));
-  constexpr bool SLOT1 = sizeof(T) == 4 && TX > 8;
+  // one slot when two would hold 128 KB or more (16 columns of 512, 8 of 1024)
+  constexpr bool SLOT1 = sizeof(T) == 4 && (TX > 8 || TX * (1 << LOGN) >= 8192);
   constexpr int TH = TX * (1 << LOGN) / 8;
   const size_t smem = (SLOT1 ? 1 : 2) * sizeof(C) * (size_t)(1 << LOGN) * TX;
   int rc = prep(kf_col<T, LOGN, TX, DIR, SLOT1>, smem);

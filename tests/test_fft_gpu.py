@@ -8,7 +8,9 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(16, 16), (40, 48), (15, 20), (256, 256), (8, 12, 10), (10, 15, 20),
           (32, 32, 32), (64, 48, 40), (128, 128, 128), (4, 6, 2), (1, 8, 8),
           # the 512-point column and row kernels of the 512^3 benchmark step
-          (512, 512), (512, 512, 16), (16, 16, 512), (512, 512, 512)]
+          (512, 512), (512, 512, 16), (16, 16, 512), (512, 512, 512),
+          # 1024-point columns (one exchange slot)
+          (1024, 64), (1024, 64, 32), (32, 1024, 64)]
 TOL = {"float64": 1e-13, "float32": 3e-6}
 
 
