@@ -51,7 +51,7 @@ struct Line {
   static constexpr int NST = S8 + (REM ? 1 : 0);
   static constexpr int RL = REM == 0 ? 8 : (1 << REM);
   // register idx -> output position jt + outm(idx) * N8 after the last stage
-  static __device__ __forceinline__ constexpr int outm(int idx) {
+  static __host__ __device__ __forceinline__ constexpr int outm(int idx) {
     return REM == 0 ? idx : (idx / RL) + (idx % RL) * (8 / RL);
   }
 };
@@ -66,7 +66,7 @@ struct Line {
 // second-stage writes of the rows: 2.8x the bank conflicts of x ^ (x << 1)
 // in the x pass at 512^2 x 64 (7.3 M against 2.6 M), 2.3 % slower.
 template <typename C>
-__device__ __forceinline__ int swz(int q) {
+__host__ __device__ __forceinline__ int swz(int q) {
   constexpr int E = 128 / sizeof(C);
   constexpr int LG = E == 16 ? 4 : 3;
 #ifdef GBS_SWZ_XOR1
@@ -86,7 +86,7 @@ __device__ __forceinline__ int swz(int q) {
 // XOR with a constant below E plus an immediate offset, instead of forming q
 // and its swizzle again for every access.
 template <typename C>
-__device__ __forceinline__ int swz_join(int sb, int K) {
+__host__ __device__ __forceinline__ int swz_join(int sb, int K) {
   constexpr int E = 128 / sizeof(C);
   const int sK = swz<C>(K);
   return (sb ^ (sK & (E - 1))) + (sK & ~(E - 1));
@@ -890,7 +890,7 @@ __host__ __device__ constexpr int xr_slot() {
 // Register index holding stage-0 position jt + r N/8 in the output order of
 // run(): the i with Line::outm(i) == r.
 template <int LOGN>
-__device__ __forceinline__ constexpr int inv_outm(int r) {
+__host__ __device__ __forceinline__ constexpr int inv_outm(int r) {
   int i = 0;
   while (Line<LOGN>::outm(i) != r) ++i;
   return i;
