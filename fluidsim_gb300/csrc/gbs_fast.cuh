@@ -788,9 +788,11 @@ __host__ __device__ constexpr bool xp_alt() { return Line<LOGN>::NST == 3; }
 // No pre- or post-processing twiddles (the half-length real transforms of
 // kf3_x spend about as many instructions on those as on a radix-8 stage).
 // LP row pairs per CTA; N/8 threads per line.
+// (FP64: one CTA per SM, so that the lines fit in registers)
 template <typename T, int LOGN, int LP, bool ST>
 __global__ void __launch_bounds__((ST ? 7 : 6) * LP * (1 << LOGN) / 8,
-                                  min_blocks((ST ? 7 : 6) * LP * (1 << LOGN) / 8))
+                                  sizeof(T) == 8 ? 1
+                                                 : min_blocks((ST ? 7 : 6) * LP * (1 << LOGN) / 8))
 kf3_xp(const cplx<T>* __restrict__ W, cplx<T>* __restrict__ F, Geo g,
        const cplx<T>* __restrict__ twx, unsigned long long* vmax) {
   using C = cplx<T>;

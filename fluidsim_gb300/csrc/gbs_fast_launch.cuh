@@ -247,8 +247,8 @@ static int B3_launch(const Geo& g, const void* W, void* F, const void* tw,
   return GBS_OK;
 }
 
-// Rows in pairs (kf3_xp): FP32 for nx <= 1024 (one CTA of <= 1024 threads
-// holds the NF lines of a pair), LP pairs per CTA up to GBS_X_THREADS threads.
+// Rows in pairs (kf3_xp): nx <= 1024 (one CTA of <= 1024 threads holds the
+// NF lines of a pair), LP pairs per CTA up to GBS_X_THREADS threads.
 // (512^3 FP32: 1.81 -> 1.55 ms against kf3_x's half-length real transforms.)
 template <typename T, int LOGM, bool ST>
 static int B3p_launch(const Geo& g, const void* W, void* F, const void* tw,
@@ -306,7 +306,10 @@ static int B3_pick(const Geo& g, const void* W, void* F, const void* tw,
   if constexpr (sizeof(T) == 4 && !ST && LOGM >= GBS_XR_LOGM_MIN && LOGM <= GBS_XR_LOGM_MAX)
     if (((int64_t)g.nz * g.ny) % 2 == 0) return B3r_launch<T, LOGM>(g, W, F, tw, vmax, xs, st);
 #endif
-  if constexpr (sizeof(T) == 4 && LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
+  // FP64 takes the paired form too, at one CTA per SM (up to 168
+  // registers): the half-length form's FP64 instantiations spill 400-1700
+  // bytes at their 40 registers (512^3 FP64 3.20 -> 3.34 steps/s)
+  if constexpr (LOGM <= 9) return B3p_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
   else return B3_launch<T, LOGM, ST>(g, W, F, tw, vmax, st);
 }
 
